@@ -1,0 +1,433 @@
+// rt_api.cu — the C ABI declared in include/rtcore.h.
+//
+// Argument validation happens here, on the host, before anything is queued:
+// a bad size, alignment or index returns RT_ERR_INVALID / RT_ERR_TOO_LARGE
+// with a message in rt_last_error_string() and launches nothing.  Errors the
+// device finds (a stack overflow, an out-of-range vertex index) are recorded
+// in the AS header's status word or the context's statistics block.
+#include <atomic>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#include "rt_internal.h"
+
+using namespace rt;
+
+namespace {
+
+constexpr uint32_t kWorkSlots = 256;
+
+struct CtxDevice {
+    RtStats stats;
+    uint32_t work[kWorkSlots];
+};
+
+thread_local std::string g_last_error;
+std::atomic<unsigned long long> g_kernel_launches{0};
+
+int32_t fail(int32_t code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return code;
+}
+
+int32_t cuda_fail(cudaError_t e, const char* what) {
+    return fail(e == cudaErrorMemoryAllocation ? RT_ERR_OOM : RT_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+bool aligned(uint64_t a, uint64_t n) { return (a % n) == 0; }
+
+RtShaderBindingTable reference_sbt() {
+    // src/main.rs:289-305: hit groups {any-hit 3, closest-hit 4 | 5 | 6}
+    RtShaderBindingTable s;
+    memset(&s, 0, sizeof s);
+    s.hit_group_count = 3;
+    s.hit_groups[0].closest_hit = RT_PROGRAM_CLOSEST_HIT_TEXTURED;
+    s.hit_groups[1].closest_hit = RT_PROGRAM_CLOSEST_HIT_MIRROR;
+    s.hit_groups[2].closest_hit = RT_PROGRAM_CLOSEST_HIT_PORTAL;
+    for (int i = 0; i < 3; i++) s.hit_groups[i].any_hit = RT_PROGRAM_ANY_HIT_ALPHA_CLIP;
+    return s;
+}
+
+int32_t check_sbt(const RtShaderBindingTable* sbt) {
+    if (sbt->hit_group_count > RT_MAX_HIT_GROUPS)
+        return fail(RT_ERR_INVALID, "hit_group_count %u > %u", sbt->hit_group_count, RT_MAX_HIT_GROUPS);
+    for (uint32_t i = 0; i < sbt->hit_group_count; i++) {
+        if (sbt->hit_groups[i].closest_hit > RT_PROGRAM_CLOSEST_HIT_PORTAL)
+            return fail(RT_ERR_INVALID, "hit group %u: unknown closest-hit program %u", i, sbt->hit_groups[i].closest_hit);
+        if (sbt->hit_groups[i].any_hit > RT_PROGRAM_ANY_HIT_ALPHA_CLIP)
+            return fail(RT_ERR_INVALID, "hit group %u: unknown any-hit program %u", i, sbt->hit_groups[i].any_hit);
+    }
+    return RT_OK;
+}
+
+}  // namespace
+
+void rt::note_launch() { g_kernel_launches.fetch_add(1, std::memory_order_relaxed); }
+
+struct rt_ctx {
+    uint32_t flags = 0;
+    int device = 0;
+    int num_sms = 1;
+    RtTextureDesc textures[RT_MAX_BOUND_IMAGES];
+    CtxDevice* dev = nullptr;
+    std::atomic<uint32_t> work_slot{0};
+    std::mutex mu;
+};
+
+namespace {
+struct MaybeLock {
+    std::unique_lock<std::mutex> lk;
+    explicit MaybeLock(rt_ctx* c) {
+        if (c && (c->flags & RT_CTX_THREADSAFE)) lk = std::unique_lock<std::mutex>(c->mu);
+    }
+};
+}  // namespace
+
+extern "C" {
+
+RTCORE_API const char* rt_last_error_string(void) { return g_last_error.c_str(); }
+
+RTCORE_API const char* rt_version_string(void) { return "rtcore-gb300 0.1 (sm_103a)"; }
+
+RTCORE_API uint64_t rt_kernel_launch_count(void) { return g_kernel_launches.load(std::memory_order_relaxed); }
+
+RTCORE_API int32_t rt_ctx_create(uint32_t flags, rt_ctx** out) {
+    if (!out) return fail(RT_ERR_INVALID, "out is NULL");
+    *out = nullptr;
+    if (flags & ~RT_CTX_THREADSAFE) return fail(RT_ERR_INVALID, "unknown context flags 0x%x", flags);
+    rt_ctx* c = new (std::nothrow) rt_ctx();
+    if (!c) return fail(RT_ERR_OOM, "context allocation failed");
+    c->flags = flags;
+    memset(c->textures, 0, sizeof c->textures);
+    cudaError_t e = cudaGetDevice(&c->device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->device);
+    if (e == cudaSuccess) e = cudaMalloc(&c->dev, sizeof(CtxDevice));
+    if (e == cudaSuccess) e = cudaMemset(c->dev, 0, sizeof(CtxDevice));
+    if (e == cudaSuccess) e = upload_srgb_table();
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) {
+        if (c->dev) cudaFree(c->dev);
+        delete c;
+        return cuda_fail(e, "rt_ctx_create");
+    }
+    *out = c;
+    return RT_OK;
+}
+
+RTCORE_API int32_t rt_ctx_destroy(rt_ctx* ctx) {
+    if (!ctx) return RT_OK;
+    if (ctx->dev) cudaFree(ctx->dev);
+    delete ctx;
+    return RT_OK;
+}
+
+RTCORE_API int32_t rt_ctx_set_texture(rt_ctx* ctx, uint32_t index, const RtTextureDesc* desc) {
+    if (!ctx || !desc) return fail(RT_ERR_INVALID, "ctx or desc is NULL");
+    if (index >= RT_MAX_BOUND_IMAGES) return fail(RT_ERR_INVALID, "texture index %u >= %u", index, RT_MAX_BOUND_IMAGES);
+    if (desc->address != 0) {
+        uint32_t texel = 0;
+        if (desc->format == RT_FORMAT_R8G8B8A8_UNORM || desc->format == RT_FORMAT_R8G8B8A8_SRGB) texel = 4;
+        else if (desc->format == RT_FORMAT_R32G32B32A32_SFLOAT) texel = 16;
+        else return fail(RT_ERR_UNSUPPORTED, "texture format %u", desc->format);
+        if (desc->filter > RT_FILTER_LINEAR) return fail(RT_ERR_INVALID, "texture filter %u", desc->filter);
+        if (desc->width == 0 || desc->height == 0) return fail(RT_ERR_INVALID, "empty texture");
+        if ((uint64_t)desc->row_pitch < (uint64_t)desc->width * texel)
+            return fail(RT_ERR_INVALID, "row_pitch %u < width*%u", desc->row_pitch, texel);
+        if (!aligned(desc->address, texel) || !aligned(desc->row_pitch, texel))
+            return fail(RT_ERR_INVALID, "texture address/pitch not %u-byte aligned", texel);
+    }
+    MaybeLock l(ctx);
+    ctx->textures[index] = *desc;
+    return RT_OK;
+}
+
+RTCORE_API int32_t rt_ctx_read_stats(rt_ctx* ctx, RtStats* out, int32_t reset, void* stream) {
+    if (!ctx || !out) return fail(RT_ERR_INVALID, "ctx or out is NULL");
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    cudaError_t e = cudaStreamSynchronize(s);
+    if (e == cudaSuccess) e = cudaMemcpy(out, &ctx->dev->stats, sizeof(RtStats), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && reset) e = cudaMemset(&ctx->dev->stats, 0, sizeof(RtStats));
+    if (e != cudaSuccess) return cuda_fail(e, "rt_ctx_read_stats");
+    return RT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Acceleration structures
+// ---------------------------------------------------------------------------
+static int32_t blas_prim_count(const RtGeometryTriangles* g, uint32_t count, uint32_t* n_out) {
+    if (count > RT_MAX_BLAS_GEOMETRIES)
+        return fail(RT_ERR_TOO_LARGE, "geometry_count %u > %u", count, RT_MAX_BLAS_GEOMETRIES);
+    if (count > 0 && !g) return fail(RT_ERR_INVALID, "geometries is NULL");
+    uint64_t n = 0;
+    for (uint32_t i = 0; i < count; i++) {
+        if (g[i].primitive_count > 0) {
+            if (g[i].vertex_address == 0) return fail(RT_ERR_INVALID, "geometry %u: vertex_address is 0", i);
+            if (g[i].vertex_stride < 12 || (g[i].vertex_stride % 4) != 0)
+                return fail(RT_ERR_INVALID, "geometry %u: vertex_stride %u (need >= 12, multiple of 4)", i,
+                            g[i].vertex_stride);
+            if (!aligned(g[i].vertex_address, 4) || !aligned(g[i].index_address, 4))
+                return fail(RT_ERR_INVALID, "geometry %u: buffers must be 4-byte aligned", i);
+        }
+        n += g[i].primitive_count;
+    }
+    if (n > kMaxPrimitives) return fail(RT_ERR_TOO_LARGE, "%llu triangles > %u", (unsigned long long)n, kMaxPrimitives);
+    *n_out = (uint32_t)n;
+    return RT_OK;
+}
+
+RTCORE_API int32_t rt_get_blas_build_sizes(const RtGeometryTriangles* geometries, uint32_t geometry_count,
+                                           uint32_t build_flags, RtBuildSizes* out) {
+    if (!out) return fail(RT_ERR_INVALID, "out is NULL");
+    (void)build_flags;
+    uint32_t n = 0;
+    int32_t r = blas_prim_count(geometries, geometry_count, &n);
+    if (r) return r;
+    AsLayout al = AsLayout::make(n, false);
+    ScratchLayout sl = ScratchLayout::make(n, false);
+    out->acceleration_structure_size = al.total;
+    out->build_scratch_size = sl.build_total;
+    out->update_scratch_size = sl.update_total;
+    return RT_OK;
+}
+
+RTCORE_API int32_t rt_cmd_build_blas(rt_ctx* ctx, const RtGeometryTriangles* geometries, uint32_t geometry_count,
+                                     uint32_t build_flags, uint64_t dst, uint64_t dst_size, uint64_t scratch,
+                                     uint64_t scratch_size, void* stream) {
+    MaybeLock l(ctx);
+    uint32_t n = 0;
+    int32_t r = blas_prim_count(geometries, geometry_count, &n);
+    if (r) return r;
+    if (build_flags & RT_BUILD_QUANTIZED_NODES)
+        return fail(RT_ERR_UNSUPPORTED, "RT_BUILD_QUANTIZED_NODES is not available in this build");
+    AsLayout al = AsLayout::make(n, false);
+    ScratchLayout sl = ScratchLayout::make(n, false);
+    if (!dst || !aligned(dst, RT_AS_ALIGNMENT)) return fail(RT_ERR_INVALID, "dst must be non-null and 256-byte aligned");
+    if (dst_size < al.total)
+        return fail(RT_ERR_INVALID, "dst_size %llu < required %llu", (unsigned long long)dst_size,
+                    (unsigned long long)al.total);
+    if (!scratch || !aligned(scratch, RT_AS_ALIGNMENT))
+        return fail(RT_ERR_INVALID, "scratch must be non-null and 256-byte aligned");
+    if (scratch_size < sl.build_total)
+        return fail(RT_ERR_INVALID, "scratch_size %llu < required %llu", (unsigned long long)scratch_size,
+                    (unsigned long long)sl.build_total);
+    BlasInput in;
+    memset(&in, 0, sizeof in);
+    in.geometry_count = geometry_count ? geometry_count : 1;
+    in.n = n;
+    uint32_t prefix = 0;
+    for (uint32_t i = 0; i < geometry_count; i++) {
+        in.g[i].pos = reinterpret_cast<const float*>(geometries[i].vertex_address);
+        in.g[i].idx = reinterpret_cast<const uint32_t*>(geometries[i].index_address);
+        in.g[i].stride_floats = geometries[i].vertex_stride / 4;
+        in.g[i].max_vertex = geometries[i].max_vertex;
+        in.g[i].prim_count = geometries[i].primitive_count;
+        in.g[i].flags = geometries[i].flags;
+        in.g[i].prefix = prefix;
+        prefix += geometries[i].primitive_count;
+    }
+    cudaError_t e = launch_blas_build(in, build_flags, reinterpret_cast<uint8_t*>(dst),
+                                      reinterpret_cast<uint8_t*>(scratch), reinterpret_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return cuda_fail(e, "rt_cmd_build_blas");
+    return RT_OK;
+}
+
+RTCORE_API int32_t rt_get_tlas_build_sizes(uint32_t instance_count, uint32_t build_flags, RtBuildSizes* out) {
+    if (!out) return fail(RT_ERR_INVALID, "out is NULL");
+    (void)build_flags;
+    if (instance_count > kMaxPrimitives) return fail(RT_ERR_TOO_LARGE, "%u instances > %u", instance_count, kMaxPrimitives);
+    AsLayout al = AsLayout::make(instance_count, true);
+    ScratchLayout sl = ScratchLayout::make(instance_count, true);
+    out->acceleration_structure_size = al.total;
+    out->build_scratch_size = sl.build_total;
+    out->update_scratch_size = sl.update_total;
+    return RT_OK;
+}
+
+RTCORE_API int32_t rt_cmd_build_tlas(rt_ctx* ctx, uint64_t instances, uint32_t instance_count, uint32_t build_flags,
+                                     uint64_t dst, uint64_t dst_size, uint64_t scratch, uint64_t scratch_size,
+                                     void* stream) {
+    MaybeLock l(ctx);
+    if (instance_count > kMaxPrimitives) return fail(RT_ERR_TOO_LARGE, "%u instances > %u", instance_count, kMaxPrimitives);
+    if (instance_count > 0 && (!instances || !aligned(instances, 16)))
+        return fail(RT_ERR_INVALID, "instances must be non-null and 16-byte aligned");
+    AsLayout al = AsLayout::make(instance_count, true);
+    ScratchLayout sl = ScratchLayout::make(instance_count, true);
+    if (!dst || !aligned(dst, RT_AS_ALIGNMENT)) return fail(RT_ERR_INVALID, "dst must be non-null and 256-byte aligned");
+    if (dst_size < al.total)
+        return fail(RT_ERR_INVALID, "dst_size %llu < required %llu", (unsigned long long)dst_size,
+                    (unsigned long long)al.total);
+    if (!scratch || !aligned(scratch, RT_AS_ALIGNMENT))
+        return fail(RT_ERR_INVALID, "scratch must be non-null and 256-byte aligned");
+    if (scratch_size < sl.build_total)
+        return fail(RT_ERR_INVALID, "scratch_size %llu < required %llu", (unsigned long long)scratch_size,
+                    (unsigned long long)sl.build_total);
+    cudaError_t e = launch_tlas_build(reinterpret_cast<const RtAccelerationStructureInstance*>(instances), instance_count,
+                                      build_flags, reinterpret_cast<uint8_t*>(dst), reinterpret_cast<uint8_t*>(scratch),
+                                      reinterpret_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return cuda_fail(e, "rt_cmd_build_tlas");
+    return RT_OK;
+}
+
+RTCORE_API int32_t rt_cmd_update_tlas(rt_ctx* ctx, uint64_t instances, uint32_t instance_count, uint64_t src,
+                                      uint64_t dst, uint64_t dst_size, uint64_t scratch, uint64_t scratch_size,
+                                      void* stream) {
+    MaybeLock l(ctx);
+    if (instance_count > kMaxPrimitives) return fail(RT_ERR_TOO_LARGE, "%u instances > %u", instance_count, kMaxPrimitives);
+    if (instance_count > 0 && (!instances || !aligned(instances, 16)))
+        return fail(RT_ERR_INVALID, "instances must be non-null and 16-byte aligned");
+    if (!src || !dst || !aligned(src, RT_AS_ALIGNMENT) || !aligned(dst, RT_AS_ALIGNMENT))
+        return fail(RT_ERR_INVALID, "src/dst must be non-null and 256-byte aligned");
+    AsLayout al = AsLayout::make(instance_count, true);
+    ScratchLayout sl = ScratchLayout::make(instance_count, true);
+    if (dst_size < al.total)
+        return fail(RT_ERR_INVALID, "dst_size %llu < required %llu", (unsigned long long)dst_size,
+                    (unsigned long long)al.total);
+    if (!scratch || !aligned(scratch, RT_AS_ALIGNMENT))
+        return fail(RT_ERR_INVALID, "scratch must be non-null and 256-byte aligned");
+    if (scratch_size < sl.update_total)
+        return fail(RT_ERR_INVALID, "scratch_size %llu < required %llu", (unsigned long long)scratch_size,
+                    (unsigned long long)sl.update_total);
+    cudaError_t e = launch_tlas_update(reinterpret_cast<const RtAccelerationStructureInstance*>(instances),
+                                       instance_count, reinterpret_cast<const uint8_t*>(src),
+                                       reinterpret_cast<uint8_t*>(dst), dst_size, reinterpret_cast<uint8_t*>(scratch),
+                                       reinterpret_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return cuda_fail(e, "rt_cmd_update_tlas");
+    return RT_OK;
+}
+
+RTCORE_API int32_t rt_cmd_copy_acceleration_structure(rt_ctx* ctx, uint64_t src, uint64_t dst, uint64_t dst_size,
+                                                      uint32_t mode, void* stream) {
+    MaybeLock l(ctx);
+    if (!src || !dst || !aligned(src, RT_AS_ALIGNMENT) || !aligned(dst, RT_AS_ALIGNMENT))
+        return fail(RT_ERR_INVALID, "src/dst must be non-null and 256-byte aligned");
+    if (src == dst) return fail(RT_ERR_INVALID, "src == dst");
+    if (mode != RT_COPY_MODE_CLONE && mode != RT_COPY_MODE_COMPACT) return fail(RT_ERR_INVALID, "copy mode %u", mode);
+    if (dst_size < kHeaderBytes) return fail(RT_ERR_INVALID, "dst_size %llu < header", (unsigned long long)dst_size);
+    cudaError_t e = launch_as_copy(reinterpret_cast<const uint8_t*>(src), reinterpret_cast<uint8_t*>(dst), dst_size,
+                                   mode, reinterpret_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return cuda_fail(e, "rt_cmd_copy_acceleration_structure");
+    return RT_OK;
+}
+
+RTCORE_API int32_t rt_get_acceleration_structure_info(uint64_t as, RtAccelerationStructureInfo* out, void* stream) {
+    if (!as || !out || !aligned(as, RT_AS_ALIGNMENT)) return fail(RT_ERR_INVALID, "bad AS address or out");
+    AsHeader h;
+    cudaError_t e = cudaStreamSynchronize(reinterpret_cast<cudaStream_t>(stream));
+    if (e == cudaSuccess) e = cudaMemcpy(&h, reinterpret_cast<const void*>(as), sizeof h, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(e, "rt_get_acceleration_structure_info");
+    if (h.magic != kAsMagic) return fail(RT_ERR_BAD_AS, "not an acceleration structure written by this library");
+    memset(out, 0, sizeof *out);
+    out->type = h.type;
+    out->build_flags = h.build_flags;
+    out->node_count = h.node_count;
+    out->primitive_count = h.prim_count;
+    out->node_bytes = h.node_bytes;
+    out->tree_depth = h.depth;
+    out->total_size = h.total_size;
+    out->compacted_size = h.compacted_size;
+    for (int k = 0; k < 3; k++) {
+        out->bounds_lo[k] = h.bounds_lo[k];
+        out->bounds_hi[k] = h.bounds_hi[k];
+    }
+    out->status = h.status;
+    return RT_OK;
+}
+
+RTCORE_API uint64_t rt_get_acceleration_structure_device_address(uint64_t as_memory) {
+    if (!aligned(as_memory, RT_AS_ALIGNMENT)) {
+        fail(RT_ERR_INVALID, "AS memory not 256-byte aligned");
+        return 0;
+    }
+    return as_memory;
+}
+
+// ---------------------------------------------------------------------------
+// Dispatch
+// ---------------------------------------------------------------------------
+RTCORE_API int32_t rt_cmd_trace_rays(rt_ctx* ctx, const RtPushConstantBufferAddresses* push,
+                                     const RtShaderBindingTable* sbt, const RtTraceRaysDesc* desc, void* stream) {
+    if (!ctx || !push || !desc) return fail(RT_ERR_INVALID, "ctx, push or desc is NULL");
+    if (!push->uniforms || !push->acceleration_structure)
+        return fail(RT_ERR_INVALID, "push constants need uniforms and acceleration_structure");
+    if (!aligned(push->acceleration_structure, RT_AS_ALIGNMENT) || !aligned(push->uniforms, 16) ||
+        !aligned(push->model_info, 8))
+        return fail(RT_ERR_INVALID, "misaligned push-constant address");
+    if (desc->width == 0 || desc->height == 0) return fail(RT_ERR_INVALID, "empty launch %ux%u", desc->width, desc->height);
+    if ((uint64_t)desc->width * desc->height > (1ull << 31))
+        return fail(RT_ERR_TOO_LARGE, "launch %ux%u too large", desc->width, desc->height);
+    if (desc->max_trace_depth == 0 || desc->max_trace_depth > 64)
+        return fail(RT_ERR_INVALID, "max_trace_depth %u (need 1..64)", desc->max_trace_depth);
+    if (desc->shadow_ray_count > 256) return fail(RT_ERR_INVALID, "shadow_ray_count %u > 256", desc->shadow_ray_count);
+    if (!desc->image_address && !desc->radiance_address) return fail(RT_ERR_INVALID, "no output buffer");
+    if (!aligned(desc->image_address, 4) || !aligned(desc->radiance_address, 16))
+        return fail(RT_ERR_INVALID, "misaligned output buffer");
+    RtShaderBindingTable table = sbt ? *sbt : reference_sbt();
+    int32_t r = check_sbt(&table);
+    if (r) return r;
+    MaybeLock l(ctx);
+    TraceLaunch p;
+    p.push = *push;
+    p.sbt = table;
+    p.desc = *desc;
+    memcpy(p.textures, ctx->textures, sizeof p.textures);
+    p.stats = &ctx->dev->stats;
+    p.status = &ctx->dev->stats.status;
+    p.work = &ctx->dev->work[ctx->work_slot.fetch_add(1) % kWorkSlots];
+    cudaError_t e = launch_trace_rays(p, ctx->num_sms, reinterpret_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return cuda_fail(e, "rt_cmd_trace_rays");
+    return RT_OK;
+}
+
+RTCORE_API int32_t rt_cmd_trace_ray_buffer(rt_ctx* ctx, uint64_t tlas, const RtPushConstantBufferAddresses* push,
+                                           const RtShaderBindingTable* sbt, uint32_t ray_flags, uint32_t cull_mask,
+                                           uint32_t sbt_offset, uint64_t rays, uint32_t ray_count, uint64_t hits,
+                                           void* stream) {
+    if (!ctx) return fail(RT_ERR_INVALID, "ctx is NULL");
+    if (!tlas || !aligned(tlas, RT_AS_ALIGNMENT)) return fail(RT_ERR_INVALID, "tlas must be non-null and 256-byte aligned");
+    if (ray_count > 0 && (!rays || !hits || !aligned(rays, 16) || !aligned(hits, 16)))
+        return fail(RT_ERR_INVALID, "rays/hits must be non-null and 16-byte aligned");
+    if (ray_flags & ~(0xFFu | RT_RAY_FLAG_EXT_COLLECT_STATS))
+        return fail(RT_ERR_INVALID, "unknown ray flags 0x%x", ray_flags);
+    RtShaderBindingTable table = sbt ? *sbt : reference_sbt();
+    int32_t r = check_sbt(&table);
+    if (r) return r;
+    MaybeLock l(ctx);
+    RayBufferLaunch p;
+    memset(&p.push, 0, sizeof p.push);
+    if (push) p.push = *push;
+    p.sbt = table;
+    memcpy(p.textures, ctx->textures, sizeof p.textures);
+    p.tlas = tlas;
+    p.rays = reinterpret_cast<const RtRay*>(rays);
+    p.hits = reinterpret_cast<RtHit*>(hits);
+    p.count = ray_count;
+    p.ray_flags = ray_flags & 0xFFu;
+    p.cull_mask = cull_mask & 0xFFu;
+    p.sbt_offset = sbt_offset;
+    p.collect_stats = (ray_flags & RT_RAY_FLAG_EXT_COLLECT_STATS) ? 1u : 0u;
+    p.stats = &ctx->dev->stats;
+    p.status = &ctx->dev->stats.status;
+    cudaError_t e = launch_trace_ray_buffer(p, ctx->num_sms, reinterpret_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return cuda_fail(e, "rt_cmd_trace_ray_buffer");
+    return RT_OK;
+}
+
+RTCORE_API int32_t rt_debug_eval(uint32_t function, uint64_t in, uint64_t out, uint32_t count, void* stream) {
+    if (function > RT_FN_WATERTIGHT) return fail(RT_ERR_INVALID, "unknown function %u", function);
+    if (count > 0 && (!in || !out || !aligned(in, 4) || !aligned(out, 4)))
+        return fail(RT_ERR_INVALID, "in/out must be non-null and 4-byte aligned");
+    cudaError_t e = launch_debug_eval(function, reinterpret_cast<const float*>(in), reinterpret_cast<float*>(out), count,
+                                      reinterpret_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return cuda_fail(e, "rt_debug_eval");
+    return RT_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,1140 @@
+// rt_build.cu — BLAS / TLAS construction, TLAS refit and AS copies.
+//
+// Build = LBVH (Karras 2012) collapsed to 8-wide nodes:
+//   1. primitive boxes (triangles, or instance world boxes) + centroid bounds
+//   2. 30-bit Morton codes of the centroids
+//   3. stable LSD radix sort, 8-bit digits, 4 passes (reduce-then-scan:
+//      per-tile digit histograms, one exclusive scan, stable scatter ranked
+//      with warp match_any)
+//   4. Karras hierarchy over the sorted codes (index-augmented for ties)
+//   5. bottom-up boxes with one arrival counter per internal node
+//   6. collapse to 8-wide nodes: a node takes its binary children and
+//      repeatedly opens the child of largest surface area until it has 8
+//      children or none can open; a subtree of <= leaf_max primitives is a
+//      leaf (a contiguous range of the sorted order).  The first kLevels
+//      wide levels run as one launch each, the rest as one depth-first task
+//      per thread.
+//   7. primitive records written in leaf order.
+// Everything runs on the caller's stream; no host synchronisation.
+//
+// Replaces vkCmdBuildAccelerationStructuresKHR as called by
+// AccelerationStructure::build_blas / new (src/util_structs.rs:140-283),
+// build_tlas (src/util_functions.rs:453-510) and update_tlas
+// (src/util_structs.rs:285-357), and vkCmdCopyAccelerationStructureKHR CLONE
+// (src/util_structs.rs:359-405).
+#include <algorithm>
+#include <cfloat>
+#include <cstring>
+
+#include "rt_internal.h"
+
+namespace rt {
+
+namespace {
+
+constexpr uint32_t kNone = 0xFFFFFFFFu;
+constexpr uint32_t kLeafBit = 0x80000000u;
+constexpr int kLevels = 6;                     // wide levels built breadth-first
+constexpr uint32_t kFrontierCap = 1u << 18;    // 8^kLevels
+constexpr int kTailStack = 192;
+constexpr int kSortThreads = 256;
+constexpr int kSortItems = 8;
+constexpr uint32_t kSortTile = kSortThreads * kSortItems;
+
+struct BuildState {
+    uint32_t cb[6];   // centroid bounds, ordered-uint encoding: min xyz, max xyz
+    uint32_t bb[6];   // primitive box bounds
+    uint32_t node_counter;
+    uint32_t frontier_count[kLevels + 2];
+    uint32_t error;
+    uint32_t depth;
+};
+
+__device__ __forceinline__ uint32_t f2o(float f) {
+    uint32_t u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float o2f(uint32_t u) {
+    return __uint_as_float((u & 0x80000000u) ? (u & 0x7FFFFFFFu) : ~u);
+}
+
+__device__ __forceinline__ void pad_box(float lo[3], float hi[3]) {
+    for (int k = 0; k < 3; k++) {
+        float m = fmaxf(fabsf(lo[k]), fabsf(hi[k]));
+        float pad = m * 9.5367431640625e-07f + 1e-30f;  // 2^-20 relative
+        lo[k] -= pad;
+        hi[k] += pad;
+    }
+}
+
+__device__ __forceinline__ bool finite3(const float v[3]) {
+    return fabsf(v[0]) <= FLT_MAX && fabsf(v[1]) <= FLT_MAX && fabsf(v[2]) <= FLT_MAX;
+}
+
+// Block-wide min/max reduction of 12 ordered-uint values, then atomics.
+__device__ void reduce_bounds(BuildState* st, const float cmin[3], const float cmax[3], const float bmin[3],
+                              const float bmax[3]) {
+    uint32_t v[12];
+    for (int k = 0; k < 3; k++) {
+        v[k] = f2o(cmin[k]);
+        v[3 + k] = f2o(cmax[k]);
+        v[6 + k] = f2o(bmin[k]);
+        v[9 + k] = f2o(bmax[k]);
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        for (int k = 0; k < 12; k++) {
+            uint32_t o = __shfl_xor_sync(0xFFFFFFFFu, v[k], off);
+            bool is_min = (k < 3) || (k >= 6 && k < 9);
+            v[k] = is_min ? min(v[k], o) : max(v[k], o);
+        }
+    }
+    if ((threadIdx.x & 31) == 0) {
+        for (int k = 0; k < 3; k++) {
+            atomicMin(&st->cb[k], v[k]);
+            atomicMax(&st->cb[3 + k], v[3 + k]);
+            atomicMin(&st->bb[k], v[6 + k]);
+            atomicMax(&st->bb[3 + k], v[9 + k]);
+        }
+    }
+}
+
+__global__ void k_init_state(BuildState* st) {
+    if (threadIdx.x == 0) {
+        for (int k = 0; k < 3; k++) {
+            st->cb[k] = 0xFFFFFFFFu;
+            st->cb[3 + k] = 0u;
+            st->bb[k] = 0xFFFFFFFFu;
+            st->bb[3 + k] = 0u;
+        }
+        st->node_counter = 1;
+        for (int k = 0; k < kLevels + 2; k++) st->frontier_count[k] = 0;
+        st->error = 0;
+        st->depth = 1;
+    }
+}
+
+__device__ __forceinline__ int find_geometry(const BlasInput& in, uint32_t i) {
+    int lo = 0, hi = (int)in.geometry_count - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (in.g[mid].prefix <= i) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// Fetches triangle i's vertices; false for an invalid index or an inactive
+// (NaN) triangle.
+__device__ bool fetch_triangle(const BlasInput& in, uint32_t i, int* geom, uint32_t* prim, float v[3][3]) {
+    int g = find_geometry(in, i);
+    const BuildGeom& G = in.g[g];
+    uint32_t p = i - G.prefix;
+    *geom = g;
+    *prim = p;
+    uint32_t vi[3];
+    if (G.idx) {
+        vi[0] = G.idx[3 * (size_t)p];
+        vi[1] = G.idx[3 * (size_t)p + 1];
+        vi[2] = G.idx[3 * (size_t)p + 2];
+    } else {
+        vi[0] = 3 * p;
+        vi[1] = 3 * p + 1;
+        vi[2] = 3 * p + 2;
+    }
+    bool ok = true;
+    for (int c = 0; c < 3; c++) {
+        if (vi[c] > G.max_vertex) {
+            ok = false;
+            v[c][0] = v[c][1] = v[c][2] = __int_as_float(0x7FC00000);
+            continue;
+        }
+        const float* src = G.pos + (size_t)vi[c] * G.stride_floats;
+        v[c][0] = src[0];
+        v[c][1] = src[1];
+        v[c][2] = src[2];
+        if (!finite3(v[c])) ok = false;
+    }
+    return ok;
+}
+
+__global__ void k_blas_prims(const __grid_constant__ BlasInput in, float4* boxes, BuildState* st) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    float cmin[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, cmax[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    float bmin[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, bmax[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    if (i < in.n) {
+        int g;
+        uint32_t p;
+        float v[3][3];
+        float lo[3], hi[3];
+        bool ok = fetch_triangle(in, i, &g, &p, v);
+        if (ok) {
+            for (int k = 0; k < 3; k++) {
+                lo[k] = fminf(fminf(v[0][k], v[1][k]), v[2][k]);
+                hi[k] = fmaxf(fmaxf(v[0][k], v[1][k]), v[2][k]);
+            }
+            pad_box(lo, hi);
+            for (int k = 0; k < 3; k++) {
+                float c = 0.5f * (lo[k] + hi[k]);
+                cmin[k] = c;
+                cmax[k] = c;
+                bmin[k] = lo[k];
+                bmax[k] = hi[k];
+            }
+        } else {
+            for (int k = 0; k < 3; k++) {
+                lo[k] = INFINITY;
+                hi[k] = -INFINITY;
+            }
+            bool bad_index = false;
+            const BuildGeom& G = in.g[g];
+            if (G.idx) {
+                for (int c = 0; c < 3; c++) bad_index |= G.idx[3 * (size_t)p + c] > G.max_vertex;
+            } else {
+                bad_index = 3 * p + 2 > G.max_vertex;
+            }
+            if (bad_index) atomicOr(&st->error, 1u << RT_ERR_INVALID);
+        }
+        boxes[2 * (size_t)i] = make_float4(lo[0], lo[1], lo[2], 0.0f);
+        boxes[2 * (size_t)i + 1] = make_float4(hi[0], hi[1], hi[2], 0.0f);
+    }
+    reduce_bounds(st, cmin, cmax, bmin, bmax);
+}
+
+// Instance world boxes: the 8 transformed corners of the BLAS bounds, padded
+// so the box stays conservative for the rounded object-space ray.
+__global__ void k_tlas_prims(const RtAccelerationStructureInstance* inst, uint32_t n, float4* boxes,
+                             InstRecord* temp, BuildState* st) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    float cmin[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, cmax[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    float bmin[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, bmax[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    if (i < n) {
+        RtAccelerationStructureInstance r = inst[i];
+        InstRecord rec;
+        const float* m = &r.transform[0][0];
+        for (int k = 0; k < 12; k++) rec.o2w[k] = m[k];
+        bool valid = affine_inverse(m, rec.w2o);
+        rec.blas = r.acceleration_structure_reference;
+        rec.instance_id = i;
+        rec.custom_mask = r.instance_custom_index_and_mask;
+        rec.sbt_flags = r.instance_shader_binding_table_record_offset_and_flags;
+        rec._pad[0] = rec._pad[1] = 0;
+        float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+        if (rec.blas == 0) valid = false;
+        if (valid) {
+            const AsHeader* bh = reinterpret_cast<const AsHeader*>(rec.blas);
+            if (bh->magic != kAsMagic || bh->type != kAsTypeBottom) {
+                valid = false;
+                atomicOr(&st->error, 1u << RT_ERR_BAD_AS);
+            } else if (bh->prim_count == 0) {
+                valid = false;
+            } else {
+                float blo[3] = {bh->bounds_lo[0], bh->bounds_lo[1], bh->bounds_lo[2]};
+                float bhi[3] = {bh->bounds_hi[0], bh->bounds_hi[1], bh->bounds_hi[2]};
+                for (int c = 0; c < 8; c++) {
+                    V3 p = mk3((c & 1) ? bhi[0] : blo[0], (c & 2) ? bhi[1] : blo[1], (c & 4) ? bhi[2] : blo[2]);
+                    V3 q = xform_point(rec.o2w, p);
+                    lo[0] = fminf(lo[0], q.x);
+                    lo[1] = fminf(lo[1], q.y);
+                    lo[2] = fminf(lo[2], q.z);
+                    hi[0] = fmaxf(hi[0], q.x);
+                    hi[1] = fmaxf(hi[1], q.y);
+                    hi[2] = fmaxf(hi[2], q.z);
+                }
+                float ext = fmaxf(fmaxf(hi[0] - lo[0], hi[1] - lo[1]), hi[2] - lo[2]);
+                for (int k = 0; k < 3; k++) {
+                    float pad = (fmaxf(fabsf(lo[k]), fabsf(hi[k])) + ext) * 1e-5f + 1e-20f;
+                    lo[k] -= pad;
+                    hi[k] += pad;
+                }
+                if (!finite3(lo) || !finite3(hi)) valid = false;
+            }
+        }
+        if (!valid) {
+            for (int k = 0; k < 3; k++) {
+                lo[k] = INFINITY;
+                hi[k] = -INFINITY;
+            }
+        } else {
+            for (int k = 0; k < 3; k++) {
+                float c = 0.5f * (lo[k] + hi[k]);
+                cmin[k] = cmax[k] = c;
+                bmin[k] = lo[k];
+                bmax[k] = hi[k];
+            }
+        }
+        rec.valid = valid ? 1u : 0u;
+        temp[i] = rec;
+        boxes[2 * (size_t)i] = make_float4(lo[0], lo[1], lo[2], 0.0f);
+        boxes[2 * (size_t)i + 1] = make_float4(hi[0], hi[1], hi[2], 0.0f);
+    }
+    reduce_bounds(st, cmin, cmax, bmin, bmax);
+}
+
+__device__ __forceinline__ uint32_t expand_bits10(uint32_t x) {
+    x = (x * 0x00010001u) & 0xFF0000FFu;
+    x = (x * 0x00000101u) & 0x0F00F00Fu;
+    x = (x * 0x00000011u) & 0xC30C30C3u;
+    x = (x * 0x00000005u) & 0x49249249u;
+    return x;
+}
+
+__global__ void k_morton(const float4* boxes, uint32_t n, const BuildState* st, uint32_t* keys, uint32_t* vals) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4 lo = boxes[2 * (size_t)i], hi = boxes[2 * (size_t)i + 1];
+    float c[3] = {0.5f * (lo.x + hi.x), 0.5f * (lo.y + hi.y), 0.5f * (lo.z + hi.z)};
+    uint32_t q[3] = {0, 0, 0};
+    if (finite3(c)) {
+        for (int k = 0; k < 3; k++) {
+            float mn = o2f(st->cb[k]), mx = o2f(st->cb[3 + k]);
+            float ext = mx - mn;
+            float x = ext > 0.0f ? (c[k] - mn) / ext : 0.0f;
+            float s = fminf(fmaxf(x * 1024.0f, 0.0f), 1023.0f);
+            q[k] = (uint32_t)s;
+        }
+    }
+    keys[i] = (expand_bits10(q[0]) << 2) | (expand_bits10(q[1]) << 1) | expand_bits10(q[2]);
+    vals[i] = i;
+}
+
+// ---- radix sort -----------------------------------------------------------
+__global__ void __launch_bounds__(kSortThreads) k_radix_hist(const uint32_t* keys, uint32_t n, int shift,
+                                                             uint32_t* hist, uint32_t nblocks) {
+    __shared__ uint32_t h[256];
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) h[i] = 0;
+    __syncthreads();
+    uint32_t base = blockIdx.x * kSortTile;
+    for (int j = 0; j < kSortItems; j++) {
+        uint32_t idx = base + j * kSortThreads + threadIdx.x;
+        if (idx < n) atomicAdd(&h[(keys[idx] >> shift) & 255u], 1u);
+    }
+    __syncthreads();
+    for (int d = threadIdx.x; d < 256; d += blockDim.x) hist[(size_t)d * nblocks + blockIdx.x] = h[d];
+}
+
+// Exclusive scan of m values by one block of 1024 threads.
+__global__ void __launch_bounds__(1024) k_scan_exclusive(uint32_t* data, uint32_t m) {
+    __shared__ uint32_t warp_sums[32];
+    uint32_t per = (m + 1023) / 1024;
+    uint32_t b = threadIdx.x * per, e = min(m, b + per);
+    uint32_t sum = 0;
+    for (uint32_t i = b; i < e; i++) sum += data[i];
+    uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t incl = sum;
+    for (int off = 1; off < 32; off <<= 1) {
+        uint32_t o = __shfl_up_sync(0xFFFFFFFFu, incl, off);
+        if (lane >= off) incl += o;
+    }
+    if (lane == 31) warp_sums[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = warp_sums[lane];
+        uint32_t wi = w;
+        for (int off = 1; off < 32; off <<= 1) {
+            uint32_t o = __shfl_up_sync(0xFFFFFFFFu, wi, off);
+            if (lane >= off) wi += o;
+        }
+        warp_sums[lane] = wi - w;
+    }
+    __syncthreads();
+    uint32_t run = warp_sums[warp] + incl - sum;
+    for (uint32_t i = b; i < e; i++) {
+        uint32_t v = data[i];
+        data[i] = run;
+        run += v;
+    }
+}
+
+__global__ void __launch_bounds__(kSortThreads) k_radix_scatter(const uint32_t* kin, const uint32_t* vin,
+                                                                uint32_t* kout, uint32_t* vout, uint32_t n,
+                                                                int shift, const uint32_t* hist, uint32_t nblocks) {
+    __shared__ uint32_t digit_base[256];
+    __shared__ uint32_t run[256];
+    __shared__ uint32_t warp_cnt[kSortThreads / 32][256];
+    for (int d = threadIdx.x; d < 256; d += blockDim.x) {
+        digit_base[d] = hist[(size_t)d * nblocks + blockIdx.x];
+        run[d] = 0;
+    }
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t lanemask_lt = (1u << lane) - 1u;
+    uint32_t base = blockIdx.x * kSortTile;
+    for (int j = 0; j < kSortItems; j++) {
+        for (int i = threadIdx.x; i < (kSortThreads / 32) * 256; i += blockDim.x) (&warp_cnt[0][0])[i] = 0;
+        __syncthreads();
+        uint32_t idx = base + j * kSortThreads + threadIdx.x;
+        bool valid = idx < n;
+        uint32_t key = valid ? kin[idx] : 0u;
+        uint32_t val = valid ? vin[idx] : 0u;
+        uint32_t d = valid ? ((key >> shift) & 255u) : 256u;
+        uint32_t peers = __match_any_sync(0xFFFFFFFFu, d);
+        uint32_t rank = __popc(peers & lanemask_lt);
+        if (valid && rank == 0) warp_cnt[warp][d] = __popc(peers);
+        __syncthreads();
+        if (threadIdx.x < 256) {
+            uint32_t dd = threadIdx.x;
+            uint32_t r = run[dd];
+            for (int w = 0; w < kSortThreads / 32; w++) {
+                uint32_t c = warp_cnt[w][dd];
+                warp_cnt[w][dd] = r;
+                r += c;
+            }
+            run[dd] = r;
+        }
+        __syncthreads();
+        if (valid) {
+            uint32_t pos = digit_base[d] + warp_cnt[warp][d] + rank;
+            if (pos < n) {
+                kout[pos] = key;
+                vout[pos] = val;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void k_gather_boxes(const float4* boxes, const uint32_t* vals, uint32_t n, float4* sboxes) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t p = vals[i];
+    sboxes[2 * (size_t)i] = boxes[2 * (size_t)p];
+    sboxes[2 * (size_t)i + 1] = boxes[2 * (size_t)p + 1];
+}
+
+// ---- Karras hierarchy -------------------------------------------------------
+__device__ __forceinline__ int kdelta(const uint32_t* k, int n, int i, int j) {
+    if (j < 0 || j >= n) return -1;
+    uint32_t a = k[i], b = k[j];
+    if (a == b) return 32 + __clz((uint32_t)i ^ (uint32_t)j);
+    return __clz(a ^ b);
+}
+
+__global__ void k_karras(const uint32_t* keys, uint32_t n_u, uint4* inodes, uint32_t* iparent, uint32_t* lparent) {
+    int n = (int)n_u;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n - 1) return;
+    int d = (kdelta(keys, n, i, i + 1) - kdelta(keys, n, i, i - 1)) >= 0 ? 1 : -1;
+    int dmin = kdelta(keys, n, i, i - d);
+    int lmax = 2;
+    while (kdelta(keys, n, i, i + lmax * d) > dmin) lmax <<= 1;
+    int l = 0;
+    for (int t = lmax >> 1; t >= 1; t >>= 1)
+        if (kdelta(keys, n, i, i + (l + t) * d) > dmin) l += t;
+    int j = i + l * d;
+    int dnode = kdelta(keys, n, i, j);
+    int s = 0;
+    int t = l;
+    do {
+        t = (t + 1) >> 1;
+        if (kdelta(keys, n, i, i + (s + t) * d) > dnode) s += t;
+    } while (t > 1);
+    int gamma = i + s * d + min(d, 0);
+    int first = min(i, j), last = max(i, j);
+    uint32_t left = (first == gamma) ? (kLeafBit | (uint32_t)gamma) : (uint32_t)gamma;
+    uint32_t right = (last == gamma + 1) ? (kLeafBit | (uint32_t)(gamma + 1)) : (uint32_t)(gamma + 1);
+    inodes[i] = make_uint4(left, right, (uint32_t)first, (uint32_t)last);
+    if (left & kLeafBit) lparent[gamma] = (uint32_t)i;
+    else iparent[gamma] = (uint32_t)i;
+    if (right & kLeafBit) lparent[gamma + 1] = (uint32_t)i;
+    else iparent[gamma + 1] = (uint32_t)i;
+    if (i == 0) iparent[0] = kNone;
+}
+
+__device__ __forceinline__ void load_box_cg(const float4* b, size_t i, float lo[3], float hi[3]) {
+    float4 l = __ldcg(&b[2 * i]), h = __ldcg(&b[2 * i + 1]);
+    lo[0] = l.x; lo[1] = l.y; lo[2] = l.z;
+    hi[0] = h.x; hi[1] = h.y; hi[2] = h.z;
+}
+
+__global__ void k_bottom_up(const uint4* inodes, const uint32_t* lparent, const uint32_t* iparent,
+                            const float4* sboxes, float4* iboxes, uint32_t* flags, uint32_t n, uint32_t* err) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t p = lparent[i];
+    for (int guard = 0; p != kNone; guard++) {
+        if (guard >= 160 || p >= n - 1) {  // deeper than any Karras tree of 2^28 keys
+            atomicOr(err, 1u << RT_ERR_BAD_AS);
+            return;
+        }
+        __threadfence();
+        if (atomicAdd(&flags[p], 1u) == 0u) return;
+        uint4 nd = __ldcg(&inodes[p]);
+        float llo[3], lhi[3], rlo[3], rhi[3];
+        if (nd.x & kLeafBit) load_box_cg(sboxes, nd.x & ~kLeafBit, llo, lhi);
+        else load_box_cg(iboxes, nd.x, llo, lhi);
+        if (nd.y & kLeafBit) load_box_cg(sboxes, nd.y & ~kLeafBit, rlo, rhi);
+        else load_box_cg(iboxes, nd.y, rlo, rhi);
+        iboxes[2 * (size_t)p] = make_float4(fminf(llo[0], rlo[0]), fminf(llo[1], rlo[1]), fminf(llo[2], rlo[2]), 0.0f);
+        iboxes[2 * (size_t)p + 1] =
+            make_float4(fmaxf(lhi[0], rhi[0]), fmaxf(lhi[1], rhi[1]), fmaxf(lhi[2], rhi[2]), 0.0f);
+        p = __ldcg(&iparent[p]);
+    }
+}
+
+// ---- collapse to 8-wide -------------------------------------------------------
+struct CollapseCtx {
+    const uint4* inodes;
+    const float4* iboxes;
+    const float4* sboxes;
+    WideNode* nodes;
+    uint32_t* parents;   // may be null
+    BuildState* st;
+    uint32_t leaf_max;
+    uint32_t max_nodes;
+    uint32_t n;          // primitives
+};
+
+__device__ __forceinline__ void ref_range(const CollapseCtx& c, uint32_t r, uint32_t* first, uint32_t* last) {
+    if (r & kLeafBit) {
+        *first = *last = r & ~kLeafBit;
+    } else {
+        uint4 nd = c.inodes[r];
+        *first = nd.z;
+        *last = nd.w;
+    }
+}
+__device__ __forceinline__ void ref_box(const CollapseCtx& c, uint32_t r, float lo[3], float hi[3]) {
+    const float4* b = (r & kLeafBit) ? c.sboxes : c.iboxes;
+    size_t i = r & ~kLeafBit;
+    float4 l = b[2 * i], h = b[2 * i + 1];
+    lo[0] = l.x; lo[1] = l.y; lo[2] = l.z;
+    hi[0] = h.x; hi[1] = h.y; hi[2] = h.z;
+}
+__device__ __forceinline__ float half_area(const float lo[3], const float hi[3]) {
+    float dx = fmaxf(hi[0] - lo[0], 0.0f), dy = fmaxf(hi[1] - lo[1], 0.0f), dz = fmaxf(hi[2] - lo[2], 0.0f);
+    return dx * dy + dy * dz + dz * dx;
+}
+
+__device__ void write_node(WideNode* dst, const float lo[8][3], const float hi[8][3], const uint32_t ref[8],
+                           const uint32_t meta[8], int cnt) {
+    WideNode nd;
+    for (int k = 0; k < 8; k++) {
+        bool v = k < cnt;
+        nd.lox[k] = v ? lo[k][0] : 0.0f;
+        nd.loy[k] = v ? lo[k][1] : 0.0f;
+        nd.loz[k] = v ? lo[k][2] : 0.0f;
+        nd.hix[k] = v ? hi[k][0] : 0.0f;
+        nd.hiy[k] = v ? hi[k][1] : 0.0f;
+        nd.hiz[k] = v ? hi[k][2] : 0.0f;
+        nd.child_ref[k] = v ? ref[k] : 0u;
+    }
+    uint32_t m0 = 0, m1 = 0;
+    for (int k = 0; k < 4; k++) {
+        m0 |= (k < cnt ? meta[k] : 0u) << (8 * k);
+        m1 |= (k + 4 < cnt ? meta[k + 4] : 0u) << (8 * k);
+    }
+    nd.meta[0] = m0;
+    nd.meta[1] = m1;
+    for (int k = 0; k < 6; k++) nd._pad[k] = 0;
+    const uint4* s = reinterpret_cast<const uint4*>(&nd);
+    uint4* d = reinterpret_cast<uint4*>(dst);
+    for (int k = 0; k < 16; k++) d[k] = s[k];
+}
+
+// A binary reference is in range: leaf < n, internal < n - 1.
+__device__ __forceinline__ bool ref_ok(const CollapseCtx& c, uint32_t r) {
+    return (r & kLeafBit) ? ((r & ~kLeafBit) < c.n) : (r + 1u < c.n);
+}
+
+template <class Push>
+__device__ void collapse_task(const CollapseCtx& c, uint32_t bref, uint32_t slot, uint32_t depth, Push push) {
+    uint32_t refs[8];
+    int cnt;
+    if (bref + 1u >= c.n || slot >= c.max_nodes) {
+        atomicOr(&c.st->error, 1u << RT_ERR_BAD_AS);
+        return;
+    }
+    uint4 root = c.inodes[bref];
+    refs[0] = root.x;
+    refs[1] = root.y;
+    cnt = 2;
+    if (!ref_ok(c, refs[0]) || !ref_ok(c, refs[1])) cnt = 0;
+    while (cnt >= 2 && cnt < 8) {
+        int best = -1;
+        float best_area = -1.0f;
+        for (int k = 0; k < cnt; k++) {
+            uint32_t r = refs[k];
+            if (r & kLeafBit) continue;
+            uint32_t f, l;
+            ref_range(c, r, &f, &l);
+            if (l - f + 1 <= c.leaf_max) continue;
+            float lo[3], hi[3];
+            ref_box(c, r, lo, hi);
+            float a = half_area(lo, hi);
+            if (a > best_area) {
+                best_area = a;
+                best = k;
+            }
+        }
+        if (best < 0) break;
+        uint4 nd = c.inodes[refs[best]];
+        if (!ref_ok(c, nd.x) || !ref_ok(c, nd.y)) {
+            cnt = 0;
+            break;
+        }
+        refs[best] = nd.x;
+        refs[cnt++] = nd.y;
+    }
+    if (cnt == 0) atomicOr(&c.st->error, 1u << RT_ERR_BAD_AS);  // malformed hierarchy: empty node
+    float lo[8][3], hi[8][3];
+    uint32_t ref[8], meta[8];
+    for (int k = 0; k < cnt; k++) {
+        uint32_t r = refs[k];
+        uint32_t f, l;
+        ref_range(c, r, &f, &l);
+        ref_box(c, r, lo[k], hi[k]);
+        uint32_t size = l - f + 1;
+        if ((r & kLeafBit) || size <= c.leaf_max) {
+            meta[k] = size;
+            ref[k] = f;
+        } else {
+            uint32_t cs = atomicAdd(&c.st->node_counter, 1u);
+            if (cs >= c.max_nodes) {
+                atomicOr(&c.st->error, 1u << RT_ERR_TOO_LARGE);
+                meta[k] = 0;
+                ref[k] = 0;
+                continue;
+            }
+            meta[k] = kMetaInternal;
+            ref[k] = cs;
+            if (c.parents) c.parents[cs] = slot;
+            push(r, cs, depth + 1);
+        }
+    }
+    write_node(&c.nodes[slot], lo, hi, ref, meta, cnt);
+    atomicMax(&c.st->depth, depth + 1);
+}
+
+// Root wide node: a single leaf for n <= leaf_max, else the level-0 task.
+__global__ void k_collapse_root(CollapseCtx c, uint32_t n, uint4* frontier0) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    if (c.parents) c.parents[0] = kNone;
+    if (n == 0 || n <= c.leaf_max) {
+        float lo[8][3], hi[8][3];
+        uint32_t ref[8] = {0}, meta[8] = {0};
+        int cnt = 0;
+        if (n > 0) {
+            for (int k = 0; k < 3; k++) {
+                lo[0][k] = o2f(c.st->bb[k]);
+                hi[0][k] = o2f(c.st->bb[3 + k]);
+            }
+            ref[0] = 0;
+            meta[0] = n;
+            cnt = 1;
+        }
+        write_node(&c.nodes[0], lo, hi, ref, meta, cnt);
+        return;
+    }
+    frontier0[0] = make_uint4(0u, 0u, 0u, 0u);
+    c.st->frontier_count[0] = 1;
+}
+
+__global__ void k_collapse_level(CollapseCtx c, int level, const uint4* fin, uint4* fout) {
+    uint32_t count = c.st->frontier_count[level];
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < count; t += gridDim.x * blockDim.x) {
+        uint4 task = fin[t];
+        collapse_task(c, task.x, task.y, task.z, [&](uint32_t r, uint32_t s, uint32_t d) {
+            uint32_t k = atomicAdd(&c.st->frontier_count[level + 1], 1u);
+            if (k < kFrontierCap) fout[k] = make_uint4(r, s, d, 0u);
+            else atomicOr(&c.st->error, 1u << RT_ERR_TOO_LARGE);
+        });
+    }
+}
+
+__global__ void k_collapse_tail(CollapseCtx c, const uint4* fin) {
+    uint32_t count = c.st->frontier_count[kLevels];
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < count; t += gridDim.x * blockDim.x) {
+        uint2 stack[kTailStack];
+        uint32_t dstack[kTailStack];
+        int sp = 0;
+        uint4 task = fin[t];
+        stack[sp] = make_uint2(task.x, task.y);
+        dstack[sp++] = task.z;
+        while (sp > 0) {
+            --sp;
+            uint2 e = stack[sp];
+            uint32_t d = dstack[sp];
+            collapse_task(c, e.x, e.y, d, [&](uint32_t r, uint32_t s, uint32_t dd) {
+                if (sp < kTailStack) {
+                    stack[sp] = make_uint2(r, s);
+                    dstack[sp++] = dd;
+                } else {
+                    atomicOr(&c.st->error, 1u << RT_ERR_STACK_OVERFLOW);
+                }
+            });
+        }
+    }
+}
+
+// ---- primitive records ----------------------------------------------------------
+__global__ void k_write_tris(const __grid_constant__ BlasInput in, const uint32_t* vals, TriRecord* tris) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= in.n) return;
+    uint32_t p = vals[i];
+    int g;
+    uint32_t prim;
+    float v[3][3];
+    bool ok = fetch_triangle(in, p, &g, &prim, v);
+    if (!ok) {
+        float qn = __int_as_float(0x7FC00000);
+        for (int c = 0; c < 3; c++) v[c][0] = v[c][1] = v[c][2] = qn;
+    }
+    uint32_t flags = (in.g[g].flags & RT_GEOMETRY_OPAQUE) ? 1u : 0u;
+    TriRecord r;
+    r.v0 = make_float4(v[0][0], v[0][1], v[0][2], __uint_as_float(prim));
+    r.v1 = make_float4(v[1][0], v[1][1], v[1][2], __uint_as_float((uint32_t)g));
+    r.v2 = make_float4(v[2][0], v[2][1], v[2][2], __uint_as_float(flags));
+    tris[i] = r;
+}
+
+__global__ void k_write_insts(const InstRecord* temp, const uint32_t* vals, uint32_t n, InstRecord* out) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    out[i] = temp[vals[i]];
+}
+
+struct HeaderStatic {
+    uint32_t type, build_flags, prim_count, max_nodes, geometry_count, leaf_max;
+    uint64_t total_size, nodes_offset, prims_offset, parents_offset;
+    uint64_t prim_bytes;
+};
+
+__global__ void k_finalize(AsHeader* h, const BuildState* st, HeaderStatic hs) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    h->magic = kAsMagic;
+    h->type = hs.type;
+    h->build_flags = hs.build_flags;
+    uint32_t err = st->error;
+    uint32_t status = RT_OK;
+    for (uint32_t e = 1; e < 32; e++)
+        if (err & (1u << e)) {
+            status = e;
+            break;
+        }
+    h->status = status;
+    uint32_t nc = st->node_counter;
+    if (nc > hs.max_nodes) nc = hs.max_nodes;
+    h->node_count = nc;
+    h->prim_count = hs.prim_count;
+    h->max_nodes = hs.max_nodes;
+    h->node_bytes = kNodeBytes;
+    h->total_size = hs.total_size;
+    h->nodes_offset = hs.nodes_offset;
+    h->prims_offset = hs.prims_offset;
+    h->parents_offset = hs.parents_offset;
+    for (int k = 0; k < 3; k++) {
+        float lo = o2f(st->bb[k]), hi = o2f(st->bb[3 + k]);
+        if (hs.prim_count == 0 || !(lo <= hi)) {
+            lo = INFINITY;
+            hi = -INFINITY;
+        }
+        h->bounds_lo[k] = lo;
+        h->bounds_hi[k] = hi;
+    }
+    h->geometry_count = hs.geometry_count;
+    h->depth = st->depth;
+    h->leaf_max = hs.leaf_max;
+    uint64_t nodes_end = hs.nodes_offset + (uint64_t)nc * kNodeBytes;
+    uint64_t par = hs.parents_offset ? align_up(nodes_end, 256) : 0;
+    uint64_t par_end = par ? par + (uint64_t)nc * 4 : nodes_end;
+    h->compacted_size = align_up(align_up(par_end, 256) + hs.prim_count * hs.prim_bytes, 256);
+}
+
+// ---- TLAS refit ---------------------------------------------------------------------
+__global__ void k_refit_insts(const RtAccelerationStructureInstance* inst, uint32_t n, AsHeader* h,
+                              float4* sboxes, uint32_t* err) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    InstRecord* recs = reinterpret_cast<InstRecord*>(reinterpret_cast<uint8_t*>(h) + h->prims_offset);
+    InstRecord rec = recs[i];
+    uint32_t id = rec.instance_id;
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    bool valid = false;
+    if (id < n) {
+        RtAccelerationStructureInstance r = inst[id];
+        const float* m = &r.transform[0][0];
+        for (int k = 0; k < 12; k++) rec.o2w[k] = m[k];
+        valid = affine_inverse(m, rec.w2o);
+        rec.blas = r.acceleration_structure_reference;
+        rec.custom_mask = r.instance_custom_index_and_mask;
+        rec.sbt_flags = r.instance_shader_binding_table_record_offset_and_flags;
+        if (rec.blas == 0) valid = false;
+        if (valid) {
+            const AsHeader* bh = reinterpret_cast<const AsHeader*>(rec.blas);
+            if (bh->magic != kAsMagic || bh->type != kAsTypeBottom) {
+                valid = false;
+                atomicOr(err, 1u << RT_ERR_BAD_AS);
+            } else if (bh->prim_count == 0) {
+                valid = false;
+            } else {
+                for (int c = 0; c < 8; c++) {
+                    V3 p = mk3((c & 1) ? bh->bounds_hi[0] : bh->bounds_lo[0],
+                               (c & 2) ? bh->bounds_hi[1] : bh->bounds_lo[1],
+                               (c & 4) ? bh->bounds_hi[2] : bh->bounds_lo[2]);
+                    V3 q = xform_point(rec.o2w, p);
+                    lo[0] = fminf(lo[0], q.x);
+                    lo[1] = fminf(lo[1], q.y);
+                    lo[2] = fminf(lo[2], q.z);
+                    hi[0] = fmaxf(hi[0], q.x);
+                    hi[1] = fmaxf(hi[1], q.y);
+                    hi[2] = fmaxf(hi[2], q.z);
+                }
+                float ext = fmaxf(fmaxf(hi[0] - lo[0], hi[1] - lo[1]), hi[2] - lo[2]);
+                for (int k = 0; k < 3; k++) {
+                    float pad = (fmaxf(fabsf(lo[k]), fabsf(hi[k])) + ext) * 1e-5f + 1e-20f;
+                    lo[k] -= pad;
+                    hi[k] += pad;
+                }
+                if (!finite3(lo) || !finite3(hi)) valid = false;
+            }
+        }
+    } else {
+        atomicOr(err, 1u << RT_ERR_INVALID);
+    }
+    if (!valid) {
+        for (int k = 0; k < 3; k++) {
+            lo[k] = INFINITY;
+            hi[k] = -INFINITY;
+        }
+    }
+    rec.valid = valid ? 1u : 0u;
+    recs[i] = rec;
+    sboxes[2 * (size_t)i] = make_float4(lo[0], lo[1], lo[2], 0.0f);
+    sboxes[2 * (size_t)i + 1] = make_float4(hi[0], hi[1], hi[2], 0.0f);
+}
+
+__device__ __forceinline__ int internal_children(const WideNode* nd) {
+    uint32_t m0 = __ldcg(&nd->meta[0]), m1 = __ldcg(&nd->meta[1]);
+    int c = 0;
+    for (int k = 0; k < 8; k++) c += node_meta(m0, m1, k) == kMetaInternal;
+    return c;
+}
+
+__global__ void k_refit_nodes(AsHeader* h, const float4* sboxes, uint32_t* counters, uint32_t* err) {
+    uint32_t count = h->node_count;
+    uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
+    if (slot >= count) return;
+    uint8_t* base = reinterpret_cast<uint8_t*>(h);
+    WideNode* nodes = reinterpret_cast<WideNode*>(base + h->nodes_offset);
+    const uint32_t* parents = reinterpret_cast<const uint32_t*>(base + h->parents_offset);
+    if (internal_children(&nodes[slot]) != 0) return;
+    for (int guard = 0; guard < 64; guard++) {
+        WideNode* nd = &nodes[slot];
+        uint32_t m0 = __ldcg(&nd->meta[0]), m1 = __ldcg(&nd->meta[1]);
+        float ulo[3] = {INFINITY, INFINITY, INFINITY}, uhi[3] = {-INFINITY, -INFINITY, -INFINITY};
+        for (int k = 0; k < 8; k++) {
+            uint32_t m = node_meta(m0, m1, k);
+            if (m == 0) continue;
+            uint32_t r = __ldcg(&nd->child_ref[k]);
+            float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+            if (m == kMetaInternal) {
+                const WideNode* cn = &nodes[r];
+                uint32_t c0 = __ldcg(&cn->meta[0]), c1 = __ldcg(&cn->meta[1]);
+                for (int q = 0; q < 8; q++) {
+                    if (node_meta(c0, c1, q) == 0) continue;
+                    lo[0] = fminf(lo[0], __ldcg(&cn->lox[q]));
+                    lo[1] = fminf(lo[1], __ldcg(&cn->loy[q]));
+                    lo[2] = fminf(lo[2], __ldcg(&cn->loz[q]));
+                    hi[0] = fmaxf(hi[0], __ldcg(&cn->hix[q]));
+                    hi[1] = fmaxf(hi[1], __ldcg(&cn->hiy[q]));
+                    hi[2] = fmaxf(hi[2], __ldcg(&cn->hiz[q]));
+                }
+            } else {
+                for (uint32_t q = 0; q < m; q++) {
+                    float4 l = sboxes[2 * (size_t)(r + q)], u = sboxes[2 * (size_t)(r + q) + 1];
+                    lo[0] = fminf(lo[0], l.x);
+                    lo[1] = fminf(lo[1], l.y);
+                    lo[2] = fminf(lo[2], l.z);
+                    hi[0] = fmaxf(hi[0], u.x);
+                    hi[1] = fmaxf(hi[1], u.y);
+                    hi[2] = fmaxf(hi[2], u.z);
+                }
+            }
+            nd->lox[k] = lo[0];
+            nd->loy[k] = lo[1];
+            nd->loz[k] = lo[2];
+            nd->hix[k] = hi[0];
+            nd->hiy[k] = hi[1];
+            nd->hiz[k] = hi[2];
+            for (int a = 0; a < 3; a++) {
+                ulo[a] = fminf(ulo[a], lo[a]);
+                uhi[a] = fmaxf(uhi[a], hi[a]);
+            }
+        }
+        __threadfence();
+        uint32_t p = __ldcg(&parents[slot]);
+        if (p == kNone || p >= count) {
+            for (int a = 0; a < 3; a++) {
+                h->bounds_lo[a] = ulo[a];
+                h->bounds_hi[a] = uhi[a];
+            }
+            return;
+        }
+        int need = internal_children(&nodes[p]);
+        if ((int)atomicAdd(&counters[p], 1u) + 1 < need) return;
+        slot = p;
+    }
+    atomicOr(err, 1u << RT_ERR_STACK_OVERFLOW);
+}
+
+__global__ void k_refit_status(AsHeader* h, const uint32_t* err) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    uint32_t e = *err;
+    for (uint32_t b = 1; b < 32; b++)
+        if (e & (1u << b)) {
+            h->status = b;
+            return;
+        }
+}
+
+// ---- AS copy (CLONE / COMPACT) ------------------------------------------------------
+__global__ void k_as_copy(const uint8_t* src, uint8_t* dst, uint64_t dst_size, uint32_t mode) {
+    const AsHeader* h = reinterpret_cast<const AsHeader*>(src);
+    if (h->magic != kAsMagic) {
+        if (blockIdx.x == 0 && threadIdx.x == 0 && dst_size >= kHeaderBytes)
+            reinterpret_cast<AsHeader*>(dst)->status = RT_ERR_BAD_AS;
+        return;
+    }
+    uint64_t nodes_bytes = (uint64_t)h->node_count * kNodeBytes;
+    uint64_t prim_bytes = (uint64_t)h->prim_count * (h->type == kAsTypeTop ? kInstBytes : kTriBytes);
+    uint64_t par_bytes = h->parents_offset ? (uint64_t)h->node_count * 4 : 0;
+    uint64_t need = mode == RT_COPY_MODE_COMPACT ? h->compacted_size : h->total_size;
+    if (need > dst_size) {
+        if (blockIdx.x == 0 && threadIdx.x == 0 && dst_size >= kHeaderBytes) {
+            AsHeader* d = reinterpret_cast<AsHeader*>(dst);
+            d->magic = 0;
+            d->status = RT_ERR_INVALID;
+        }
+        return;
+    }
+    uint64_t tid = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x, stride = (uint64_t)gridDim.x * blockDim.x;
+    if (mode != RT_COPY_MODE_COMPACT) {
+        // CLONE: the whole blob, position independent (offsets only).
+        const uint4* s = reinterpret_cast<const uint4*>(src);
+        uint4* d = reinterpret_cast<uint4*>(dst);
+        uint64_t n16 = h->total_size / 16;
+        for (uint64_t i = tid; i < n16; i += stride) d[i] = s[i];
+        return;
+    }
+    // COMPACT: header | nodes[node_count] | parents[node_count] | prims
+    uint64_t c_nodes = h->nodes_offset;
+    uint64_t c_par = h->parents_offset ? align_up(c_nodes + nodes_bytes, 256) : 0;
+    uint64_t c_prims = align_up(c_par ? c_par + par_bytes : c_nodes + nodes_bytes, 256);
+    auto copy = [&](uint64_t so, uint64_t dof, uint64_t bytes) {
+        const uint32_t* s = reinterpret_cast<const uint32_t*>(src + so);
+        uint32_t* d = reinterpret_cast<uint32_t*>(dst + dof);
+        for (uint64_t i = tid; i < bytes / 4; i += stride) d[i] = s[i];
+    };
+    copy(h->nodes_offset, c_nodes, nodes_bytes);
+    if (par_bytes) copy(h->parents_offset, c_par, par_bytes);
+    copy(h->prims_offset, c_prims, prim_bytes);
+    if (tid == 0) {
+        AsHeader hd = *h;
+        hd.max_nodes = h->node_count;
+        hd.parents_offset = c_par;
+        hd.prims_offset = c_prims;
+        hd.total_size = h->compacted_size;
+        *reinterpret_cast<AsHeader*>(dst) = hd;
+    }
+}
+
+inline uint32_t blocks_for(uint64_t n, uint32_t t) { return (uint32_t)((n + t - 1) / t); }
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Layouts
+// ---------------------------------------------------------------------------
+AsLayout AsLayout::make(uint32_t n, bool top) {
+    AsLayout l;
+    l.max_nodes = (uint32_t)max_wide_nodes(n);
+    l.nodes = kHeaderBytes;
+    uint64_t end = l.nodes + (uint64_t)l.max_nodes * kNodeBytes;
+    if (top) {
+        l.parents = align_up(end, 256);
+        end = l.parents + (uint64_t)l.max_nodes * 4;
+    } else {
+        l.parents = 0;
+    }
+    l.prims = align_up(end, 256);
+    l.total = align_up(l.prims + (uint64_t)n * (top ? kInstBytes : kTriBytes), 256);
+    return l;
+}
+
+ScratchLayout ScratchLayout::make(uint32_t n, bool top) {
+    ScratchLayout s{};
+    uint64_t nn = n ? n : 1;
+    uint64_t ni = n > 1 ? n - 1 : 1;
+    uint64_t o = 0;
+    auto take = [&](uint64_t bytes) {
+        uint64_t r = o;
+        o = align_up(o + bytes, 256);
+        return r;
+    };
+    s.sort_blocks = (uint32_t)((nn + kSortTile - 1) / kSortTile);
+    s.state = take(sizeof(BuildState));
+    s.boxes = take(nn * 32);
+    s.sboxes = take(nn * 32);
+    s.keys0 = take(nn * 4);
+    s.keys1 = take(nn * 4);
+    s.vals0 = take(nn * 4);
+    s.vals1 = take(nn * 4);
+    s.hist = take((uint64_t)256 * s.sort_blocks * 4);
+    s.inodes = take(ni * 16);
+    s.iboxes = take(ni * 32);
+    s.iparent = take(ni * 4);
+    s.lparent = take(nn * 4);
+    s.flags = take(ni * 4);
+    uint64_t f = std::min<uint64_t>(kFrontierCap, max_wide_nodes(n));
+    s.frontier0 = take(f * 16);
+    s.frontier1 = take(f * 16);
+    s.temp_inst = top ? take(nn * kInstBytes) : 0;
+    s.refit_counters = 0;
+    s.build_total = o;
+    // update (refit) scratch: sorted boxes + one counter per node
+    uint64_t u = 0;
+    u = align_up(u + nn * 32, 256);
+    s.refit_counters = u;
+    u = align_up(u + max_wide_nodes(n) * 4 + 4, 256);  // + error word
+    s.update_total = u;
+    return s;
+}
+
+// ---------------------------------------------------------------------------
+// Launchers
+// ---------------------------------------------------------------------------
+namespace {
+
+cudaError_t build_common(uint32_t n, bool top, uint32_t build_flags, uint32_t geometry_count, uint8_t* dst,
+                         uint8_t* scratch, cudaStream_t stream, const BlasInput* blas,
+                         const RtAccelerationStructureInstance* inst) {
+    ScratchLayout sl = ScratchLayout::make(n, top);
+    AsLayout al = AsLayout::make(n, top);
+    BuildState* st = reinterpret_cast<BuildState*>(scratch + sl.state);
+    float4* boxes = reinterpret_cast<float4*>(scratch + sl.boxes);
+    float4* sboxes = reinterpret_cast<float4*>(scratch + sl.sboxes);
+    uint32_t* keys[2] = {reinterpret_cast<uint32_t*>(scratch + sl.keys0), reinterpret_cast<uint32_t*>(scratch + sl.keys1)};
+    uint32_t* vals[2] = {reinterpret_cast<uint32_t*>(scratch + sl.vals0), reinterpret_cast<uint32_t*>(scratch + sl.vals1)};
+    uint32_t* hist = reinterpret_cast<uint32_t*>(scratch + sl.hist);
+    uint4* inodes = reinterpret_cast<uint4*>(scratch + sl.inodes);
+    float4* iboxes = reinterpret_cast<float4*>(scratch + sl.iboxes);
+    uint32_t* iparent = reinterpret_cast<uint32_t*>(scratch + sl.iparent);
+    uint32_t* lparent = reinterpret_cast<uint32_t*>(scratch + sl.lparent);
+    uint32_t* flags = reinterpret_cast<uint32_t*>(scratch + sl.flags);
+    uint4* fr[2] = {reinterpret_cast<uint4*>(scratch + sl.frontier0), reinterpret_cast<uint4*>(scratch + sl.frontier1)};
+    InstRecord* temp = top ? reinterpret_cast<InstRecord*>(scratch + sl.temp_inst) : nullptr;
+    const uint32_t T = 256;
+
+    note_launch(), k_init_state<<<1, 32, 0, stream>>>(st);
+    if (n > 0) {
+        if (top) note_launch(), k_tlas_prims<<<blocks_for(n, T), T, 0, stream>>>(inst, n, boxes, temp, st);
+        else note_launch(), k_blas_prims<<<blocks_for(n, T), T, 0, stream>>>(*blas, boxes, st);
+        note_launch(), k_morton<<<blocks_for(n, T), T, 0, stream>>>(boxes, n, st, keys[0], vals[0]);
+        int cur = 0;
+        if (n > 1) {
+            for (int pass = 0; pass < 4; pass++) {
+                int shift = pass * 8;
+                note_launch(), k_radix_hist<<<sl.sort_blocks, kSortThreads, 0, stream>>>(keys[cur], n, shift, hist, sl.sort_blocks);
+                note_launch(), k_scan_exclusive<<<1, 1024, 0, stream>>>(hist, 256u * sl.sort_blocks);
+                note_launch(), k_radix_scatter<<<sl.sort_blocks, kSortThreads, 0, stream>>>(keys[cur], vals[cur], keys[cur ^ 1],
+                                                                             vals[cur ^ 1], n, shift, hist,
+                                                                             sl.sort_blocks);
+                cur ^= 1;
+            }
+        }
+        note_launch(), k_gather_boxes<<<blocks_for(n, T), T, 0, stream>>>(boxes, vals[cur], n, sboxes);
+        if (n > 1) {
+            note_launch(), k_karras<<<blocks_for(n - 1, T), T, 0, stream>>>(keys[cur], n, inodes, iparent, lparent);
+            cudaMemsetAsync(flags, 0, (size_t)(n - 1) * 4, stream);
+            note_launch(), k_bottom_up<<<blocks_for(n, T), T, 0, stream>>>(inodes, lparent, iparent, sboxes, iboxes,
+                                                                             flags, n, &st->error);
+        }
+        CollapseCtx cc;
+        cc.inodes = inodes;
+        cc.iboxes = iboxes;
+        cc.sboxes = sboxes;
+        cc.nodes = reinterpret_cast<WideNode*>(dst + al.nodes);
+        cc.parents = top ? reinterpret_cast<uint32_t*>(dst + al.parents) : nullptr;
+        cc.st = st;
+        cc.leaf_max = top ? kTlasLeafMax : kBlasLeafMax;
+        cc.max_nodes = al.max_nodes;
+        cc.n = n;
+        note_launch(), k_collapse_root<<<1, 32, 0, stream>>>(cc, n, fr[0]);
+        if (n > cc.leaf_max) {
+            uint64_t cap = 1;
+            for (int lv = 0; lv < kLevels; lv++) {
+                uint32_t g = blocks_for(std::min<uint64_t>(cap, al.max_nodes), 128);
+                note_launch(), k_collapse_level<<<g, 128, 0, stream>>>(cc, lv, fr[lv & 1], fr[(lv + 1) & 1]);
+                cap *= 8;
+            }
+            uint32_t g = blocks_for(std::min<uint64_t>(kFrontierCap, al.max_nodes), 128);
+            note_launch(), k_collapse_tail<<<g, 128, 0, stream>>>(cc, fr[kLevels & 1]);
+        }
+        if (top) {
+            note_launch(), k_write_insts<<<blocks_for(n, T), T, 0, stream>>>(temp, vals[cur], n,
+                                                              reinterpret_cast<InstRecord*>(dst + al.prims));
+        } else {
+            note_launch(), k_write_tris<<<blocks_for(n, T), T, 0, stream>>>(*blas, vals[cur], reinterpret_cast<TriRecord*>(dst + al.prims));
+        }
+    } else {
+        CollapseCtx cc{};
+        cc.nodes = reinterpret_cast<WideNode*>(dst + al.nodes);
+        cc.parents = top ? reinterpret_cast<uint32_t*>(dst + al.parents) : nullptr;
+        cc.st = st;
+        cc.leaf_max = 1;
+        cc.max_nodes = al.max_nodes;
+        cc.n = n;
+        note_launch(), k_collapse_root<<<1, 32, 0, stream>>>(cc, 0, fr[0]);
+    }
+    HeaderStatic hs;
+    hs.type = top ? kAsTypeTop : kAsTypeBottom;
+    hs.build_flags = build_flags;
+    hs.prim_count = n;
+    hs.max_nodes = al.max_nodes;
+    hs.geometry_count = geometry_count;
+    hs.leaf_max = top ? kTlasLeafMax : kBlasLeafMax;
+    hs.total_size = al.total;
+    hs.nodes_offset = al.nodes;
+    hs.prims_offset = al.prims;
+    hs.parents_offset = al.parents;
+    hs.prim_bytes = top ? kInstBytes : kTriBytes;
+    note_launch(), k_finalize<<<1, 32, 0, stream>>>(reinterpret_cast<AsHeader*>(dst), st, hs);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_blas_build(const BlasInput& in, uint32_t build_flags, uint8_t* dst, uint8_t* scratch,
+                              cudaStream_t stream) {
+    return build_common(in.n, false, build_flags, in.geometry_count, dst, scratch, stream, &in, nullptr);
+}
+
+cudaError_t launch_tlas_build(const RtAccelerationStructureInstance* instances, uint32_t n, uint32_t build_flags,
+                              uint8_t* dst, uint8_t* scratch, cudaStream_t stream) {
+    return build_common(n, true, build_flags, 1, dst, scratch, stream, nullptr, instances);
+}
+
+cudaError_t launch_as_copy(const uint8_t* src, uint8_t* dst, uint64_t dst_size, uint32_t mode, cudaStream_t stream) {
+    note_launch(), k_as_copy<<<1024, 256, 0, stream>>>(src, dst, dst_size, mode);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_tlas_update(const RtAccelerationStructureInstance* instances, uint32_t n, const uint8_t* src,
+                               uint8_t* dst, uint64_t dst_size, uint8_t* scratch, cudaStream_t stream) {
+    ScratchLayout sl = ScratchLayout::make(n, true);
+    AsLayout al = AsLayout::make(n, true);
+    if (src != dst) {
+        note_launch(), k_as_copy<<<1024, 256, 0, stream>>>(src, dst, dst_size, RT_COPY_MODE_CLONE);
+    }
+    float4* sboxes = reinterpret_cast<float4*>(scratch);
+    uint32_t* counters = reinterpret_cast<uint32_t*>(scratch + sl.refit_counters);
+    // the error word lives after the counters
+    uint32_t* err = counters + al.max_nodes;
+    cudaMemsetAsync(counters, 0, (size_t)al.max_nodes * 4 + 4, stream);
+    AsHeader* h = reinterpret_cast<AsHeader*>(dst);
+    if (n > 0) note_launch(), k_refit_insts<<<blocks_for(n, 256), 256, 0, stream>>>(instances, n, h, sboxes, err);
+    note_launch(), k_refit_nodes<<<blocks_for(al.max_nodes, 128), 128, 0, stream>>>(h, sboxes, counters, err);
+    note_launch(), k_refit_status<<<1, 32, 0, stream>>>(h, err);
+    return cudaGetLastError();
+}
+
+}  // namespace rt

@@ -1,0 +1,91 @@
+// rt_internal.h — host-side launch interface between the C ABI and kernels.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "rt_device.cuh"
+
+namespace rt {
+
+// Counts every kernel this library launches (rt_kernel_launch_count).
+void note_launch();
+
+// One BLAS geometry as the build kernels see it.
+struct BuildGeom {
+    const float* pos;
+    const uint32_t* idx;      // nullptr = non-indexed
+    uint32_t stride_floats;
+    uint32_t max_vertex;
+    uint32_t prim_count;
+    uint32_t flags;
+    uint32_t prefix;          // first global primitive of this geometry
+    uint32_t _pad;
+};
+
+struct BlasInput {
+    BuildGeom g[RT_MAX_BLAS_GEOMETRIES];
+    uint32_t geometry_count;
+    uint32_t n;
+};
+
+// Byte offsets of the build scratch regions for n primitives.
+struct ScratchLayout {
+    uint64_t boxes, sboxes, keys0, keys1, vals0, vals1, hist, inodes, iboxes, iparent, lparent, flags;
+    uint64_t frontier0, frontier1, state, temp_inst, refit_counters;
+    uint64_t build_total;
+    uint64_t update_total;
+    uint32_t sort_blocks;
+    static ScratchLayout make(uint32_t n, bool top_level);
+};
+
+// Byte offsets inside the AS blob.
+struct AsLayout {
+    uint64_t nodes, parents, prims, total;
+    uint32_t max_nodes;
+    static AsLayout make(uint32_t n, bool top_level);
+};
+
+constexpr uint32_t kMaxPrimitives = (1u << 28) - 1;  // leaf refs carry 28 bits
+
+cudaError_t launch_blas_build(const BlasInput& in, uint32_t build_flags, uint8_t* dst, uint8_t* scratch,
+                              cudaStream_t stream);
+cudaError_t launch_tlas_build(const RtAccelerationStructureInstance* instances, uint32_t n, uint32_t build_flags,
+                              uint8_t* dst, uint8_t* scratch, cudaStream_t stream);
+cudaError_t launch_tlas_update(const RtAccelerationStructureInstance* instances, uint32_t n, const uint8_t* src,
+                               uint8_t* dst, uint64_t dst_size, uint8_t* scratch, cudaStream_t stream);
+cudaError_t launch_as_copy(const uint8_t* src, uint8_t* dst, uint64_t dst_size, uint32_t mode, cudaStream_t stream);
+
+// Trace entry points (rt_trace.cu).
+struct TraceLaunch {
+    RtPushConstantBufferAddresses push;
+    RtShaderBindingTable sbt;
+    RtTraceRaysDesc desc;
+    RtTextureDesc textures[RT_MAX_BOUND_IMAGES];
+    RtStats* stats;            // device
+    uint32_t* status;          // device (same block)
+    uint32_t* work;            // device pixel-fetch counter for this launch
+};
+cudaError_t launch_trace_rays(const TraceLaunch& p, int num_sms, cudaStream_t stream);
+
+struct RayBufferLaunch {
+    RtPushConstantBufferAddresses push;  // model_info may be 0
+    RtShaderBindingTable sbt;
+    RtTextureDesc textures[RT_MAX_BOUND_IMAGES];
+    uint64_t tlas;
+    const RtRay* rays;
+    RtHit* hits;
+    uint32_t count;
+    uint32_t ray_flags;
+    uint32_t cull_mask;
+    uint32_t sbt_offset;
+    uint32_t collect_stats;
+    RtStats* stats;
+    uint32_t* status;
+};
+cudaError_t launch_trace_ray_buffer(const RayBufferLaunch& p, int num_sms, cudaStream_t stream);
+
+cudaError_t launch_debug_eval(uint32_t fn, const float* in, float* out, uint32_t count, cudaStream_t stream);
+cudaError_t upload_srgb_table();
+
+}  // namespace rt

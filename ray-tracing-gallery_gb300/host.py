@@ -1,0 +1,350 @@
+"""Host side above the C ABI, mirroring the reference's Rust host for this path.
+
+Names follow the reference so a maintainer can map each call:
+
+=====================================  =========================================
+this module                            reference (src/...)
+=====================================  =========================================
+ScratchBuffer.ensure_size_of           util_structs.rs:420-524 (grow-only)
+AccelerationStructure.build_blas       util_structs.rs:140-224 (+ new :226-283)
+AccelerationStructure.build_tlas       util_functions.rs:453-510 (build_tlas)
+AccelerationStructure.update_tlas      util_structs.rs:285-357
+AccelerationStructure.clone            util_structs.rs:359-405
+GpuModel.new                           Model::new, util_structs.rs:1158-1236
+ImageManager.push_image                util_structs.rs:1296-1377
+PerFrameResources.record               command_buffer_recording.rs:79-126
+=====================================  =========================================
+
+Device memory comes from PyTorch (its caching allocator returns 512-byte
+aligned blocks); every compute call goes through librtcore.so.  There is no
+CPU fallback: without a CUDA device or without the built library these
+classes raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import abi
+from .scenes import Model, Scene, Texture
+
+try:
+    import torch
+except ImportError:  # pragma: no cover - torch is part of the image
+    torch = None
+
+
+def _require_cuda():
+    if torch is None or not torch.cuda.is_available():
+        raise RuntimeError("a CUDA device is required for the ray-tracing core (there is no CPU fallback)")
+
+
+class Device:
+    """One librtcore context on the current CUDA device."""
+
+    def __init__(self, threadsafe: bool = False):
+        _require_cuda()
+        self.lib = abi.load_library()
+        torch.cuda.init()
+        self.ctx = C.c_void_p()
+        self.check(self.lib.rt_ctx_create(abi.RT_CTX_THREADSAFE if threadsafe else 0, C.byref(self.ctx)))
+        self._texture_refs: dict[int, object] = {}
+
+    # -- plumbing ---------------------------------------------------------
+    def check(self, status: int) -> None:
+        abi.check(self.lib, status)
+
+    @staticmethod
+    def stream_handle(stream=None) -> C.c_void_p:
+        s = stream if stream is not None else torch.cuda.current_stream()
+        return C.c_void_p(s.cuda_stream)
+
+    @staticmethod
+    def alloc(nbytes: int) -> "torch.Tensor":
+        t = torch.empty(max(int(nbytes), 1), dtype=torch.uint8, device="cuda")
+        assert t.data_ptr() % abi.RT_AS_ALIGNMENT == 0
+        return t
+
+    @staticmethod
+    def upload(a: np.ndarray) -> "torch.Tensor":
+        a = np.ascontiguousarray(a)
+        t = torch.from_numpy(a.view(np.uint8).reshape(-1).copy()).to("cuda")
+        return t
+
+    def set_texture(self, index: int, tex: Texture) -> None:
+        buf = self.upload(tex.texels)
+        d = abi.RtTextureDesc()
+        d.address = buf.data_ptr()
+        d.height, d.width = tex.texels.shape[0], tex.texels.shape[1]
+        d.row_pitch = tex.row_pitch
+        d.format = tex.format
+        d.filter = tex.filter
+        self.check(self.lib.rt_ctx_set_texture(self.ctx, index, C.byref(d)))
+        self._texture_refs[index] = buf
+
+    def read_stats(self, reset: bool = True, stream=None) -> dict:
+        s = abi.RtStats()
+        self.check(self.lib.rt_ctx_read_stats(self.ctx, C.byref(s), 1 if reset else 0, self.stream_handle(stream)))
+        return s.as_dict()
+
+    def close(self) -> None:
+        if self.ctx:
+            torch.cuda.synchronize()
+            self.lib.rt_ctx_destroy(self.ctx)
+            self.ctx = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class ScratchBuffer:
+    """Grow-only scratch (ScratchBuffer::ensure_size_of): reallocated only
+    when a build needs more than it holds."""
+
+    def __init__(self, name: str = "scratch"):
+        self.name = name
+        self.buffer = None
+
+    def ensure_size_of(self, size: int) -> int:
+        if self.buffer is None or self.buffer.numel() < size:
+            if self.buffer is not None:
+                torch.cuda.current_stream().synchronize()
+            self.buffer = Device.alloc(max(size, 256))
+        return self.buffer.data_ptr()
+
+    @property
+    def size(self) -> int:
+        return 0 if self.buffer is None else self.buffer.numel()
+
+
+@dataclass
+class GeometryDesc:
+    """src/util_structs.rs:123-129 (`Geometry`)."""
+    position_buffer_address: int
+    index_buffer_address: int
+    num_indices: int
+    num_vertices: int
+    opaque: bool
+
+
+class AccelerationStructure:
+    BOTTOM_LEVEL = 0
+    TOP_LEVEL = 1
+
+    def __init__(self, buffer, size: int, flags: int, ty: int, name: str = ""):
+        self.buffer = buffer
+        self.size = size
+        self.flags = flags
+        self.ty = ty
+        self.name = name
+
+    def device_address(self, device: Device | None = None) -> int:
+        return self.buffer.data_ptr()
+
+    @classmethod
+    def build_blas(cls, device: Device, name: str, scratch: ScratchBuffer, geometries: list[GeometryDesc],
+                   flags: int = abi.RT_BUILD_PREFER_FAST_TRACE, stream=None) -> "AccelerationStructure":
+        arr = (abi.RtGeometryTriangles * max(len(geometries), 1))()
+        for i, g in enumerate(geometries):
+            arr[i].vertex_address = g.position_buffer_address
+            arr[i].index_address = g.index_buffer_address
+            arr[i].vertex_stride = 12
+            arr[i].max_vertex = max(g.num_vertices - 1, 0)
+            arr[i].primitive_count = g.num_indices // 3
+            arr[i].flags = abi.RT_GEOMETRY_OPAQUE if g.opaque else 0
+        sizes = abi.RtBuildSizes()
+        device.check(device.lib.rt_get_blas_build_sizes(arr, len(geometries), flags, C.byref(sizes)))
+        scr = scratch.ensure_size_of(sizes.build_scratch_size)
+        buf = Device.alloc(sizes.acceleration_structure_size)
+        device.check(device.lib.rt_cmd_build_blas(device.ctx, arr, len(geometries), flags, buf.data_ptr(),
+                                                  sizes.acceleration_structure_size, scr, scratch.size,
+                                                  Device.stream_handle(stream)))
+        return cls(buf, sizes.acceleration_structure_size, flags, cls.BOTTOM_LEVEL, name)
+
+    @classmethod
+    def build_tlas(cls, device: Device, instances, num_instances: int, scratch: ScratchBuffer,
+                   flags: int = abi.RT_BUILD_PREFER_FAST_TRACE | abi.RT_BUILD_ALLOW_UPDATE,
+                   stream=None) -> "AccelerationStructure":
+        sizes = abi.RtBuildSizes()
+        device.check(device.lib.rt_get_tlas_build_sizes(num_instances, flags, C.byref(sizes)))
+        scr = scratch.ensure_size_of(sizes.build_scratch_size)
+        buf = Device.alloc(sizes.acceleration_structure_size)
+        device.check(device.lib.rt_cmd_build_tlas(device.ctx, instances.data_ptr(), num_instances, flags,
+                                                  buf.data_ptr(), sizes.acceleration_structure_size, scr,
+                                                  scratch.size, Device.stream_handle(stream)))
+        return cls(buf, sizes.acceleration_structure_size, flags, cls.TOP_LEVEL, "tlas")
+
+    def rebuild_tlas(self, device: Device, instances, num_instances: int, scratch: ScratchBuffer, stream=None) -> None:
+        """Full rebuild into the same memory (instance count unchanged)."""
+        sizes = abi.RtBuildSizes()
+        device.check(device.lib.rt_get_tlas_build_sizes(num_instances, self.flags, C.byref(sizes)))
+        scr = scratch.ensure_size_of(sizes.build_scratch_size)
+        device.check(device.lib.rt_cmd_build_tlas(device.ctx, instances.data_ptr(), num_instances, self.flags,
+                                                  self.buffer.data_ptr(), self.size, scr, scratch.size,
+                                                  Device.stream_handle(stream)))
+
+    def update_tlas(self, device: Device, instances, num_instances: int, scratch: ScratchBuffer, stream=None) -> None:
+        """In-place refit (src == dst), util_structs.rs:318-319."""
+        sizes = abi.RtBuildSizes()
+        device.check(device.lib.rt_get_tlas_build_sizes(num_instances, self.flags, C.byref(sizes)))
+        scr = scratch.ensure_size_of(sizes.update_scratch_size)
+        addr = self.buffer.data_ptr()
+        device.check(device.lib.rt_cmd_update_tlas(device.ctx, instances.data_ptr(), num_instances, addr, addr,
+                                                   self.size, scr, scratch.size, Device.stream_handle(stream)))
+
+    def clone(self, device: Device, name: str, stream=None) -> "AccelerationStructure":
+        buf = Device.alloc(self.size)
+        device.check(device.lib.rt_cmd_copy_acceleration_structure(device.ctx, self.buffer.data_ptr(), buf.data_ptr(),
+                                                                   self.size, abi.RT_COPY_MODE_CLONE,
+                                                                   Device.stream_handle(stream)))
+        return AccelerationStructure(buf, self.size, self.flags, self.ty, name)
+
+    def info(self, device: Device, stream=None) -> abi.RtAccelerationStructureInfo:
+        inf = abi.RtAccelerationStructureInfo()
+        device.check(device.lib.rt_get_acceleration_structure_info(self.buffer.data_ptr(), C.byref(inf),
+                                                                   Device.stream_handle(stream)))
+        return inf
+
+
+class GpuModel:
+    """Model::new: vertex, normal, uv, index and geometry-info buffers plus
+    the model's BLAS (one geometry per material)."""
+
+    def __init__(self, device: Device, model: Model, scratch: ScratchBuffer, model_id: int,
+                 build_flags: int = abi.RT_BUILD_PREFER_FAST_TRACE, stream=None):
+        self.id = model_id
+        self.name = model.name
+        self.position_buffer = Device.upload(np.ascontiguousarray(model.positions, np.float32))
+        self.normal_buffer = Device.upload(np.ascontiguousarray(model.normals, np.float32))
+        self.uv_buffer = Device.upload(np.ascontiguousarray(model.uvs, np.float32))
+        self.index_buffers = []
+        infos = np.zeros(len(model.geometries), abi.GEOMETRY_INFO_DTYPE)
+        geoms = []
+        for i, g in enumerate(model.geometries):
+            ib = Device.upload(np.ascontiguousarray(g.indices, np.uint32))
+            self.index_buffers.append(ib)
+            geoms.append(GeometryDesc(self.position_buffer.data_ptr(), ib.data_ptr(), int(g.indices.size),
+                                      len(model.positions), g.opaque))
+            infos[i] = (ib.data_ptr(), g.diffuse_image, g.metallic_roughness_image, g.normal_map_image, 0)
+        self.geometry_info_buffer = Device.upload(infos)
+        self.blas = AccelerationStructure.build_blas(device, f"{model.name} blas", scratch, geoms, build_flags,
+                                                     stream)
+
+    def model_info(self) -> tuple:
+        return (self.position_buffer.data_ptr(), self.normal_buffer.data_ptr(), self.uv_buffer.data_ptr(),
+                self.geometry_info_buffer.data_ptr())
+
+
+class ImageManager:
+    """The bindless texture array: every texture of a scene bound at its index."""
+
+    def __init__(self, device: Device):
+        self.device = device
+
+    def push_images(self, textures: dict[int, Texture]) -> None:
+        for idx, tex in textures.items():
+            self.device.set_texture(idx, tex)
+
+
+class GpuScene:
+    """Everything a scene needs resident on the device: models with BLASes,
+    the ModelInfo array, textures, the instance buffer and its TLAS."""
+
+    def __init__(self, device: Device, scene: Scene, scratch: ScratchBuffer | None = None,
+                 tlas_flags: int = abi.RT_BUILD_PREFER_FAST_TRACE | abi.RT_BUILD_ALLOW_UPDATE, stream=None):
+        self.device = device
+        self.scene = scene
+        self.scratch = scratch or ScratchBuffer("scene scratch")
+        self.models = [GpuModel(device, m, self.scratch, i, stream=stream) for i, m in enumerate(scene.models)]
+        infos = np.array([m.model_info() for m in self.models], abi.MODEL_INFO_DTYPE)
+        self.model_info_buffer = Device.upload(infos)
+        ImageManager(device).push_images(scene.textures)
+        self.num_instances = len(scene.instances)
+        self.instances_host = self.patch_instances(scene.instances)
+        self.instances_buffer = Device.upload(self.instances_host)
+        self.tlas = AccelerationStructure.build_tlas(device, self.instances_buffer, self.num_instances, self.scratch,
+                                                     tlas_flags, stream)
+
+    def patch_instances(self, instances: np.ndarray) -> np.ndarray:
+        """Scene instances carry model indices; replace them by BLAS addresses."""
+        out = instances.copy()
+        addrs = np.array([m.blas.device_address() for m in self.models], np.uint64)
+        out["blas"] = addrs[instances["blas"].astype(np.int64)]
+        return out
+
+    def push_constants(self, uniforms_address: int, tlas: AccelerationStructure | None = None):
+        p = abi.RtPushConstantBufferAddresses()
+        p.model_info = self.model_info_buffer.data_ptr()
+        p.uniforms = uniforms_address
+        p.acceleration_structure = (tlas or self.tlas).device_address()
+        return p
+
+
+class PerFrameResources:
+    """command_buffer_recording.rs:22-55: per-frame uniforms, output image,
+    instance buffer and TLAS (a CLONE of the scene's, src/main.rs:600-668)."""
+
+    def __init__(self, device: Device, gpu_scene: GpuScene, width: int, height: int, radiance: bool = False,
+                 clone_tlas: bool = False):
+        self.device = device
+        self.gpu_scene = gpu_scene
+        self.width, self.height = width, height
+        self.uniforms_buffer = Device.alloc(C.sizeof(abi.RtUniforms))
+        self.image = torch.zeros((height, width, 4), dtype=torch.uint8, device="cuda")
+        self.radiance = torch.zeros((height, width, 4), dtype=torch.float32, device="cuda") if radiance else None
+        self.instances_buffer = gpu_scene.instances_buffer.clone()
+        self.num_instances = gpu_scene.num_instances
+        self.scratch = ScratchBuffer("frame scratch")
+        self.tlas = gpu_scene.tlas.clone(device, "frame tlas") if clone_tlas else gpu_scene.tlas
+
+    def write_uniforms(self, uniforms: abi.RtUniforms, stream=None) -> None:
+        host = torch.frombuffer(bytearray(bytes(uniforms)), dtype=torch.uint8)
+        self.uniforms_buffer.copy_(host, non_blocking=False)
+
+    def record(self, max_trace_depth: int, shadow_ray_count: int, flags: int = 0,
+               sbt: abi.RtShaderBindingTable | None = None, stream=None) -> None:
+        """cmd_trace_rays(raygen, miss, hit, {}, W, H, 1)."""
+        push = self.gpu_scene.push_constants(self.uniforms_buffer.data_ptr(), self.tlas)
+        d = abi.RtTraceRaysDesc()
+        d.width, d.height = self.width, self.height
+        d.max_trace_depth = max_trace_depth
+        d.shadow_ray_count = shadow_ray_count
+        d.flags = flags
+        d.image_address = self.image.data_ptr()
+        d.radiance_address = self.radiance.data_ptr() if self.radiance is not None else 0
+        sbt_p = C.byref(sbt) if sbt is not None else None
+        self.device.check(self.device.lib.rt_cmd_trace_rays(self.device.ctx, C.byref(push), sbt_p, C.byref(d),
+                                                            Device.stream_handle(stream)))
+
+
+def render(device: Device, scene: Scene, radiance: bool = True, flags: int = 0):
+    """Builds a scene, renders one frame and returns (image, radiance, stats)."""
+    gs = GpuScene(device, scene)
+    fr = PerFrameResources(device, gs, scene.width, scene.height, radiance=radiance)
+    fr.write_uniforms(scene.uniforms)
+    device.read_stats(reset=True)
+    fr.record(scene.max_trace_depth, scene.shadow_ray_count, flags, scene.sbt)
+    stats = device.read_stats(reset=True)
+    img = fr.image.cpu().numpy()
+    rad = fr.radiance.cpu().numpy() if radiance else None
+    return img, rad, stats
+
+
+def trace_ray_buffer(device: Device, gpu_scene: GpuScene, rays: np.ndarray, ray_flags: int = 0,
+                     cull_mask: int = 0xFF, sbt_offset: int = 0, with_models: bool = True,
+                     sbt: abi.RtShaderBindingTable | None = None):
+    """Traversal-only query of `rays` (RAY_DTYPE) against the scene's TLAS."""
+    rb = Device.upload(rays)
+    hb = Device.alloc(len(rays) * abi.HIT_DTYPE.itemsize)
+    push = gpu_scene.push_constants(0) if with_models else abi.RtPushConstantBufferAddresses()
+    device.check(device.lib.rt_cmd_trace_ray_buffer(device.ctx, gpu_scene.tlas.device_address(), C.byref(push),
+                                                    C.byref(sbt) if sbt is not None else None, ray_flags, cull_mask,
+                                                    sbt_offset, rb.data_ptr(), len(rays), hb.data_ptr(),
+                                                    Device.stream_handle()))
+    torch.cuda.synchronize()
+    return hb.cpu().numpy().view(abi.HIT_DTYPE)

@@ -1,0 +1,96 @@
+"""CPU tests of the C ABI: layouts, exported symbols, host-side validation.
+No compute call is made here (there is no GPU on this side)."""
+import ctypes as C
+import re
+import subprocess
+from pathlib import Path
+
+import pytest
+
+from rtgallery import abi
+
+ROOT = Path(__file__).resolve().parent.parent
+HEADER = ROOT / "include" / "rtcore.h"
+
+
+def declared_functions() -> set[str]:
+    text = HEADER.read_text()
+    return set(re.findall(r"RTCORE_API\s+[\w\s\*]+?\b(rt_\w+)\s*\(", text))
+
+
+def test_layouts_match_reference():
+    abi.check_layouts()
+
+
+def test_header_static_asserts_compile(tmp_path):
+    src = tmp_path / "t.c"
+    src.write_text('#include "rtcore.h"\nint main(void){return 0;}\n')
+    r = subprocess.run(["gcc", "-std=c11", "-Wall", "-Werror", "-I", str(ROOT / "include"), str(src), "-o",
+                        str(tmp_path / "t")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run(["g++", "-std=c++17", "-Wall", "-Werror", "-x", "c++", "-I", str(ROOT / "include"), str(src),
+                        "-o", str(tmp_path / "t2")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+
+
+def test_library_exports_every_declared_symbol(rtlib):
+    declared = declared_functions()
+    assert len(declared) >= 17
+    assert declared == set(abi.EXPORTED_FUNCTIONS), declared ^ set(abi.EXPORTED_FUNCTIONS)
+    out = subprocess.run(["nm", "-D", "--defined-only", str(abi.library_path())], capture_output=True, text=True).stdout
+    exported = {line.split()[-1] for line in out.splitlines() if " T " in line}
+    assert declared <= exported
+    # only the ABI is exported from our code (cudart's own symbols aside)
+    ours = {s for s in exported if s.startswith("rt_")}
+    assert ours == declared
+    for name in declared:
+        assert hasattr(rtlib, name)
+
+
+def test_version_string(rtlib):
+    assert b"sm_103a" in rtlib.rt_version_string()
+
+
+def test_blas_size_query_validates_on_host(rtlib):
+    g = (abi.RtGeometryTriangles * 2)()
+    g[0].vertex_address = 4096
+    g[0].index_address = 8192
+    g[0].vertex_stride = 12
+    g[0].max_vertex = 99
+    g[0].primitive_count = 1000
+    g[1].vertex_address = 4096
+    g[1].vertex_stride = 12
+    g[1].primitive_count = 24
+    s = abi.RtBuildSizes()
+    assert rtlib.rt_get_blas_build_sizes(g, 2, 0, C.byref(s)) == abi.RT_OK
+    assert s.acceleration_structure_size >= 512 + 1024 * 48 and s.acceleration_structure_size % 256 == 0
+    assert s.build_scratch_size > 0
+    g[0].vertex_stride = 10
+    assert rtlib.rt_get_blas_build_sizes(g, 2, 0, C.byref(s)) == abi.RT_ERR_INVALID
+    assert b"vertex_stride" in rtlib.rt_last_error_string()
+    assert rtlib.rt_get_blas_build_sizes(g, 129, 0, C.byref(s)) == abi.RT_ERR_TOO_LARGE
+    g[0].vertex_stride = 12
+    g[0].primitive_count = 1 << 28
+    assert rtlib.rt_get_blas_build_sizes(g, 2, 0, C.byref(s)) == abi.RT_ERR_TOO_LARGE
+
+
+def test_tlas_size_query(rtlib):
+    a, b = abi.RtBuildSizes(), abi.RtBuildSizes()
+    assert rtlib.rt_get_tlas_build_sizes(256, 0, C.byref(a)) == 0
+    assert rtlib.rt_get_tlas_build_sizes(4096, 0, C.byref(b)) == 0
+    assert b.acceleration_structure_size > a.acceleration_structure_size
+    assert a.update_scratch_size < a.build_scratch_size
+    assert rtlib.rt_get_tlas_build_sizes(0, 0, C.byref(a)) == 0
+
+
+def test_null_and_alignment_rejected_before_launch(rtlib):
+    assert rtlib.rt_ctx_create(0, None) == abi.RT_ERR_INVALID
+    s = abi.RtBuildSizes()
+    assert rtlib.rt_get_tlas_build_sizes(4, 0, None) == abi.RT_ERR_INVALID
+    # misaligned destination: rejected on the host, nothing is launched
+    assert rtlib.rt_cmd_build_tlas(None, 16, 4, 0, 4096 + 16, 1 << 20, 8192, 1 << 20, None) == abi.RT_ERR_INVALID
+    assert rtlib.rt_cmd_copy_acceleration_structure(None, 256, 256, 4096, 0, None) == abi.RT_ERR_INVALID
+    assert rtlib.rt_get_acceleration_structure_device_address(4096 + 8) == 0
+    assert rtlib.rt_get_acceleration_structure_device_address(4096) == 4096
+    assert rtlib.rt_debug_eval(99, 0, 0, 0, None) == abi.RT_ERR_INVALID
+    del s
