@@ -28,8 +28,14 @@ __constant__ float c_srgb_lut[256];
 namespace {
 
 constexpr uint32_t kStackSize = 64;
+// Stack entries: internal node index (bit 31 clear, < 2^30); leaf =
+// bit 31 | (count - 1) << 28 | first primitive; kMarker = return to the
+// TLAS.  kNoEntry would be a leaf of 8 primitives starting at 2^28 - 1,
+// which no structure can hold (primitive counts are < 2^28), so it is free
+// to mean "stack empty".
 constexpr uint32_t kMarker = 0x7FFFFFFFu;
 constexpr uint32_t kLeafEntry = 0x80000000u;
+constexpr uint32_t kNoEntry = 0xFFFFFFFFu;
 constexpr float kPi = 3.141592653589793f;
 
 struct Counters {
@@ -374,7 +380,7 @@ __device__ void traverse(const Env& e, V3 wo, V3 wd, float tmin, float tmax, uin
             }
         }
         // ---- pop ----
-        entry = kMarker + 1;
+        entry = kNoEntry;
         const float cull = best.t * kBoxFarScale;
         while (sp > 0) {
             uint2 s = stack[--sp];
@@ -382,7 +388,7 @@ __device__ void traverse(const Env& e, V3 wo, V3 wd, float tmin, float tmax, uin
             entry = s.x;
             break;
         }
-        if (entry == kMarker + 1) return;
+        if (entry == kNoEntry) return;
     }
 }
 

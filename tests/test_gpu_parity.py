@@ -139,7 +139,8 @@ def test_ray_buffer_bit_exact(device, name):
             assert ((g["instance_id"] == 0xFFFFFFFF) == (h["instance_id"] == 0xFFFFFFFF)).all()
         else:
             _assert_hits_equal(g, h, f"{name} flags {flags:#x}")
-    assert (h["instance_id"] != 0xFFFFFFFF).sum() > 100
+        if flags == abi.RT_RAY_FLAG_NONE:
+            assert (h["instance_id"] != 0xFFFFFFFF).sum() > 100
     # cull mask: instances whose mask misses the ray's are skipped
     g = _host().trace_ray_buffer(device, gs, rays, cull_mask=0x00)
     assert (g["instance_id"] == 0xFFFFFFFF).all()
@@ -280,4 +281,4 @@ def test_mid_size_mesh_bit_exact(device):
     g = host.trace_ray_buffer(device, gs, rays, with_models=False)
     o, _ = O.OracleScene(sc).trace(rays, with_models=False)
     _assert_hits_equal(g, o, "icosphere l6")
-    assert (g["instance_id"] != 0xFFFFFFFF).mean() > 0.3
+    assert (g["instance_id"] != 0xFFFFFFFF).mean() > 0.2
