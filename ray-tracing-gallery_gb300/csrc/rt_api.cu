@@ -11,6 +11,7 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <vector>
 
 #include "rt_internal.h"
 
@@ -72,6 +73,15 @@ int32_t check_sbt(const RtShaderBindingTable* sbt) {
 
 void rt::note_launch() { g_kernel_launches.fetch_add(1, std::memory_order_relaxed); }
 
+// Wavefront workspace of one stream: grown stream-ordered (cudaFreeAsync /
+// cudaMallocAsync on that stream), so launches on one stream reuse it
+// safely and launches on different streams never share one.
+struct Workspace {
+    cudaStream_t stream;
+    void* ptr;
+    uint64_t size;
+};
+
 struct rt_ctx {
     uint32_t flags = 0;
     int device = 0;
@@ -80,7 +90,32 @@ struct rt_ctx {
     CtxDevice* dev = nullptr;
     std::atomic<uint32_t> work_slot{0};
     std::mutex mu;
+    std::vector<Workspace> workspaces;
 };
+
+namespace {
+cudaError_t ctx_workspace(rt_ctx* c, cudaStream_t s, uint64_t need, uint8_t** out) {
+    for (auto& w : c->workspaces) {
+        if (w.stream != s) continue;
+        if (w.size < need) {
+            cudaError_t e = cudaFreeAsync(w.ptr, s);
+            w.ptr = nullptr;
+            w.size = 0;
+            if (e == cudaSuccess) e = cudaMallocAsync(&w.ptr, need, s);
+            if (e != cudaSuccess) return e;
+            w.size = need;
+        }
+        *out = reinterpret_cast<uint8_t*>(w.ptr);
+        return cudaSuccess;
+    }
+    Workspace w{s, nullptr, need};
+    cudaError_t e = cudaMallocAsync(&w.ptr, need, s);
+    if (e != cudaSuccess) return e;
+    c->workspaces.push_back(w);
+    *out = reinterpret_cast<uint8_t*>(w.ptr);
+    return cudaSuccess;
+}
+}  // namespace
 
 namespace {
 struct MaybeLock {
@@ -124,6 +159,9 @@ RTCORE_API int32_t rt_ctx_create(uint32_t flags, rt_ctx** out) {
 
 RTCORE_API int32_t rt_ctx_destroy(rt_ctx* ctx) {
     if (!ctx) return RT_OK;
+    cudaDeviceSynchronize();
+    for (auto& w : ctx->workspaces)
+        if (w.ptr) cudaFree(w.ptr);
     if (ctx->dev) cudaFree(ctx->dev);
     delete ctx;
     return RT_OK;
@@ -380,8 +418,12 @@ RTCORE_API int32_t rt_cmd_trace_rays(rt_ctx* ctx, const RtPushConstantBufferAddr
     memcpy(p.textures, ctx->textures, sizeof p.textures);
     p.stats = &ctx->dev->stats;
     p.status = &ctx->dev->stats.status;
-    p.work = &ctx->dev->work[ctx->work_slot.fetch_add(1) % kWorkSlots];
-    cudaError_t e = launch_trace_rays(p, ctx->num_sms, reinterpret_cast<cudaStream_t>(stream));
+    p.work = nullptr;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    uint8_t* ws = nullptr;
+    cudaError_t e = ctx_workspace(ctx, s, trace_workspace_bytes(desc->width, desc->height), &ws);
+    if (e != cudaSuccess) return cuda_fail(e, "rt_cmd_trace_rays (workspace)");
+    e = launch_trace_rays(p, ws, ctx->num_sms, s);
     if (e != cudaSuccess) return cuda_fail(e, "rt_cmd_trace_rays");
     return RT_OK;
 }
@@ -415,6 +457,7 @@ RTCORE_API int32_t rt_cmd_trace_ray_buffer(rt_ctx* ctx, uint64_t tlas, const RtP
     p.collect_stats = (ray_flags & RT_RAY_FLAG_EXT_COLLECT_STATS) ? 1u : 0u;
     p.stats = &ctx->dev->stats;
     p.status = &ctx->dev->stats.status;
+    p.work = &ctx->dev->work[ctx->work_slot.fetch_add(1) % kWorkSlots];
     cudaError_t e = launch_trace_ray_buffer(p, ctx->num_sms, reinterpret_cast<cudaStream_t>(stream));
     if (e != cudaSuccess) return cuda_fail(e, "rt_cmd_trace_ray_buffer");
     return RT_OK;

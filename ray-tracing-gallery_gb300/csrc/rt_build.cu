@@ -200,8 +200,72 @@ __global__ void k_blas_prims(const __grid_constant__ BlasInput in, float4* boxes
     reduce_bounds(st, cmin, cmax, bmin, bmax);
 }
 
-// Instance world boxes: the 8 transformed corners of the BLAS bounds, padded
-// so the box stays conservative for the rounded object-space ray.
+// Fills a TLAS instance record from the caller's instance `r` (index id):
+// world-to-object inverse, BLAS fields for the traversal, and the world box
+// = the 8 transformed corners of the BLAS bounds, padded so the box stays
+// conservative for the rounded object-space ray.  Returns false (empty box,
+// tri_count 0) for a singular transform or a null / empty BLAS.
+__device__ bool fill_instance(const RtAccelerationStructureInstance& r, uint32_t id, InstRecord* rec, float lo[3],
+                              float hi[3], uint32_t* err) {
+    const float* m = &r.transform[0][0];
+    for (int k = 0; k < 12; k++) rec->o2w[k] = m[k];
+    bool valid = affine_inverse(m, rec->w2o);
+    rec->blas = r.acceleration_structure_reference;
+    rec->instance_id = id;
+    rec->custom_mask = r.instance_custom_index_and_mask;
+    rec->sbt_flags = r.instance_shader_binding_table_record_offset_and_flags;
+    rec->tri_count = 0;
+    rec->node_count = 0;
+    rec->prims_off256 = 0;
+    for (int k = 0; k < 3; k++) {
+        lo[k] = INFINITY;
+        hi[k] = -INFINITY;
+    }
+    if (rec->blas == 0) valid = false;
+    if (valid) {
+        const AsHeader* bh = reinterpret_cast<const AsHeader*>(rec->blas);
+        if (bh->magic != kAsMagic || bh->type != kAsTypeBottom) {
+            valid = false;
+            atomicOr(err, 1u << RT_ERR_BAD_AS);
+        } else if (bh->prim_count == 0) {
+            valid = false;
+        } else {
+            float blo[3] = {bh->bounds_lo[0], bh->bounds_lo[1], bh->bounds_lo[2]};
+            float bhi[3] = {bh->bounds_hi[0], bh->bounds_hi[1], bh->bounds_hi[2]};
+            for (int c = 0; c < 8; c++) {
+                V3 p = mk3((c & 1) ? bhi[0] : blo[0], (c & 2) ? bhi[1] : blo[1], (c & 4) ? bhi[2] : blo[2]);
+                V3 q = xform_point(rec->o2w, p);
+                lo[0] = fminf(lo[0], q.x);
+                lo[1] = fminf(lo[1], q.y);
+                lo[2] = fminf(lo[2], q.z);
+                hi[0] = fmaxf(hi[0], q.x);
+                hi[1] = fmaxf(hi[1], q.y);
+                hi[2] = fmaxf(hi[2], q.z);
+            }
+            float ext = fmaxf(fmaxf(hi[0] - lo[0], hi[1] - lo[1]), hi[2] - lo[2]);
+            for (int k = 0; k < 3; k++) {
+                float pad = (fmaxf(fabsf(lo[k]), fabsf(hi[k])) + ext) * 1e-5f + 1e-20f;
+                lo[k] -= pad;
+                hi[k] += pad;
+            }
+            if (!finite3(lo) || !finite3(hi)) valid = false;
+            if (valid) {
+                rec->tri_count = bh->prim_count;
+                rec->node_count = bh->node_count;
+                rec->prims_off256 = (uint32_t)(bh->prims_offset / 256);
+            }
+        }
+    }
+    if (!valid) {
+        rec->tri_count = 0;
+        for (int k = 0; k < 3; k++) {
+            lo[k] = INFINITY;
+            hi[k] = -INFINITY;
+        }
+    }
+    return valid;
+}
+
 __global__ void k_tlas_prims(const RtAccelerationStructureInstance* inst, uint32_t n, float4* boxes,
                              InstRecord* temp, BuildState* st) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -210,51 +274,8 @@ __global__ void k_tlas_prims(const RtAccelerationStructureInstance* inst, uint32
     if (i < n) {
         RtAccelerationStructureInstance r = inst[i];
         InstRecord rec;
-        const float* m = &r.transform[0][0];
-        for (int k = 0; k < 12; k++) rec.o2w[k] = m[k];
-        bool valid = affine_inverse(m, rec.w2o);
-        rec.blas = r.acceleration_structure_reference;
-        rec.instance_id = i;
-        rec.custom_mask = r.instance_custom_index_and_mask;
-        rec.sbt_flags = r.instance_shader_binding_table_record_offset_and_flags;
-        rec._pad[0] = rec._pad[1] = 0;
-        float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
-        if (rec.blas == 0) valid = false;
-        if (valid) {
-            const AsHeader* bh = reinterpret_cast<const AsHeader*>(rec.blas);
-            if (bh->magic != kAsMagic || bh->type != kAsTypeBottom) {
-                valid = false;
-                atomicOr(&st->error, 1u << RT_ERR_BAD_AS);
-            } else if (bh->prim_count == 0) {
-                valid = false;
-            } else {
-                float blo[3] = {bh->bounds_lo[0], bh->bounds_lo[1], bh->bounds_lo[2]};
-                float bhi[3] = {bh->bounds_hi[0], bh->bounds_hi[1], bh->bounds_hi[2]};
-                for (int c = 0; c < 8; c++) {
-                    V3 p = mk3((c & 1) ? bhi[0] : blo[0], (c & 2) ? bhi[1] : blo[1], (c & 4) ? bhi[2] : blo[2]);
-                    V3 q = xform_point(rec.o2w, p);
-                    lo[0] = fminf(lo[0], q.x);
-                    lo[1] = fminf(lo[1], q.y);
-                    lo[2] = fminf(lo[2], q.z);
-                    hi[0] = fmaxf(hi[0], q.x);
-                    hi[1] = fmaxf(hi[1], q.y);
-                    hi[2] = fmaxf(hi[2], q.z);
-                }
-                float ext = fmaxf(fmaxf(hi[0] - lo[0], hi[1] - lo[1]), hi[2] - lo[2]);
-                for (int k = 0; k < 3; k++) {
-                    float pad = (fmaxf(fabsf(lo[k]), fabsf(hi[k])) + ext) * 1e-5f + 1e-20f;
-                    lo[k] -= pad;
-                    hi[k] += pad;
-                }
-                if (!finite3(lo) || !finite3(hi)) valid = false;
-            }
-        }
-        if (!valid) {
-            for (int k = 0; k < 3; k++) {
-                lo[k] = INFINITY;
-                hi[k] = -INFINITY;
-            }
-        } else {
+        float lo[3], hi[3];
+        if (fill_instance(r, i, &rec, lo, hi, &st->error)) {
             for (int k = 0; k < 3; k++) {
                 float c = 0.5f * (lo[k] + hi[k]);
                 cmin[k] = cmax[k] = c;
@@ -262,7 +283,6 @@ __global__ void k_tlas_prims(const RtAccelerationStructureInstance* inst, uint32
                 bmax[k] = hi[k];
             }
         }
-        rec.valid = valid ? 1u : 0u;
         temp[i] = rec;
         boxes[2 * (size_t)i] = make_float4(lo[0], lo[1], lo[2], 0.0f);
         boxes[2 * (size_t)i + 1] = make_float4(hi[0], hi[1], hi[2], 0.0f);
@@ -748,55 +768,13 @@ __global__ void k_refit_insts(const RtAccelerationStructureInstance* inst, uint3
     InstRecord rec = recs[i];
     uint32_t id = rec.instance_id;
     float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
-    bool valid = false;
     if (id < n) {
         RtAccelerationStructureInstance r = inst[id];
-        const float* m = &r.transform[0][0];
-        for (int k = 0; k < 12; k++) rec.o2w[k] = m[k];
-        valid = affine_inverse(m, rec.w2o);
-        rec.blas = r.acceleration_structure_reference;
-        rec.custom_mask = r.instance_custom_index_and_mask;
-        rec.sbt_flags = r.instance_shader_binding_table_record_offset_and_flags;
-        if (rec.blas == 0) valid = false;
-        if (valid) {
-            const AsHeader* bh = reinterpret_cast<const AsHeader*>(rec.blas);
-            if (bh->magic != kAsMagic || bh->type != kAsTypeBottom) {
-                valid = false;
-                atomicOr(err, 1u << RT_ERR_BAD_AS);
-            } else if (bh->prim_count == 0) {
-                valid = false;
-            } else {
-                for (int c = 0; c < 8; c++) {
-                    V3 p = mk3((c & 1) ? bh->bounds_hi[0] : bh->bounds_lo[0],
-                               (c & 2) ? bh->bounds_hi[1] : bh->bounds_lo[1],
-                               (c & 4) ? bh->bounds_hi[2] : bh->bounds_lo[2]);
-                    V3 q = xform_point(rec.o2w, p);
-                    lo[0] = fminf(lo[0], q.x);
-                    lo[1] = fminf(lo[1], q.y);
-                    lo[2] = fminf(lo[2], q.z);
-                    hi[0] = fmaxf(hi[0], q.x);
-                    hi[1] = fmaxf(hi[1], q.y);
-                    hi[2] = fmaxf(hi[2], q.z);
-                }
-                float ext = fmaxf(fmaxf(hi[0] - lo[0], hi[1] - lo[1]), hi[2] - lo[2]);
-                for (int k = 0; k < 3; k++) {
-                    float pad = (fmaxf(fabsf(lo[k]), fabsf(hi[k])) + ext) * 1e-5f + 1e-20f;
-                    lo[k] -= pad;
-                    hi[k] += pad;
-                }
-                if (!finite3(lo) || !finite3(hi)) valid = false;
-            }
-        }
+        fill_instance(r, id, &rec, lo, hi, err);
     } else {
+        rec.tri_count = 0;
         atomicOr(err, 1u << RT_ERR_INVALID);
     }
-    if (!valid) {
-        for (int k = 0; k < 3; k++) {
-            lo[k] = INFINITY;
-            hi[k] = -INFINITY;
-        }
-    }
-    rec.valid = valid ? 1u : 0u;
     recs[i] = rec;
     sboxes[2 * (size_t)i] = make_float4(lo[0], lo[1], lo[2], 0.0f);
     sboxes[2 * (size_t)i + 1] = make_float4(hi[0], hi[1], hi[2], 0.0f);

@@ -77,16 +77,19 @@ struct alignas(16) TriRecord {
 };
 static_assert(sizeof(TriRecord) == kTriBytes, "tri size");
 
-// TLAS instance record, sorted order.
+// TLAS instance record, sorted order.  The last 32 bytes are read with two
+// 128-bit loads when a ray enters the instance: they carry everything the
+// traversal needs from the BLAS header, so the header is never read then.
 struct alignas(16) InstRecord {
     float w2o[12];           // world -> object, row-major 3x4
     float o2w[12];           // object -> world (the instance transform)
-    uint64_t blas;           // BLAS address
-    uint32_t instance_id;    // index in the caller's instance array
-    uint32_t custom_mask;    // custom index (24) | mask (8) << 24
-    uint32_t sbt_flags;      // SBT offset (24) | flags (8) << 24
-    uint32_t valid;          // 0: singular transform or null BLAS
-    uint32_t _pad[2];
+    uint64_t blas;           // @96 BLAS address
+    uint32_t instance_id;    // @104 index in the caller's instance array
+    uint32_t custom_mask;    // @108 custom index (24) | mask (8) << 24
+    uint32_t sbt_flags;      // @112 SBT offset (24) | flags (8) << 24
+    uint32_t tri_count;      // @116 BLAS triangles; 0 = never hit (singular transform, null or empty BLAS)
+    uint32_t node_count;     // @120 BLAS wide nodes
+    uint32_t prims_off256;   // @124 BLAS triangle records offset / 256
 };
 static_assert(sizeof(InstRecord) == kInstBytes, "inst size");
 

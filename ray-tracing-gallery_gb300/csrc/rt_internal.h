@@ -64,9 +64,11 @@ struct TraceLaunch {
     RtTextureDesc textures[RT_MAX_BOUND_IMAGES];
     RtStats* stats;            // device
     uint32_t* status;          // device (same block)
-    uint32_t* work;            // device pixel-fetch counter for this launch
+    uint32_t* work;            // unused by the wavefront pipeline (kept for layout)
 };
-cudaError_t launch_trace_rays(const TraceLaunch& p, int num_sms, cudaStream_t stream);
+// Bytes of the wavefront workspace a width x height launch needs.
+uint64_t trace_workspace_bytes(uint32_t width, uint32_t height);
+cudaError_t launch_trace_rays(const TraceLaunch& p, uint8_t* workspace, int num_sms, cudaStream_t stream);
 
 struct RayBufferLaunch {
     RtPushConstantBufferAddresses push;  // model_info may be 0
@@ -82,6 +84,7 @@ struct RayBufferLaunch {
     uint32_t collect_stats;
     RtStats* stats;
     uint32_t* status;
+    uint32_t* work;            // device fetch counter for this launch (zeroed by the launcher)
 };
 cudaError_t launch_trace_ray_buffer(const RayBufferLaunch& p, int num_sms, cudaStream_t stream);
 

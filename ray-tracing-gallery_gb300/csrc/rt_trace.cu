@@ -1,174 +1,81 @@
-// rt_trace.cu — traversal and the reference's ray-tracing programs.
+// rt_trace.cu — traversal, and the reference's pipeline as wavefronts.
 //
 // Traversal (replaces the driver's traceRayEXT, called at
 // shaders/ray-tracing/src/lib.rs:67-82,151-163 and
-// shaders/closest_hit_textured.glsl:159-172): one ray per thread, explicit
-// stack in local memory, 8-wide nodes read with 128-bit loads, the eight
-// child slab tests sorted front-to-back with a 19-comparator network on
-// (tnear bits | slot) keys, the watertight FP32 triangle test, alpha-clip
-// any-hit inline for non-opaque geometry, and the closest hit chosen under
-// the total order (t, instance index, geometry index, primitive index) so the
-// result does not depend on the BVH or the visit order.
+// shaders/closest_hit_textured.glsl:159-172) runs in persistent kernels: a
+// lane holds one ray, advances it by exactly one step per loop iteration
+// (one 8-wide node, one leaf, or a return from an instance), and as soon as
+// its ray finishes it takes the next one from a warp-aggregated atomic
+// counter — so lanes never wait for the slowest ray of their warp.  A node
+// step reads the 256-byte node with 128-bit loads, runs the eight slab tests
+// and orders the hit children front to back with a 19-comparator sorting
+// network on (tnear bits | slot) keys.  Leaves run the watertight FP32
+// triangle test; non-opaque candidates run the alpha-clip any-hit inline.
+// The closest hit is the minimum under (t, instance index, geometry index,
+// primitive index), so the result does not depend on the BVH or visit order.
 //
-// Pipeline (replaces cmd_trace_rays with the reference's programs,
-// src/command_buffer_recording.rs:116-126): a persistent kernel whose
-// threads each run one pixel's raygen loop as a state machine — every loop
-// iteration is exactly one traversal (bounce ray or shadow ray), so the warp
-// stays in the traversal code regardless of which program each lane is in.
-// Idle lanes fetch new pixels (warp-aggregated atomic on 8x4 pixel tiles).
+// Pipeline (replaces cmd_trace_rays, src/command_buffer_recording.rs:116-126,
+// with the programs of src/main.rs:289-305), one frame:
+//   raygen -> [trace closest (bounce b) -> shade (b)] x max_trace_depth
+//          -> trace shadow rays (any hit, terminate on first) -> resolve -> output
+// `shade` runs the closest-hit / miss programs for every ray of bounce b:
+// misses and terminal hits write the pixel's colour; mirror / portal hits
+// append the next bounce ray; textured hits store their BRDF terms and
+// shadow origin and append the pixel to the shadow list.  Appends are
+// warp-aggregated (one atomic per warp), which compacts the wavefronts.
 #include <algorithm>
-#include <cfloat>
 
 #include "rt_internal.h"
+#include "rt_shade.cuh"
 
 namespace rt {
 
-__constant__ float c_srgb_lut[256];
-
 namespace {
 
-constexpr uint32_t kStackSize = 64;
 // Stack entries: internal node index (bit 31 clear, < 2^30); leaf =
 // bit 31 | (count - 1) << 28 | first primitive; kMarker = return to the
 // TLAS.  kNoEntry would be a leaf of 8 primitives starting at 2^28 - 1,
 // which no structure can hold (primitive counts are < 2^28), so it is free
-// to mean "stack empty".
+// to mean "done".
+constexpr uint32_t kStackSize = 64;
 constexpr uint32_t kMarker = 0x7FFFFFFFu;
 constexpr uint32_t kLeafEntry = 0x80000000u;
 constexpr uint32_t kNoEntry = 0xFFFFFFFFu;
-constexpr float kPi = 3.141592653589793f;
+constexpr uint32_t kNoPixel = 0xFFFFFFFFu;
+constexpr uint32_t kNoItem = 0xFFFFFFFFu;
+// Upper bound of traversal steps of one ray; reaching it means a malformed
+// structure: the ray stops and RT_ERR_TIMEOUT is recorded.
+constexpr uint32_t kMaxTraversalSteps = 1u << 22;
+constexpr int kTraceThreads = 128;
+constexpr int kMaxDepth = 64;
+
+constexpr int kModeBounce = 0;   // closest hit of a bounce list -> hit records
+constexpr int kModeShadow = 1;   // any hit of generated shadow rays -> lit counters
+constexpr int kModeRayBuf = 2;   // the API's RtRay -> RtHit query
 
 struct Counters {
     uint32_t primary, secondary, shadow;
     uint32_t nodes, tris, insts;
 };
 
-struct Hit {
-    float t, u, v;
-    uint32_t inst;    // sorted TLAS index (kNoHit when none)
-    uint32_t geom, prim;
-    uint32_t inst_id; // caller's instance index (tie-break key)
-    bool front;
-};
-constexpr uint32_t kNoHit = 0xFFFFFFFFu;
-
-struct Env {
-    const WideNode* tnodes;
-    const InstRecord* insts;
-    const RtModelInfo* models;   // may be null
-    const RtShaderBindingTable* sbt;
-    const RtTextureDesc* textures;
-    uint32_t* status;
-    uint32_t tnode_count;
-    uint32_t inst_count;
-};
-
-// Upper bound of loop iterations of one traversal; reaching it means a
-// malformed structure: the ray stops and RT_ERR_TIMEOUT is recorded.
-constexpr uint32_t kMaxTraversalSteps = 1u << 22;
-
-__device__ __forceinline__ Env make_env(uint64_t tlas, const RtPushConstantBufferAddresses& push,
-                                        const RtShaderBindingTable* sbt, const RtTextureDesc* tex, uint32_t* status) {
-    Env e;
-    const uint8_t* base = reinterpret_cast<const uint8_t*>(tlas);
-    const AsHeader* h = reinterpret_cast<const AsHeader*>(base);
-    e.tnodes = reinterpret_cast<const WideNode*>(base + h->nodes_offset);
-    e.insts = reinterpret_cast<const InstRecord*>(base + h->prims_offset);
-    bool ok = h->magic == kAsMagic && h->type == kAsTypeTop;
-    e.tnode_count = ok ? h->node_count : 0u;
-    e.inst_count = ok ? h->prim_count : 0u;
-    if (!ok) atomicOr(status, 1u << RT_ERR_BAD_AS);
-    e.models = reinterpret_cast<const RtModelInfo*>(push.model_info);
-    e.sbt = sbt;
-    e.textures = tex;
-    e.status = status;
-    return e;
+__device__ __forceinline__ uint32_t lanemask_lt() {
+    uint32_t m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
 }
 
-// ---------------------------------------------------------------------------
-// Textures: software sampling, REPEAT, fixed arithmetic order (oracle twin).
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ int wrap_i(int i, int n) {
-    int r = i % n;
-    return r < 0 ? r + n : r;
-}
-
-__device__ __forceinline__ float4 texel_fetch(const RtTextureDesc& t, int x, int y) {
-    const uint8_t* row = reinterpret_cast<const uint8_t*>(t.address) + (size_t)y * t.row_pitch;
-    if (t.format == RT_FORMAT_R32G32B32A32_SFLOAT) {
-        return __ldg(reinterpret_cast<const float4*>(row) + x);
+// Index for this lane in a warp-aggregated append (one atomic per warp).
+// Every converged lane must call it; `pred` selects the appending lanes.
+__device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool pred) {
+    unsigned m = __activemask();
+    unsigned b = __ballot_sync(m, pred);
+    uint32_t base = 0;
+    if (b) {
+        int leader = __ffs(b) - 1;
+        if ((int)(threadIdx.x & 31u) == leader) base = atomicAdd(counter, (uint32_t)__popc(b));
+        base = __shfl_sync(m, base, leader);
     }
-    uint32_t p = __ldg(reinterpret_cast<const uint32_t*>(row) + x);
-    uint32_t r = p & 0xFFu, g = (p >> 8) & 0xFFu, b = (p >> 16) & 0xFFu, a = p >> 24;
-    float4 o;
-    if (t.format == RT_FORMAT_R8G8B8A8_SRGB) {
-        o.x = c_srgb_lut[r];
-        o.y = c_srgb_lut[g];
-        o.z = c_srgb_lut[b];
-    } else {
-        o.x = (float)r / 255.0f;
-        o.y = (float)g / 255.0f;
-        o.z = (float)b / 255.0f;
-    }
-    o.w = (float)a / 255.0f;
-    return o;
-}
-
-__device__ float4 tex_sample(const RtTextureDesc& t, float u, float v) {
-    if (t.address == 0 || t.width == 0 || t.height == 0) return make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    int w = (int)t.width, h = (int)t.height;
-    if (t.filter == RT_FILTER_LINEAR) {
-        float x = u * (float)w - 0.5f, y = v * (float)h - 0.5f;
-        float x0 = floorf(x), y0 = floorf(y);
-        float fx = x - x0, fy = y - y0;
-        int ix = wrap_i((int)fmaxf(fminf(x0, 2.0e9f), -2.0e9f), w);
-        int iy = wrap_i((int)fmaxf(fminf(y0, 2.0e9f), -2.0e9f), h);
-        int ix1 = ix + 1 == w ? 0 : ix + 1, iy1 = iy + 1 == h ? 0 : iy + 1;
-        float4 t00 = texel_fetch(t, ix, iy), t10 = texel_fetch(t, ix1, iy);
-        float4 t01 = texel_fetch(t, ix, iy1), t11 = texel_fetch(t, ix1, iy1);
-        float w00 = (1.0f - fx) * (1.0f - fy), w10 = fx * (1.0f - fy);
-        float w01 = (1.0f - fx) * fy, w11 = fx * fy;
-        float4 o;
-        o.x = ((w00 * t00.x + w10 * t10.x) + w01 * t01.x) + w11 * t11.x;
-        o.y = ((w00 * t00.y + w10 * t10.y) + w01 * t01.y) + w11 * t11.y;
-        o.z = ((w00 * t00.z + w10 * t10.z) + w01 * t01.z) + w11 * t11.z;
-        o.w = ((w00 * t00.w + w10 * t10.w) + w01 * t01.w) + w11 * t11.w;
-        return o;
-    }
-    float x = floorf(u * (float)w), y = floorf(v * (float)h);
-    int ix = wrap_i((int)fmaxf(fminf(x, 2.0e9f), -2.0e9f), w);
-    int iy = wrap_i((int)fmaxf(fminf(y, 2.0e9f), -2.0e9f), h);
-    return texel_fetch(t, ix, iy);
-}
-
-__device__ __forceinline__ const RtHitGroup* hit_group(const Env& e, uint32_t sbt_flags, uint32_t ray_sbt_offset) {
-    if (!e.sbt) return nullptr;
-    uint32_t gi = (sbt_flags & 0xFFFFFFu) + ray_sbt_offset;
-    if (gi >= e.sbt->hit_group_count || gi >= RT_MAX_HIT_GROUPS) return nullptr;
-    return &e.sbt->hit_groups[gi];
-}
-
-// any_hit_alpha_clip.glsl:11-29
-__device__ bool alpha_clip_accepts(const Env& e, uint32_t custom, uint32_t geom, uint32_t prim, float u, float v) {
-    const RtModelInfo m = e.models[custom];
-    const RtGeometryInfo* gis = reinterpret_cast<const RtGeometryInfo*>(m.geometry_info_address);
-    const RtGeometryInfo gi = gis[geom];
-    const uint32_t* idx = reinterpret_cast<const uint32_t*>(gi.index_buffer_address) + 3 * (size_t)prim;
-    const float* uvs = reinterpret_cast<const float*>(m.uv_buffer_address);
-    uint32_t i0 = idx[0], i1 = idx[1], i2 = idx[2];
-    float w0 = (1.0f - u) - v;
-    float uvx = (uvs[2 * i0] * w0 + uvs[2 * i1] * u) + uvs[2 * i2] * v;
-    float uvy = (uvs[2 * i0 + 1] * w0 + uvs[2 * i1 + 1] * u) + uvs[2 * i2 + 1] * v;
-    uint32_t ti = gi.images.diffuse_image_index;
-    if (ti >= RT_MAX_BOUND_IMAGES) return true;
-    float4 c = tex_sample(e.textures[ti], uvx, uvy);
-    return !(c.w < 0.5f);
-}
-
-__device__ __forceinline__ bool id_less(uint32_t i, uint32_t g, uint32_t p, const Hit& b) {
-    if (i != b.inst_id) return i < b.inst_id;
-    if (g != b.geom) return g < b.geom;
-    return p < b.prim;
+    return base + __popc(b & lanemask_lt());
 }
 
 __device__ __forceinline__ uint32_t pick8(const uint32_t v[8], uint32_t s) {
@@ -178,12 +85,12 @@ __device__ __forceinline__ uint32_t pick8(const uint32_t v[8], uint32_t s) {
     return r;
 }
 
-#define RT_CSWAP(a, b)               \
-    {                                \
+#define RT_CSWAP(a, b)                  \
+    {                                   \
         uint32_t lo_ = min(k[a], k[b]); \
         uint32_t hi_ = max(k[a], k[b]); \
-        k[a] = lo_;                  \
-        k[b] = hi_;                  \
+        k[a] = lo_;                     \
+        k[b] = hi_;                     \
     }
 
 // Optimal 19-comparator sorting network for 8 keys.
@@ -196,60 +103,108 @@ __device__ __forceinline__ void sort8(uint32_t k[8]) {
     RT_CSWAP(1, 2) RT_CSWAP(3, 4) RT_CSWAP(5, 6)
 }
 
-// One traceRayEXT.  Returns with best.inst == kNoHit on a miss.
+// ---------------------------------------------------------------------------
+// Traversal state of one ray (one lane)
+// ---------------------------------------------------------------------------
+struct Trav {
+    V3 wo, wd;                 // world ray
+    V3 o, d, inv;              // ray in the current space (world or object)
+    WtRay wt;                  // watertight shear of the object-space ray
+    float tmin;
+    float t, u, v;             // best hit so far (t = tmax before any hit)
+    uint32_t hit_inst;         // sorted TLAS index of the best hit, kNoHit if none
+    uint32_t hit_geom, hit_prim;
+    bool front, in_blas;
+    uint32_t entry;            // what the next step processes
+    int sp;
+    const WideNode* nodes;
+    const TriRecord* tris;
+    uint32_t node_count, tri_count;
+    uint32_t c_inst, c_sbt_flags;  // the instance being traversed
+    uint32_t steps;
+};
+
+__device__ __forceinline__ void trav_begin(Trav& s, const Env& e, V3 o, V3 d, float tmin, float tmax) {
+    s.wo = o;
+    s.wd = d;
+    s.o = o;
+    s.d = d;
+    s.inv = safe_inv(d);
+    s.wt.kx = s.wt.ky = s.wt.kz = 0;
+    s.wt.sx = s.wt.sy = s.wt.sz = 0.0f;
+    s.tmin = tmin;
+    s.t = tmax;
+    s.u = s.v = 0.0f;
+    s.hit_inst = kNoHit;
+    s.hit_geom = s.hit_prim = kNoHit;
+    s.front = false;
+    s.in_blas = false;
+    s.sp = 0;
+    s.nodes = e.tnodes;
+    s.tris = nullptr;
+    s.node_count = e.tnode_count;
+    s.tri_count = 0;
+    s.c_inst = 0;
+    s.c_sbt_flags = 0;
+    s.steps = 0;
+    s.entry = (e.tnode_count == 0 || !(tmin <= tmax)) ? kNoEntry : 0u;  // 0 = TLAS root
+}
+
+__device__ __forceinline__ void trav_pop(Trav& s, const uint2* stack) {
+    const float cull = s.t * kBoxFarScale;
+    while (s.sp > 0) {
+        uint2 en = stack[--s.sp];
+        if (en.x != kMarker && __uint_as_float(en.y) > cull) continue;
+        s.entry = en.x;
+        return;
+    }
+    s.entry = kNoEntry;
+}
+
+__device__ __forceinline__ void trav_restore_world(Trav& s, const Env& e) {
+    s.in_blas = false;
+    s.nodes = e.tnodes;
+    s.node_count = e.tnode_count;
+    s.o = s.wo;
+    s.d = s.wd;
+    s.inv = safe_inv(s.wd);
+}
+
+// (inst, geom, prim) below the best hit's, comparing caller instance indices
+// (only reached on an exact tie in t).
+__device__ __noinline__ bool ids_below_best(const InstRecord* insts, uint32_t c_inst, uint32_t hit_inst,
+                                            uint32_t geom, uint32_t prim, uint32_t hit_geom, uint32_t hit_prim) {
+    uint32_t ci = insts[c_inst].instance_id, bi = insts[hit_inst].instance_id;
+    if (ci != bi) return ci < bi;
+    if (geom != hit_geom) return geom < hit_geom;
+    return prim < hit_prim;
+}
+
+// One traversal step.  Returns true when the ray is finished (s.t/hit_* hold
+// the result; with terminate-on-first-hit, any accepted hit finishes it).
 template <bool STATS>
-__device__ void traverse(const Env& e, V3 wo, V3 wd, float tmin, float tmax, uint32_t ray_flags, uint32_t cull_mask,
-                         uint32_t ray_sbt_offset, Hit& best, Counters& cnt) {
-    best.t = tmax;
-    best.u = best.v = 0.0f;
-    best.inst = kNoHit;
-    best.inst_id = kNoHit;
-    best.geom = kNoHit;
-    best.prim = kNoHit;
-    best.front = false;
-    const bool terminate_first = (ray_flags & RT_RAY_FLAG_TERMINATE_ON_FIRST_HIT) != 0;
-
-    uint2 stack[kStackSize];
-    int sp = 0;
-
-    V3 winv = safe_inv(wd);
-    V3 o = wo, d = wd, inv = winv;
-    WtRay wt;
-    wt.kx = wt.ky = wt.kz = 0;
-    wt.sx = wt.sy = wt.sz = 0.0f;
-    const WideNode* nodes = e.tnodes;
-    const TriRecord* tris = nullptr;
-    uint32_t node_count = e.tnode_count, tri_count = 0;
-    bool in_blas = false;
-    // current instance
-    uint32_t c_inst = 0, c_inst_id = 0, c_custom = 0, c_sbt_flags = 0;
-
-    uint32_t entry = 0;  // TLAS root node
-    if (node_count == 0) return;
-    for (uint32_t steps = 0;; steps++) {
-        if (steps >= kMaxTraversalSteps) {
-            atomicOr(e.status, 1u << RT_ERR_TIMEOUT);
-            return;
-        }
-        if (entry == kMarker) {
-            in_blas = false;
-            nodes = e.tnodes;
-            node_count = e.tnode_count;
-            o = wo;
-            d = wd;
-            inv = winv;
-        } else if ((entry & kLeafEntry) == 0 && entry >= node_count) {
+__device__ __forceinline__ bool trav_step(Trav& s, uint2* stack, const Env& e, uint32_t ray_flags, uint32_t cull_mask,
+                                          uint32_t ray_sbt_offset, Counters& cnt) {
+    const uint32_t entry = s.entry;
+    if (entry == kNoEntry) return true;
+    if (++s.steps > kMaxTraversalSteps) {
+        atomicOr(e.status, 1u << RT_ERR_TIMEOUT);
+        return true;
+    }
+    if (entry == kMarker) {
+        trav_restore_world(s, e);
+    } else if ((entry & kLeafEntry) == 0) {
+        if (entry >= s.node_count) {
             atomicOr(e.status, 1u << RT_ERR_BAD_AS);  // malformed reference: skip it
-        } else if ((entry & kLeafEntry) == 0) {
-            // ---- wide node ----
+        } else {
             if (STATS) cnt.nodes++;
-            const float4* np = reinterpret_cast<const float4*>(nodes + entry);
+            const float4* np = reinterpret_cast<const float4*>(s.nodes + entry);
             float4 a0 = __ldg(np + 0), a1 = __ldg(np + 1), b0 = __ldg(np + 2), b1 = __ldg(np + 3);
             float4 c0 = __ldg(np + 4), c1 = __ldg(np + 5), d0 = __ldg(np + 6), d1 = __ldg(np + 7);
             float4 e0 = __ldg(np + 8), e1 = __ldg(np + 9), f0 = __ldg(np + 10), f1 = __ldg(np + 11);
             uint4 r0 = __ldg(reinterpret_cast<const uint4*>(np + 12));
             uint4 r1 = __ldg(reinterpret_cast<const uint4*>(np + 13));
-            uint4 mm = __ldg(reinterpret_cast<const uint4*>(np + 14));
+            uint2 mm = __ldg(reinterpret_cast<const uint2*>(np + 14));
             const float lox[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
             const float hix[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
             const float loy[8] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y, c1.z, c1.w};
@@ -257,15 +212,14 @@ __device__ void traverse(const Env& e, V3 wo, V3 wd, float tmin, float tmax, uin
             const float loz[8] = {e0.x, e0.y, e0.z, e0.w, e1.x, e1.y, e1.z, e1.w};
             const float hiz[8] = {f0.x, f0.y, f0.z, f0.w, f1.x, f1.y, f1.z, f1.w};
             const uint32_t refs[8] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w};
-            const float tcap = best.t;
-            uint32_t keys[8];
-            uint32_t ents[8];
+            const float tcap = s.t;
+            uint32_t keys[8], ents[8];
 #pragma unroll
             for (int k = 0; k < 8; k++) {
-                float t0x = (lox[k] - o.x) * inv.x, t1x = (hix[k] - o.x) * inv.x;
-                float t0y = (loy[k] - o.y) * inv.y, t1y = (hiy[k] - o.y) * inv.y;
-                float t0z = (loz[k] - o.z) * inv.z, t1z = (hiz[k] - o.z) * inv.z;
-                float tn = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fmaxf(fminf(t0z, t1z), tmin));
+                float t0x = (lox[k] - s.o.x) * s.inv.x, t1x = (hix[k] - s.o.x) * s.inv.x;
+                float t0y = (loy[k] - s.o.y) * s.inv.y, t1y = (hiy[k] - s.o.y) * s.inv.y;
+                float t0z = (loz[k] - s.o.z) * s.inv.z, t1z = (hiz[k] - s.o.z) * s.inv.z;
+                float tn = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fmaxf(fminf(t0z, t1z), s.tmin));
                 float tf = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fminf(fmaxf(t0z, t1z), tcap));
                 uint32_t m = node_meta(mm.x, mm.y, k);
                 bool hit = (m != 0u) && (tn <= tf * kBoxFarScale);
@@ -275,314 +229,116 @@ __device__ void traverse(const Env& e, V3 wo, V3 wd, float tmin, float tmax, uin
             }
             sort8(keys);
             if (keys[0] != 0xFFFFFFFFu) {
-                // push the hit children farthest first; the nearest is next.
-                // The stored tnear (key with the slot bits cleared) is rounded
-                // down, so culling on pop stays conservative.
+                // push the other hit children farthest first; the nearest is
+                // next.  The stored tnear is rounded down: culling stays
+                // conservative.
 #pragma unroll
                 for (int q = 7; q >= 1; q--) {
                     uint32_t key = keys[q];
                     if (key == 0xFFFFFFFFu) continue;
-                    if (sp < (int)kStackSize) {
-                        stack[sp++] = make_uint2(pick8(ents, key & 7u), key & ~7u);
-                    } else {
-                        atomicOr(e.status, 1u << RT_ERR_STACK_OVERFLOW);
-                    }
+                    if (s.sp < (int)kStackSize) stack[s.sp++] = make_uint2(pick8(ents, key & 7u), key & ~7u);
+                    else atomicOr(e.status, 1u << RT_ERR_STACK_OVERFLOW);
                 }
-                entry = pick8(ents, keys[0] & 7u);
-                continue;
+                s.entry = pick8(ents, keys[0] & 7u);
+                return false;
+            }
+        }
+    } else {
+        const uint32_t first = entry & 0x0FFFFFFFu;
+        const uint32_t count = ((entry >> 28) & 7u) + 1u;
+        if (first + count > (s.in_blas ? s.tri_count : e.inst_count)) {
+            atomicOr(e.status, 1u << RT_ERR_BAD_AS);  // malformed leaf: skip it
+        } else if (!s.in_blas) {
+            // instance leaf: the record's last 32 bytes hold the BLAS fields
+            const InstRecord* ir = &e.insts[first];
+            const uint4* tail = reinterpret_cast<const uint4*>(&ir->blas);
+            uint4 q0 = __ldg(tail), q1 = __ldg(tail + 1);
+            // q0 = blas lo, blas hi, instance_id, custom_mask; q1 = sbt_flags, tri_count, node_count, prims_off256
+            if (q1.y != 0u && ((q0.w >> 24) & cull_mask) != 0u) {
+                if (STATS) cnt.insts++;
+                const float4* wp = reinterpret_cast<const float4*>(ir->w2o);
+                float4 w0 = __ldg(wp), w1 = __ldg(wp + 1), w2 = __ldg(wp + 2);
+                const float w[12] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w, w2.x, w2.y, w2.z, w2.w};
+                s.o = xform_point(w, s.wo);
+                s.d = xform_dir(w, s.wd);
+                s.inv = safe_inv(s.d);
+                s.wt = wt_setup(s.d);
+                const uint8_t* blas = reinterpret_cast<const uint8_t*>(((uint64_t)q0.y << 32) | q0.x);
+                s.nodes = reinterpret_cast<const WideNode*>(blas + kHeaderBytes);
+                s.tris = reinterpret_cast<const TriRecord*>(blas + (uint64_t)q1.w * 256u);
+                s.node_count = q1.z;
+                s.tri_count = q1.y;
+                s.c_inst = first;
+                s.c_sbt_flags = q1.x;
+                s.in_blas = true;
+                if (s.sp < (int)kStackSize) {
+                    stack[s.sp++] = make_uint2(kMarker, 0u);
+                    s.entry = 0;  // BLAS root
+                    return false;
+                }
+                atomicOr(e.status, 1u << RT_ERR_STACK_OVERFLOW);
+                trav_restore_world(s, e);
             }
         } else {
-            // ---- leaf ----
-            uint32_t first = entry & 0x0FFFFFFFu;
-            uint32_t count = ((entry >> 28) & 7u) + 1u;
-            if (first + count > (in_blas ? tri_count : e.inst_count)) {
-                atomicOr(e.status, 1u << RT_ERR_BAD_AS);  // malformed leaf: skip it
-            } else if (!in_blas) {
-                // instance leaf (one instance per TLAS leaf)
-                const InstRecord* ir = &e.insts[first];
-                uint32_t valid = __ldg(&ir->valid);
-                uint32_t cm = __ldg(&ir->custom_mask);
-                if (valid && ((cm >> 24) & cull_mask) != 0u) {
-                    if (STATS) cnt.insts++;
-                    const float4* wp = reinterpret_cast<const float4*>(ir->w2o);
-                    float4 w0 = __ldg(wp), w1 = __ldg(wp + 1), w2 = __ldg(wp + 2);
-                    const float w[12] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w, w2.x, w2.y, w2.z, w2.w};
-                    o = xform_point(w, wo);
-                    d = xform_dir(w, wd);
-                    inv = safe_inv(d);
-                    wt = wt_setup(d);
-                    uint64_t blas = __ldg(reinterpret_cast<const unsigned long long*>(&ir->blas));
-                    const uint8_t* bb = reinterpret_cast<const uint8_t*>(blas);
-                    const AsHeader* bh = reinterpret_cast<const AsHeader*>(bb);
-                    nodes = reinterpret_cast<const WideNode*>(bb + __ldg(reinterpret_cast<const unsigned long long*>(&bh->nodes_offset)));
-                    tris = reinterpret_cast<const TriRecord*>(bb + __ldg(reinterpret_cast<const unsigned long long*>(&bh->prims_offset)));
-                    node_count = __ldg(&bh->node_count);
-                    tri_count = __ldg(&bh->prim_count);
-                    c_inst = first;
-                    c_inst_id = __ldg(&ir->instance_id);
-                    c_custom = cm & 0xFFFFFFu;
-                    c_sbt_flags = __ldg(&ir->sbt_flags);
-                    in_blas = true;
-                    if (sp < (int)kStackSize) {
-                        stack[sp++] = make_uint2(kMarker, __float_as_uint(-INFINITY));
-                        entry = 0;  // BLAS root
-                        continue;
-                    }
-                    atomicOr(e.status, 1u << RT_ERR_STACK_OVERFLOW);
-                    in_blas = false;
-                    nodes = e.tnodes;
-                    node_count = e.tnode_count;
-                    o = wo;
-                    d = wd;
-                    inv = winv;
+            const uint32_t iflags = s.c_sbt_flags >> 24;
+            for (uint32_t q = 0; q < count; q++) {
+                if (STATS) cnt.tris++;
+                const float4* tp = reinterpret_cast<const float4*>(s.tris + first + q);
+                float4 p0 = __ldg(tp), p1 = __ldg(tp + 1), p2 = __ldg(tp + 2);
+                uint32_t prim = __float_as_uint(p0.w), geom = __float_as_uint(p1.w), tfl = __float_as_uint(p2.w);
+                bool opaque = (tfl & 1u) != 0u;
+                if (iflags & RT_INSTANCE_FORCE_OPAQUE) opaque = true;
+                if (iflags & RT_INSTANCE_FORCE_NO_OPAQUE) opaque = false;
+                if (ray_flags & RT_RAY_FLAG_OPAQUE) opaque = true;
+                if (ray_flags & RT_RAY_FLAG_NO_OPAQUE) opaque = false;
+                if ((ray_flags & RT_RAY_FLAG_CULL_OPAQUE) && opaque) continue;
+                if ((ray_flags & RT_RAY_FLAG_CULL_NO_OPAQUE) && !opaque) continue;
+                float t, u, v;
+                bool front;
+                if (!tri_intersect(s.o, s.wt, mk3(p0.x, p0.y, p0.z), mk3(p1.x, p1.y, p1.z), mk3(p2.x, p2.y, p2.z),
+                                   s.tmin, s.t, &t, &u, &v, &front))
+                    continue;
+                if (iflags & RT_INSTANCE_TRIANGLE_FLIP_FACING) front = !front;
+                if (!(iflags & RT_INSTANCE_TRIANGLE_FACING_CULL_DISABLE)) {
+                    if ((ray_flags & RT_RAY_FLAG_CULL_BACK_FACING) && !front) continue;
+                    if ((ray_flags & RT_RAY_FLAG_CULL_FRONT_FACING) && front) continue;
                 }
-            } else {
-                const uint32_t iflags = c_sbt_flags >> 24;
-                for (uint32_t q = 0; q < count; q++) {
-                    if (STATS) cnt.tris++;
-                    const float4* tp = reinterpret_cast<const float4*>(tris + first + q);
-                    float4 p0 = __ldg(tp), p1 = __ldg(tp + 1), p2 = __ldg(tp + 2);
-                    uint32_t prim = __float_as_uint(p0.w), geom = __float_as_uint(p1.w), tf = __float_as_uint(p2.w);
-                    bool opaque = (tf & 1u) != 0u;
-                    if (iflags & RT_INSTANCE_FORCE_OPAQUE) opaque = true;
-                    if (iflags & RT_INSTANCE_FORCE_NO_OPAQUE) opaque = false;
-                    if (ray_flags & RT_RAY_FLAG_OPAQUE) opaque = true;
-                    if (ray_flags & RT_RAY_FLAG_NO_OPAQUE) opaque = false;
-                    if ((ray_flags & RT_RAY_FLAG_CULL_OPAQUE) && opaque) continue;
-                    if ((ray_flags & RT_RAY_FLAG_CULL_NO_OPAQUE) && !opaque) continue;
-                    float t, u, v;
-                    bool front;
-                    if (!tri_intersect(o, wt, mk3(p0.x, p0.y, p0.z), mk3(p1.x, p1.y, p1.z), mk3(p2.x, p2.y, p2.z), tmin,
-                                       best.t, &t, &u, &v, &front))
+                if (t == s.t && s.hit_inst != kNoHit &&
+                    !ids_below_best(e.insts, s.c_inst, s.hit_inst, geom, prim, s.hit_geom, s.hit_prim))
+                    continue;
+                if (!opaque && e.models) {
+                    const RtHitGroup* g = hit_group(e, s.c_sbt_flags, ray_sbt_offset);
+                    if (g && g->any_hit == RT_PROGRAM_ANY_HIT_ALPHA_CLIP &&
+                        !alpha_clip_accepts(e.models, e.textures, e.insts[s.c_inst].custom_mask & 0xFFFFFFu, geom,
+                                            prim, u, v))
                         continue;
-                    if (iflags & RT_INSTANCE_TRIANGLE_FLIP_FACING) front = !front;
-                    if (!(iflags & RT_INSTANCE_TRIANGLE_FACING_CULL_DISABLE)) {
-                        if ((ray_flags & RT_RAY_FLAG_CULL_BACK_FACING) && !front) continue;
-                        if ((ray_flags & RT_RAY_FLAG_CULL_FRONT_FACING) && front) continue;
-                    }
-                    if (t == best.t && best.inst != kNoHit && !id_less(c_inst_id, geom, prim, best)) continue;
-                    if (!opaque && e.models) {
-                        const RtHitGroup* g = hit_group(e, c_sbt_flags, ray_sbt_offset);
-                        if (g && g->any_hit == RT_PROGRAM_ANY_HIT_ALPHA_CLIP &&
-                            !alpha_clip_accepts(e, c_custom, geom, prim, u, v))
-                            continue;
-                    }
-                    best.t = t;
-                    best.u = u;
-                    best.v = v;
-                    best.inst = c_inst;
-                    best.inst_id = c_inst_id;
-                    best.geom = geom;
-                    best.prim = prim;
-                    best.front = front;
-                    if (terminate_first) return;
+                }
+                s.t = t;
+                s.u = u;
+                s.v = v;
+                s.hit_inst = s.c_inst;
+                s.hit_geom = geom;
+                s.hit_prim = prim;
+                s.front = front;
+                if (ray_flags & RT_RAY_FLAG_TERMINATE_ON_FIRST_HIT) {
+                    s.entry = kNoEntry;
+                    return true;
                 }
             }
         }
-        // ---- pop ----
-        entry = kNoEntry;
-        const float cull = best.t * kBoxFarScale;
-        while (sp > 0) {
-            uint2 s = stack[--sp];
-            if (s.x != kMarker && __uint_as_float(s.y) > cull) continue;
-            entry = s.x;
-            break;
-        }
-        if (entry == kNoEntry) return;
     }
-}
-
-// ---------------------------------------------------------------------------
-// Shading (colour arithmetic; compared with a tolerance against the oracle)
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ float clampf(float x, float lo, float hi) { return fminf(fmaxf(x, lo), hi); }
-
-// pbr.glsl:56-65
-__device__ __forceinline__ float v_smith_ggx_correlated(float NoV, float NoL, float roughness) {
-    float a2 = roughness * roughness;
-    float GGXV = NoL * sqrtf(NoV * NoV * (1.0f - a2) + a2);
-    float GGXL = NoV * sqrtf(NoL * NoL * (1.0f - a2) + a2);
-    return 0.5f / (GGXV + GGXL);
-}
-// pbr.glsl:44-51
-__device__ __forceinline__ float d_ggx(float NoH, float roughness) {
-    float a = NoH * roughness;
-    float k = roughness / (1.0f - NoH * NoH + a * a);
-    return k * k * (1.0f / kPi);
-}
-// pbr.glsl:74-76
-__device__ __forceinline__ float f_schlick1(float u, float f0, float f90) {
-    return f0 + (f90 - f0) * powf(1.0f - u, 5.0f);
-}
-// lib.rs:85-92
-__device__ __forceinline__ float linear_to_srgb(float x) {
-    if (x <= 0.0031308f) return x * 12.92f;
-    return 1.055f * powf(x, 1.0f / 2.4f) - 0.055f;
-}
-__device__ __forceinline__ uint32_t to_unorm8(float x) {
-    float c = fminf(fmaxf(x, 0.0f), 1.0f);
-    return (uint32_t)(c * 255.0f + 0.5f);
-}
-// heatmap.rs:44-47
-__device__ __forceinline__ float smoothstep(float e0, float e1, float x) {
-    float t = clampf((x - e0) / (e1 - e0), 0.0f, 1.0f);
-    return t * t * (3.0f - 2.0f * t);
-}
-// heatmap.rs:5-38 (index clamped to 9 at heat == 1)
-__constant__ float c_heat_palette[10][3] = {
-    {0.0f / 255.0f, 2.0f / 255.0f, 91.0f / 255.0f},     {0.0f / 255.0f, 108.0f / 255.0f, 251.0f / 255.0f},
-    {0.0f / 255.0f, 221.0f / 255.0f, 221.0f / 255.0f},  {51.0f / 255.0f, 221.0f / 255.0f, 0.0f / 255.0f},
-    {255.0f / 255.0f, 252.0f / 255.0f, 0.0f / 255.0f},  {255.0f / 255.0f, 180.0f / 255.0f, 0.0f / 255.0f},
-    {255.0f / 255.0f, 104.0f / 255.0f, 0.0f / 255.0f},  {226.0f / 255.0f, 22.0f / 255.0f, 0.0f / 255.0f},
-    {191.0f / 255.0f, 0.0f / 255.0f, 83.0f / 255.0f},   {145.0f / 255.0f, 0.0f / 255.0f, 65.0f / 255.0f},
-};
-__device__ V3 heatmap_temperature(float heat) {
-    const float(*C)[3] = c_heat_palette;
-    float h = clampf(heat, 0.0f, 1.0f) * 10.0f;
-    int hi = (int)h;
-    int cur = hi > 9 ? 9 : hi;
-    int prv = hi - 1 > 0 ? hi - 1 : 0;
-    if (prv > 9) prv = 9;
-    int nxt = hi + 1 < 9 ? hi + 1 : 9;
-    float hf = floorf(h), hc = -floorf(-h);
-    float blur = 0.8f;
-    float wc = smoothstep(hf - blur, hf + blur, h) * (1.0f - smoothstep(hc - blur, hc + blur, h));
-    float wp = 1.0f - smoothstep(hf - blur, hf + blur, h);
-    float wn = smoothstep(hc - blur, hc + blur, h);
-    float r[3];
-    for (int k = 0; k < 3; k++) r[k] = clampf(wc * C[cur][k] + wp * C[prv][k] + wn * C[nxt][k], 0.0f, 1.0f);
-    return mk3(r[0], r[1], r[2]);
-}
-
-// pbr.glsl:174-211 split at the light intensity: out = (I * NoL) * comb.
-__device__ void brdf_parts(V3 n, V3 v, V3 l, float pr, V3 base, float metallic, bool lambert, float* NoL_out,
-                           V3* comb_out) {
-    V3 h = normalize3(add3(v, l));
-    float rough = pr * pr;
-    float NoV = clampf(dot3(n, v), 10.0e-10f, 1.0f);
-    float NoH = clampf(dot3(n, h), 0.0f, 1.0f);
-    float NoL = clampf(dot3(n, l), 0.0f, 1.0f);
-    float LoH = clampf(dot3(l, h), 0.0f, 1.0f);
-    float D = d_ggx(NoH, rough);
-    float dielectric_f0 = 0.16f * 0.5f * 0.5f;
-    float f90 = 0.5f + 2.0f * rough * LoH * LoH;
-    float V = v_smith_ggx_correlated(NoV, NoL, rough);
-    float fd = lambert ? (1.0f / kPi) : f_schlick1(NoL, 1.0f, f90) * f_schlick1(NoV, 1.0f, f90) * (1.0f / kPi);
-    float p5 = powf(1.0f - LoH, 5.0f);
-    float b3[3] = {base.x, base.y, base.z};
-    float c3[3];
-    for (int k = 0; k < 3; k++) {
-        float f0 = dielectric_f0 * (1.0f - metallic) + b3[k] * metallic;
-        float F = f0 + (f90 - f0) * p5;
-        float spec = (D * V) * F;
-        float diff = b3[k] * fd;
-        c3[k] = diff + spec;
-    }
-    *NoL_out = NoL;
-    *comb_out = mk3(c3[0], c3[1], c3[2]);
-}
-
-struct TriData {
-    V3 p[3], n[3];
-    float uv[3][2];
-    RtGeometryInfo gi;
-};
-
-// hit_shader_common.glsl:83-87,144-154
-__device__ __forceinline__ bool load_triangle(const Env& e, uint32_t custom, uint32_t geom, uint32_t prim, TriData* td) {
-    if (!e.models) return false;
-    const RtModelInfo m = e.models[custom];
-    const RtGeometryInfo* gis = reinterpret_cast<const RtGeometryInfo*>(m.geometry_info_address);
-    td->gi = gis[geom];
-    const uint32_t* idx = reinterpret_cast<const uint32_t*>(td->gi.index_buffer_address) + 3 * (size_t)prim;
-    const float* P = reinterpret_cast<const float*>(m.position_buffer_address);
-    const float* N = reinterpret_cast<const float*>(m.normal_buffer_address);
-    const float* UV = reinterpret_cast<const float*>(m.uv_buffer_address);
-    for (int k = 0; k < 3; k++) {
-        uint32_t i = idx[k];
-        td->p[k] = mk3(P[3 * (size_t)i], P[3 * (size_t)i + 1], P[3 * (size_t)i + 2]);
-        td->n[k] = mk3(N[3 * (size_t)i], N[3 * (size_t)i + 1], N[3 * (size_t)i + 2]);
-        td->uv[k][0] = UV[2 * (size_t)i];
-        td->uv[k][1] = UV[2 * (size_t)i + 1];
-    }
-    return true;
-}
-
-// closest_hit_textured.glsl:13-19
-__device__ __forceinline__ V3 project_onto_tangent_plane(V3 point, V3 vp, V3 vn) {
-    V3 vtp = sub3(point, vp);
-    float dp = fminf(0.0f, dot3(vtp, vn));
-    return sub3(vtp, mul3s(vn, dp));
-}
-
-// closest_hit_textured.glsl:99-111 (nearest-sampled texel of a 64-wide tile)
-__device__ __forceinline__ float blue_noise_r(const Env& e, uint32_t tex, uint32_t x, uint32_t y, uint32_t ox,
-                                              uint32_t oy) {
-    if (tex >= RT_MAX_BOUND_IMAGES) return 0.0f;
-    float4 c = tex_sample(e.textures[tex], (float)(x + ox) / 64.0f, (float)(y + oy) / 64.0f);
-    return c.x;
-}
-
-// closest_hit_textured.glsl:77-120: blue noise -> animated -> light sample
-__device__ V3 shadow_direction(const Env& e, const RtUniforms& U, uint32_t x, uint32_t y, uint32_t i, V3 sun_dir) {
-    float bx = blue_noise_r(e, U.blue_noise_texture_index, x, y, i * 2u * 13u, i * 2u * 41u);
-    float by = blue_noise_r(e, U.blue_noise_texture_index, x, y, (i * 2u + 1u) * 13u, (i * 2u + 1u) * 41u);
-    float g = (float)(U.frame_index % 32u) * 0.618033988749f;
-    float sx = bx + g, sy = by + g;
-    float rx = sx - floorf(sx), ry = sy - floorf(sy);
-    float rad = sqrtf(rx);
-    float ang = (ry * 2.0f) * kPi;
-    float sn, cs;
-    rt_sincos(ang, &sn, &cs);
-    float px = (rad * cs) * U.sun_radius, py = (rad * sn) * U.sun_radius;
-    V3 tangent = normalize3(cross3(sun_dir, mk3(0.0f, 1.0f, 0.0f)));
-    V3 bitangent = normalize3(cross3(tangent, sun_dir));
-    return normalize3(add3(add3(sun_dir, mul3s(tangent, px)), mul3s(bitangent, py)));
-}
-
-// Material + normal + BRDF terms of closest_hit_textured.glsl:174-226.
-__device__ void shade_textured(const Env& e, const TriData& td, V3 inrm, float u_, float v_, const float* w2o,
-                               V3 dir, V3 sun_dir, bool lambert, float* NoL, V3* comb, V3* amb) {
-    const RtGeometryInfo& gi = td.gi;
-    float4 dtex = make_float4(0, 0, 0, 0), mr = make_float4(0, 0, 0, 0);
-    if (gi.images.diffuse_image_index < RT_MAX_BOUND_IMAGES)
-        dtex = tex_sample(e.textures[gi.images.diffuse_image_index], u_, v_);
-    if (gi.images.metallic_roughness_image_index < RT_MAX_BOUND_IMAGES)
-        mr = tex_sample(e.textures[gi.images.metallic_roughness_image_index], u_, v_);
-    float metallic = mr.z, roughness = mr.y;
-    V3 base = mk3(dtex.x, dtex.y, dtex.z);
-    V3 normal;
-    int nmi = gi.images.normal_map_image_index;
-    if (nmi < 0 || (uint32_t)nmi >= RT_MAX_BOUND_IMAGES) {
-        normal = normalize3(xform_normal_w2o_t(w2o, inrm));
-    } else {
-        float4 nm = tex_sample(e.textures[nmi], u_, v_);
-        V3 map = mk3(nm.x * 2.0f - 1.0f, nm.y * 2.0f - 1.0f, nm.z * 2.0f - 1.0f);
-        V3 dp1 = sub3(td.p[1], td.p[0]), dp2 = sub3(td.p[2], td.p[0]);
-        float du1x = td.uv[1][0] - td.uv[0][0], du1y = td.uv[1][1] - td.uv[0][1];
-        float du2x = td.uv[2][0] - td.uv[0][0], du2y = td.uv[2][1] - td.uv[0][1];
-        V3 dp2perp = cross3(dp2, inrm), dp1perp = cross3(inrm, dp1);
-        V3 T = add3(mul3s(dp2perp, du1x), mul3s(dp1perp, du2x));
-        V3 B = add3(mul3s(dp2perp, du1y), mul3s(dp1perp, du2y));
-        float tt = dot3(T, T), bb = dot3(B, B);
-        float invmax = 1.0f / sqrtf(tt > bb ? tt : bb);
-        V3 m = normalize3(map);
-        V3 local = mk3((T.x * invmax * m.x + B.x * invmax * m.y) + inrm.x * m.z,
-                       (T.y * invmax * m.x + B.y * invmax * m.y) + inrm.y * m.z,
-                       (T.z * invmax * m.x + B.z * invmax * m.y) + inrm.z * m.z);
-        normal = normalize3(xform_normal_w2o_t(w2o, local));
-    }
-    V3 view = mk3(-dir.x, -dir.y, -dir.z);
-    brdf_parts(normal, view, sun_dir, roughness, base, metallic, lambert, NoL, comb);
-    *amb = mk3(0.1f * base.x, 0.1f * base.y, 0.1f * base.z);
+    trav_pop(s, stack);
+    return s.entry == kNoEntry;
 }
 
 __device__ __forceinline__ void flush_counters(RtStats* st, const Counters& c) {
-    atomicAdd(reinterpret_cast<unsigned long long*>(&st->traversals),
-              (unsigned long long)(c.primary + c.secondary + c.shadow));
-    atomicAdd(reinterpret_cast<unsigned long long*>(&st->primary_rays), (unsigned long long)c.primary);
-    atomicAdd(reinterpret_cast<unsigned long long*>(&st->secondary_rays), (unsigned long long)c.secondary);
-    atomicAdd(reinterpret_cast<unsigned long long*>(&st->shadow_rays), (unsigned long long)c.shadow);
+    unsigned long long tr = (unsigned long long)c.primary + c.secondary + c.shadow;
+    if (tr) {
+        atomicAdd(reinterpret_cast<unsigned long long*>(&st->traversals), tr);
+        atomicAdd(reinterpret_cast<unsigned long long*>(&st->primary_rays), (unsigned long long)c.primary);
+        atomicAdd(reinterpret_cast<unsigned long long*>(&st->secondary_rays), (unsigned long long)c.secondary);
+        atomicAdd(reinterpret_cast<unsigned long long*>(&st->shadow_rays), (unsigned long long)c.shadow);
+    }
     if (c.nodes | c.tris | c.insts) {
         atomicAdd(reinterpret_cast<unsigned long long*>(&st->nodes_visited), (unsigned long long)c.nodes);
         atomicAdd(reinterpret_cast<unsigned long long*>(&st->triangles_tested), (unsigned long long)c.tris);
@@ -590,186 +346,267 @@ __device__ __forceinline__ void flush_counters(RtStats* st, const Counters& c) {
     }
 }
 
-struct TraceParams {
-    TraceLaunch L;
-    uint32_t tiles_x;
-    uint32_t total;        // tiles * 32
-    uint32_t* work;        // fetch counter (zeroed before launch)
+// ---------------------------------------------------------------------------
+// Wavefront buffers (the per-stream workspace of the context)
+// ---------------------------------------------------------------------------
+struct WfCounters {
+    uint32_t ray_count[kMaxDepth + 1];  // rays of each bounce list
+    uint32_t shadow_count;              // pixels with a textured hit
+    uint32_t work[kMaxDepth + 2];       // fetch counters of the persistent trace launches
 };
 
-constexpr uint32_t kPhaseRay = 0;
-constexpr uint32_t kPhaseShadow = 1;
+struct WfBuffers {
+    float4* rays[2];           // per ray: (origin, tmin), (direction, tmax)
+    uint32_t* ray_pixel[2];    // pixel of each ray, kNoPixel for padding
+    uint4* hits;               // per ray: (t, u, v, inst), (geom, prim, front, 0)
+    float4* colour;            // per pixel, linear
+    float4* shade;             // per pixel: (so.xyz, NoL), (comb.xyz, amb.x), (amb.yz, 0, 0)
+    uint32_t* lit;             // per pixel: shadow rays that missed
+    uint32_t* shadow_list;     // pixels with a textured hit
+    unsigned long long* heat;  // per pixel traversal clock cycles (heatmap)
+    WfCounters* ctr;
+};
 
-// ray_generation (lib.rs:95-191) as a per-pixel state machine.
-template <bool STATS>
-__global__ void __launch_bounds__(128) k_trace_rays(const __grid_constant__ TraceParams P) {
+struct WfParams {
+    TraceLaunch L;
+    WfBuffers B;
+    uint32_t tiles_x;
+    uint32_t total;            // ray slots of the primary list (tiles * 32)
+    uint32_t bounce;
+};
+
+__device__ __forceinline__ void tile_pixel(uint32_t i, uint32_t tiles_x, uint32_t* x, uint32_t* y) {
+    uint32_t tile = i >> 5, l = i & 31u;
+    *x = (tile % tiles_x) * 8u + (l & 7u);
+    *y = (tile / tiles_x) * 4u + (l >> 3);
+}
+
+// ray_generation, lib.rs:126-142 (camera ray, fixed operation order)
+__global__ void k_raygen(const __grid_constant__ WfParams P) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.total) return;
+    const RtUniforms& U = *reinterpret_cast<const RtUniforms*>(P.L.push.uniforms);
+    const uint32_t W = P.L.desc.width, H = P.L.desc.height;
+    uint32_t x, y;
+    tile_pixel(i, P.tiles_x, &x, &y);
+    float4* R = P.B.rays[0];
+    if (x < W && y < H) {
+        float pcx = (float)x + 0.5f, pcy = (float)y + 0.5f;
+        float tcx = pcx / (float)W, tcy = pcy / (float)H;
+        float rx = tcx * 2.0f - 1.0f, ry = tcy * 2.0f - 1.0f;
+        const float* VI = U.view_inverse;
+        const float* PI = U.proj_inverse;
+        V3 ro = mk3(mat4_row(VI, 0, 0.0f, 0.0f, 0.0f, 1.0f), mat4_row(VI, 1, 0.0f, 0.0f, 0.0f, 1.0f),
+                    mat4_row(VI, 2, 0.0f, 0.0f, 0.0f, 1.0f));
+        V3 target = mk3(mat4_row(PI, 0, rx, ry, 1.0f, 1.0f), mat4_row(PI, 1, rx, ry, 1.0f, 1.0f),
+                        mat4_row(PI, 2, rx, ry, 1.0f, 1.0f));
+        V3 local = normalize3(target);
+        V3 rd = mk3(mat4_row(VI, 0, local.x, local.y, local.z, 0.0f), mat4_row(VI, 1, local.x, local.y, local.z, 0.0f),
+                    mat4_row(VI, 2, local.x, local.y, local.z, 0.0f));
+        R[2 * (size_t)i] = make_float4(ro.x, ro.y, ro.z, 0.01f);
+        R[2 * (size_t)i + 1] = make_float4(rd.x, rd.y, rd.z, 10000.0f);
+        P.B.ray_pixel[0][i] = y * W + x;
+    } else {
+        R[2 * (size_t)i] = make_float4(0.0f, 0.0f, 0.0f, 1.0f);  // tmin > tmax: never traversed
+        R[2 * (size_t)i + 1] = make_float4(0.0f, 0.0f, 1.0f, 0.0f);
+        P.B.ray_pixel[0][i] = kNoPixel;
+    }
+    if (i == 0) P.B.ctr->ray_count[0] = P.total;
+}
+
+// Persistent trace kernel with per-lane ray replacement.
+template <int MODE, bool STATS>
+__global__ void __launch_bounds__(kTraceThreads) k_trace(const __grid_constant__ WfParams P) {
     const TraceLaunch& L = P.L;
-    const RtUniforms& U = *reinterpret_cast<const RtUniforms*>(L.push.uniforms);
     const Env e = make_env(L.push.acceleration_structure, L.push, &L.sbt, L.textures, L.status);
-    const uint32_t W = L.desc.width, H = L.desc.height;
-    const uint32_t max_depth = L.desc.max_trace_depth;
+    const RtUniforms& U = *reinterpret_cast<const RtUniforms*>(L.push.uniforms);
+    const uint32_t b = P.bounce;
     const uint32_t nshadow = L.desc.shadow_ray_count;
-    const bool lambert = (L.desc.flags & RT_TRACE_FLAG_LAMBERT_DIFFUSE) != 0;
+    const bool heat = MODE != kModeRayBuf && U.show_heatmap != 0;
+    uint32_t total;
+    uint32_t* work;
+    if (MODE == kModeBounce) {
+        total = P.B.ctr->ray_count[b];
+        work = &P.B.ctr->work[b];
+    } else {
+        total = P.B.ctr->shadow_count * nshadow;
+        work = &P.B.ctr->work[kMaxDepth + 1];
+    }
+    const uint32_t ray_flags = MODE == kModeShadow
+                                   ? (RT_RAY_FLAG_TERMINATE_ON_FIRST_HIT | RT_RAY_FLAG_SKIP_CLOSEST_HIT_SHADER)
+                                   : RT_RAY_FLAG_NONE;
+    const uint32_t sbt_offset = MODE == kModeShadow ? 1u : 0u;
     const V3 sun_dir = mk3(U.sun_dir[0], U.sun_dir[1], U.sun_dir[2]);
-    float sun_s, sun_c;
-    rt_sincos(U.sun_radius, &sun_s, &sun_c);
-    const uint32_t lane = threadIdx.x & 31u;
-    const uint32_t lanemask_lt = (1u << lane) - 1u;
-    uint32_t* img = reinterpret_cast<uint32_t*>(L.desc.image_address);
-    float4* rad = reinterpret_cast<float4*>(L.desc.radiance_address);
+    const uint32_t W = L.desc.width;
 
     Counters cnt = {0, 0, 0, 0, 0, 0};
-    bool has = false;
-    uint32_t x = 0, y = 0, phase = kPhaseRay, bounce = 0, shadow_i = 0;
-    V3 ro = mk3(0, 0, 0), rd = mk3(0, 0, 0), so = mk3(0, 0, 0), comb = mk3(0, 0, 0), amb = mk3(0, 0, 0);
-    V3 col = mk3(0, 0, 0);
-    float NoL = 0.0f, lit = 0.0f;
-    long long t_start = 0;
-
+    uint2 stack[kStackSize];
+    Trav s;
+    uint32_t item = kNoItem, pix = kNoPixel;
+    long long t0 = 0;
     for (;;) {
-        // ---- refill idle lanes (warp-aggregated fetch of tile pixels) ----
-        unsigned m = __activemask();
-        unsigned idle = __ballot_sync(m, !has);
-        if (idle) {
-            int leader = __ffs(idle) - 1;
-            uint32_t base = 0;
-            if ((int)lane == leader) base = atomicAdd(P.work, (uint32_t)__popc(idle));
-            base = __shfl_sync(m, base, leader);
-            if (!has) {
-                uint32_t my = base + __popc(idle & lanemask_lt);
-                while (my < P.total) {
-                    uint32_t tile = my >> 5, l = my & 31u;
-                    uint32_t tx = tile % P.tiles_x, ty = tile / P.tiles_x;
-                    x = tx * 8u + (l & 7u);
-                    y = ty * 4u + (l >> 3);
-                    if (x < W && y < H) {
-                        has = true;
-                        break;
-                    }
-                    my = atomicAdd(P.work, 1u);  // outside the image: take another
+        uint32_t my = warp_append(work, item == kNoItem);
+        if (item == kNoItem) {
+            if (my >= total) break;
+            item = my;
+            if (MODE == kModeBounce) {
+                float4 a = P.B.rays[b & 1][2 * (size_t)item], c = P.B.rays[b & 1][2 * (size_t)item + 1];
+                pix = P.B.ray_pixel[b & 1][item];
+                trav_begin(s, e, mk3(a.x, a.y, a.z), mk3(c.x, c.y, c.z), a.w, c.w);
+                if (pix != kNoPixel) {
+                    if (b == 0) cnt.primary++;
+                    else cnt.secondary++;
                 }
-                if (has) {
-                    if (U.show_heatmap) t_start = clock64();
-                    // lib.rs:126-142
-                    float pcx = (float)x + 0.5f, pcy = (float)y + 0.5f;
-                    float tcx = pcx / (float)W, tcy = pcy / (float)H;
-                    float rx = tcx * 2.0f - 1.0f, ry = tcy * 2.0f - 1.0f;
-                    const float* VI = U.view_inverse;
-                    const float* PI = U.proj_inverse;
-                    ro = mk3(mat4_row(VI, 0, 0.0f, 0.0f, 0.0f, 1.0f), mat4_row(VI, 1, 0.0f, 0.0f, 0.0f, 1.0f),
-                             mat4_row(VI, 2, 0.0f, 0.0f, 0.0f, 1.0f));
-                    V3 target = mk3(mat4_row(PI, 0, rx, ry, 1.0f, 1.0f), mat4_row(PI, 1, rx, ry, 1.0f, 1.0f),
-                                    mat4_row(PI, 2, rx, ry, 1.0f, 1.0f));
-                    V3 local = normalize3(target);
-                    rd = mk3(mat4_row(VI, 0, local.x, local.y, local.z, 0.0f),
-                             mat4_row(VI, 1, local.x, local.y, local.z, 0.0f),
-                             mat4_row(VI, 2, local.x, local.y, local.z, 0.0f));
-                    phase = kPhaseRay;
-                    bounce = 0;
-                    col = mk3(0, 0, 0);
-                }
-            }
-        }
-        if (!has) break;
-
-        bool done = false;
-        Hit h;
-        if (phase == kPhaseRay) {
-            if (bounce == 0) cnt.primary++;
-            else cnt.secondary++;
-            traverse<STATS>(e, ro, rd, 0.01f, 10000.0f, RT_RAY_FLAG_NONE, 0xFFu, 0u, h, cnt);
-            col = mk3(0, 0, 0);  // payload reset (lib.rs:145-149)
-            V3 nd = mk3(0, 0, 0), no = mk3(0, 0, 0);
-            if (h.inst == kNoHit) {
-                // primary_ray_miss (lib.rs:40-51)
-                col = dot3(rd, sun_dir) > sun_c ? mk3(1.0f, 1.0f, 1.0f) : mk3(0.0f, 0.0f, 0.05f);
-                done = true;
             } else {
-                const InstRecord* ir = &e.insts[h.inst];
-                uint32_t sbt_flags = ir->sbt_flags;
-                uint32_t custom = ir->custom_mask & 0xFFFFFFu;
-                const RtHitGroup* g = hit_group(e, sbt_flags, 0u);
-                uint32_t prog = g ? g->closest_hit : RT_PROGRAM_NONE;
-                V3 bary = mk3((1.0f - h.u) - h.v, h.u, h.v);
-                TriData td;
-                if (prog == RT_PROGRAM_CLOSEST_HIT_MIRROR && load_triangle(e, custom, h.geom, h.prim, &td)) {
-                    // closest_hit_mirror.glsl:11-29
-                    V3 ni = interp3(td.n[0], td.n[1], td.n[2], bary);
-                    V3 n = normalize3(xform_normal_w2o_t(ir->w2o, ni));
-                    float k = 2.0f * dot3(n, rd);
-                    nd = sub3(rd, mul3s(n, k));
-                    no = add3(ro, mul3s(rd, h.t));
-                } else if (prog == RT_PROGRAM_CLOSEST_HIT_PORTAL) {
-                    // lib.rs:300-312
-                    nd = rd;
-                    no = add3(add3(ro, mul3s(rd, h.t)), mk3(0.0f, 5.0f, 0.0f));
-                } else if (prog == RT_PROGRAM_CLOSEST_HIT_TEXTURED && load_triangle(e, custom, h.geom, h.prim, &td)) {
-                    // closest_hit_textured.glsl:174-226
-                    V3 ip = interp3(td.p[0], td.p[1], td.p[2], bary);
-                    V3 inrm = interp3(td.n[0], td.n[1], td.n[2], bary);
-                    float iu = (td.uv[0][0] * bary.x + td.uv[1][0] * bary.y) + td.uv[2][0] * bary.z;
-                    float iv = (td.uv[0][1] * bary.x + td.uv[1][1] * bary.y) + td.uv[2][1] * bary.z;
-                    V3 oa = project_onto_tangent_plane(ip, td.p[0], td.n[0]);
-                    V3 ob = project_onto_tangent_plane(ip, td.p[1], td.n[1]);
-                    V3 oc = project_onto_tangent_plane(ip, td.p[2], td.n[2]);
-                    V3 off = interp3(oa, ob, oc, bary);
-                    so = xform_point(ir->o2w, add3(ip, off));
-                    shade_textured(e, td, inrm, iu, iv, ir->w2o, rd, sun_dir, lambert, &NoL, &comb, &amb);
-                    if (nshadow > 0) {
-                        phase = kPhaseShadow;
-                        shadow_i = 0;
-                        lit = 0.0f;
-                    } else {
-                        float sf = 0.0f;
-                        col = mk3((sf * NoL) * comb.x + amb.x, (sf * NoL) * comb.y + amb.y,
-                                  (sf * NoL) * comb.z + amb.z);
-                        done = true;
-                    }
-                }
-                if (phase == kPhaseRay && !done) {
-                    // break when new_ray_direction == 0 (lib.rs:165-171)
-                    if (nd.x == 0.0f && nd.y == 0.0f && nd.z == 0.0f) {
-                        done = true;
-                    } else {
-                        ro = no;
-                        rd = nd;
-                        bounce++;
-                        if (bounce >= max_depth) done = true;  // colour stays reset
-                    }
-                }
+                pix = P.B.shadow_list[item / nshadow];
+                uint32_t si = item % nshadow;
+                float4 so = P.B.shade[3 * (size_t)pix];
+                V3 sd = shadow_direction(e, U, pix % W, pix / W, si, sun_dir);
+                trav_begin(s, e, mk3(so.x, so.y, so.z), sd, 0.001f, 10000.0f);
+                cnt.shadow++;
             }
-        } else {
-            cnt.shadow++;
-            V3 sd = shadow_direction(e, U, x, y, shadow_i, sun_dir);
-            traverse<STATS>(e, so, sd, 0.001f, 10000.0f,
-                            RT_RAY_FLAG_TERMINATE_ON_FIRST_HIT | RT_RAY_FLAG_SKIP_CLOSEST_HIT_SHADER, 0xFFu, 1u, h,
-                            cnt);
-            lit += (h.inst == kNoHit) ? 1.0f : 0.0f;  // shadow_ray_miss clears `shadowed`
-            shadow_i++;
-            if (shadow_i >= nshadow) {
-                float sf = lit / (float)nshadow;
-                col = mk3((sf * NoL) * comb.x + amb.x, (sf * NoL) * comb.y + amb.y, (sf * NoL) * comb.z + amb.z);
-                done = true;
-            }
+            if (heat) t0 = clock64();
         }
-        if (done) {
-            V3 c = col;
-            if (U.show_heatmap) {
-                long long dt = clock64() - t_start;
-                V3 hm = heatmap_temperature((float)dt / 1000000.0f);
-                c = add3(hm, mul3s(col, 0.000001f));
-            }
-            size_t pix = (size_t)y * W + x;
-            if (rad) rad[pix] = make_float4(c.x, c.y, c.z, 1.0f);
-            if (img) {
-                uint32_t r = to_unorm8(linear_to_srgb(c.x)), g = to_unorm8(linear_to_srgb(c.y));
-                uint32_t b = to_unorm8(linear_to_srgb(c.z));
-                img[pix] = r | (g << 8) | (b << 16) | (255u << 24);
-            }
-            has = false;
+        if (!trav_step<STATS>(s, stack, e, ray_flags, 0xFFu, sbt_offset, cnt)) continue;
+        // the ray is finished
+        if (MODE == kModeBounce) {
+            P.B.hits[2 * (size_t)item] = make_uint4(__float_as_uint(s.t), __float_as_uint(s.u), __float_as_uint(s.v),
+                                                    s.hit_inst);
+            P.B.hits[2 * (size_t)item + 1] = make_uint4(s.hit_geom, s.hit_prim, s.front ? 1u : 0u, 0u);
+        } else if (s.hit_inst == kNoHit) {
+            atomicAdd(&P.B.lit[pix], 1u);  // shadow_ray_miss clears `shadowed`
         }
+        if (heat && pix != kNoPixel) atomicAdd(&P.B.heat[pix], (unsigned long long)(clock64() - t0));
+        item = kNoItem;
     }
     flush_counters(L.stats, cnt);
+}
+
+// The closest-hit and miss programs for every ray of bounce b.
+__global__ void k_shade(const __grid_constant__ WfParams P) {
+    const uint32_t b = P.bounce;
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.B.ctr->ray_count[b]) return;
+    uint32_t p = P.B.ray_pixel[b & 1][i];
+    if (p == kNoPixel) return;
+    const TraceLaunch& L = P.L;
+    const Env e = make_env(L.push.acceleration_structure, L.push, &L.sbt, L.textures, L.status);
+    const RtUniforms& U = *reinterpret_cast<const RtUniforms*>(L.push.uniforms);
+    const V3 sun_dir = mk3(U.sun_dir[0], U.sun_dir[1], U.sun_dir[2]);
+    const uint32_t nshadow = L.desc.shadow_ray_count;
+    float4 ra = P.B.rays[b & 1][2 * (size_t)i], rb = P.B.rays[b & 1][2 * (size_t)i + 1];
+    V3 ro = mk3(ra.x, ra.y, ra.z), rd = mk3(rb.x, rb.y, rb.z);
+    uint4 h0 = P.B.hits[2 * (size_t)i], h1 = P.B.hits[2 * (size_t)i + 1];
+    const float t = __uint_as_float(h0.x), hu = __uint_as_float(h0.y), hv = __uint_as_float(h0.z);
+    const uint32_t inst = h0.w;
+    bool emit_shadow = false, emit_ray = false, write_colour = false;
+    V3 col = mk3(0.0f, 0.0f, 0.0f), nd = mk3(0, 0, 0), no = mk3(0, 0, 0);
+    if (inst == kNoHit) {
+        // primary_ray_miss (lib.rs:40-51)
+        float sun_s, sun_c;
+        rt_sincos(U.sun_radius, &sun_s, &sun_c);
+        col = dot3(rd, sun_dir) > sun_c ? mk3(1.0f, 1.0f, 1.0f) : mk3(0.0f, 0.0f, 0.05f);
+        write_colour = true;
+    } else {
+        const InstRecord* ir = &e.insts[inst];
+        const uint32_t sbt_flags = ir->sbt_flags, custom = ir->custom_mask & 0xFFFFFFu;
+        const RtHitGroup* g = hit_group(e, sbt_flags, 0u);
+        const uint32_t prog = g ? g->closest_hit : RT_PROGRAM_NONE;
+        const V3 bary = mk3((1.0f - hu) - hv, hu, hv);
+        TriData td;
+        if (prog == RT_PROGRAM_CLOSEST_HIT_MIRROR && load_triangle(e, custom, h1.x, h1.y, &td)) {
+            // closest_hit_mirror.glsl:11-29
+            V3 ni = interp3(td.n[0], td.n[1], td.n[2], bary);
+            V3 n = normalize3(xform_normal_w2o_t(ir->w2o, ni));
+            float k = 2.0f * dot3(n, rd);
+            nd = sub3(rd, mul3s(n, k));
+            no = add3(ro, mul3s(rd, t));
+        } else if (prog == RT_PROGRAM_CLOSEST_HIT_PORTAL) {
+            // lib.rs:300-312
+            nd = rd;
+            no = add3(add3(ro, mul3s(rd, t)), mk3(0.0f, 5.0f, 0.0f));
+        } else if (prog == RT_PROGRAM_CLOSEST_HIT_TEXTURED && load_triangle(e, custom, h1.x, h1.y, &td)) {
+            // closest_hit_textured.glsl:174-226
+            V3 ip = interp3(td.p[0], td.p[1], td.p[2], bary);
+            V3 inrm = interp3(td.n[0], td.n[1], td.n[2], bary);
+            float iu = (td.uv[0][0] * bary.x + td.uv[1][0] * bary.y) + td.uv[2][0] * bary.z;
+            float iv = (td.uv[0][1] * bary.x + td.uv[1][1] * bary.y) + td.uv[2][1] * bary.z;
+            V3 oa = project_onto_tangent_plane(ip, td.p[0], td.n[0]);
+            V3 ob = project_onto_tangent_plane(ip, td.p[1], td.n[1]);
+            V3 oc = project_onto_tangent_plane(ip, td.p[2], td.n[2]);
+            V3 off = interp3(oa, ob, oc, bary);
+            V3 so = xform_point(ir->o2w, add3(ip, off));
+            float NoL;
+            V3 comb, amb;
+            const bool lambert = (L.desc.flags & RT_TRACE_FLAG_LAMBERT_DIFFUSE) != 0;
+            shade_textured(e, td, inrm, iu, iv, ir->w2o, rd, sun_dir, lambert, &NoL, &comb, &amb);
+            if (nshadow > 0) {
+                float4* sh = P.B.shade + 3 * (size_t)p;
+                sh[0] = make_float4(so.x, so.y, so.z, NoL);
+                sh[1] = make_float4(comb.x, comb.y, comb.z, amb.x);
+                sh[2] = make_float4(amb.y, amb.z, 0.0f, 0.0f);
+                emit_shadow = true;
+            } else {
+                float sf = 0.0f;
+                col = mk3((sf * NoL) * comb.x + amb.x, (sf * NoL) * comb.y + amb.y, (sf * NoL) * comb.z + amb.z);
+                write_colour = true;
+            }
+        }
+        if (!emit_shadow && !write_colour) {
+            // payload: break when new_ray_direction == 0 (lib.rs:165-171),
+            // and after the last iteration the colour stays reset (black)
+            if ((nd.x == 0.0f && nd.y == 0.0f && nd.z == 0.0f) || b + 1 >= L.desc.max_trace_depth) {
+                col = mk3(0.0f, 0.0f, 0.0f);
+                write_colour = true;
+            } else {
+                emit_ray = true;
+            }
+        }
+    }
+    if (write_colour) P.B.colour[p] = make_float4(col.x, col.y, col.z, 1.0f);
+    uint32_t si = warp_append(&P.B.ctr->shadow_count, emit_shadow);
+    if (emit_shadow) P.B.shadow_list[si] = p;
+    uint32_t ri = warp_append(&P.B.ctr->ray_count[b + 1], emit_ray);
+    if (emit_ray) {
+        float4* R = P.B.rays[(b + 1) & 1];
+        R[2 * (size_t)ri] = make_float4(no.x, no.y, no.z, 0.01f);
+        R[2 * (size_t)ri + 1] = make_float4(nd.x, nd.y, nd.z, 10000.0f);
+        P.B.ray_pixel[(b + 1) & 1][ri] = p;
+    }
+}
+
+// sun_factor = lit / N; colour = brdf * sun_factor + ambient.
+__global__ void k_resolve(const __grid_constant__ WfParams P) {
+    uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= P.B.ctr->shadow_count) return;
+    uint32_t p = P.B.shadow_list[k];
+    const float4* sh = P.B.shade + 3 * (size_t)p;
+    float4 s0 = sh[0], s1 = sh[1], s2 = sh[2];
+    float sf = (float)P.B.lit[p] / (float)P.L.desc.shadow_ray_count;
+    float NoL = s0.w;
+    P.B.colour[p] = make_float4((sf * NoL) * s1.x + s1.w, (sf * NoL) * s1.y + s2.x, (sf * NoL) * s1.z + s2.y, 1.0f);
+}
+
+// Heatmap (lib.rs:174-186), linear_to_srgb and the RGBA8 image write.
+__global__ void k_output(const __grid_constant__ WfParams P) {
+    const uint32_t W = P.L.desc.width, H = P.L.desc.height;
+    uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= W * H) return;
+    const RtUniforms& U = *reinterpret_cast<const RtUniforms*>(P.L.push.uniforms);
+    float4 c4 = P.B.colour[p];
+    V3 c = mk3(c4.x, c4.y, c4.z);
+    if (U.show_heatmap) {
+        V3 hm = heatmap_temperature((float)P.B.heat[p] / 1000000.0f);
+        c = add3(hm, mul3s(c, 0.000001f));
+    }
+    float4* rad = reinterpret_cast<float4*>(P.L.desc.radiance_address);
+    uint32_t* img = reinterpret_cast<uint32_t*>(P.L.desc.image_address);
+    if (rad) rad[p] = make_float4(c.x, c.y, c.z, 1.0f);
+    if (img) {
+        uint32_t r = to_unorm8(linear_to_srgb(c.x)), g = to_unorm8(linear_to_srgb(c.y));
+        uint32_t bl = to_unorm8(linear_to_srgb(c.z));
+        img[p] = r | (g << 8) | (bl << 16) | (255u << 24);
+    }
 }
 
 struct RayBufferParams {
@@ -777,38 +614,46 @@ struct RayBufferParams {
 };
 
 template <bool STATS>
-__global__ void __launch_bounds__(128) k_trace_ray_buffer(const __grid_constant__ RayBufferParams P) {
+__global__ void __launch_bounds__(kTraceThreads) k_trace_ray_buffer(const __grid_constant__ RayBufferParams P) {
     const RayBufferLaunch& L = P.L;
     const Env e = make_env(L.tlas, L.push, &L.sbt, L.textures, L.status);
     Counters cnt = {0, 0, 0, 0, 0, 0};
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < L.count; i += gridDim.x * blockDim.x) {
-        const float4* rp = reinterpret_cast<const float4*>(L.rays + i);
-        float4 a = __ldg(rp), b = __ldg(rp + 1);
-        Hit h;
-        cnt.primary++;
-        traverse<STATS>(e, mk3(a.x, a.y, a.z), mk3(b.x, b.y, b.z), a.w, b.w, L.ray_flags, L.cull_mask, L.sbt_offset,
-                        h, cnt);
+    uint2 stack[kStackSize];
+    Trav s;
+    uint32_t item = kNoItem;
+    for (;;) {
+        uint32_t my = warp_append(L.work, item == kNoItem);
+        if (item == kNoItem) {
+            if (my >= L.count) break;
+            item = my;
+            const float4* rp = reinterpret_cast<const float4*>(L.rays + item);
+            float4 a = __ldg(rp), c = __ldg(rp + 1);
+            trav_begin(s, e, mk3(a.x, a.y, a.z), mk3(c.x, c.y, c.z), a.w, c.w);
+            cnt.primary++;
+        }
+        if (!trav_step<STATS>(s, stack, e, L.ray_flags, L.cull_mask, L.sbt_offset, cnt)) continue;
         RtHit o;
-        if (h.inst != kNoHit) {
-            const InstRecord* ir = &e.insts[h.inst];
-            o.t = h.t;
-            o.u = h.u;
-            o.v = h.v;
-            o.instance_id = h.inst_id;
+        if (s.hit_inst != kNoHit) {
+            const InstRecord* ir = &e.insts[s.hit_inst];
+            o.t = s.t;
+            o.u = s.u;
+            o.v = s.v;
+            o.instance_id = ir->instance_id;
             o.instance_custom_index = ir->custom_mask & 0xFFFFFFu;
-            o.geometry_index = h.geom;
-            o.primitive_index = h.prim;
-            o.hit_kind = h.front ? 0xFEu : 0xFFu;
+            o.geometry_index = s.hit_geom;
+            o.primitive_index = s.hit_prim;
+            o.hit_kind = s.front ? 0xFEu : 0xFFu;
         } else {
-            o.t = b.w;
+            o.t = s.t;
             o.u = o.v = 0.0f;
             o.instance_id = o.instance_custom_index = o.geometry_index = o.primitive_index = 0xFFFFFFFFu;
             o.hit_kind = 0;
         }
-        uint4* hp = reinterpret_cast<uint4*>(L.hits + i);
+        uint4* hp = reinterpret_cast<uint4*>(L.hits + item);
         const uint4* op = reinterpret_cast<const uint4*>(&o);
         hp[0] = op[0];
         hp[1] = op[1];
+        item = kNoItem;
     }
     flush_counters(L.stats, cnt);
 }
@@ -875,25 +720,82 @@ int persistent_blocks(K kernel, int threads, int num_sms) {
     return per_sm * num_sms;
 }
 
+template <int MODE>
+void launch_trace_mode(const WfParams& P, bool stats, int num_sms, cudaStream_t stream) {
+    if (stats) {
+        static int blocks = 0;
+        if (!blocks) blocks = persistent_blocks(k_trace<MODE, true>, kTraceThreads, num_sms);
+        note_launch(), k_trace<MODE, true><<<blocks, kTraceThreads, 0, stream>>>(P);
+    } else {
+        static int blocks = 0;
+        if (!blocks) blocks = persistent_blocks(k_trace<MODE, false>, kTraceThreads, num_sms);
+        note_launch(), k_trace<MODE, false><<<blocks, kTraceThreads, 0, stream>>>(P);
+    }
+}
+
 }  // namespace
 
-cudaError_t launch_trace_rays(const TraceLaunch& p, int num_sms, cudaStream_t stream) {
-    TraceParams P;
+uint64_t trace_workspace_bytes(uint32_t width, uint32_t height) {
+    uint64_t tiles = (uint64_t)((width + 7) / 8) * ((height + 3) / 4);
+    uint64_t slots = tiles * 32, pix = (uint64_t)width * height;
+    uint64_t b = 0;
+    auto take = [&](uint64_t n) { b = align_up(b + n, 256); };
+    take(sizeof(WfCounters));
+    take(slots * 32);  // rays[0]
+    take(slots * 32);  // rays[1]
+    take(slots * 4);   // ray_pixel[0]
+    take(slots * 4);   // ray_pixel[1]
+    take(slots * 32);  // hits
+    take(pix * 16);    // colour
+    take(pix * 48);    // shade
+    take(pix * 4);     // lit
+    take(pix * 4);     // shadow_list
+    take(pix * 8);     // heat
+    return b;
+}
+
+cudaError_t launch_trace_rays(const TraceLaunch& p, uint8_t* ws, int num_sms, cudaStream_t stream) {
+    const uint32_t W = p.desc.width, H = p.desc.height;
+    uint64_t tiles = (uint64_t)((W + 7) / 8) * ((H + 3) / 4);
+    uint64_t slots = tiles * 32, pix = (uint64_t)W * H;
+    WfParams P;
     P.L = p;
-    P.tiles_x = (p.desc.width + 7) / 8;
-    uint32_t tiles_y = (p.desc.height + 3) / 4;
-    P.total = P.tiles_x * tiles_y * 32u;
-    P.work = p.work;
-    cudaError_t err = cudaMemsetAsync(P.work, 0, sizeof(uint32_t), stream);
+    P.tiles_x = (W + 7) / 8;
+    P.total = (uint32_t)slots;
+    P.bounce = 0;
+    uint64_t off = 0;
+    auto take = [&](uint64_t n) {
+        uint8_t* r = ws + off;
+        off = align_up(off + n, 256);
+        return r;
+    };
+    P.B.ctr = reinterpret_cast<WfCounters*>(take(sizeof(WfCounters)));
+    P.B.rays[0] = reinterpret_cast<float4*>(take(slots * 32));
+    P.B.rays[1] = reinterpret_cast<float4*>(take(slots * 32));
+    P.B.ray_pixel[0] = reinterpret_cast<uint32_t*>(take(slots * 4));
+    P.B.ray_pixel[1] = reinterpret_cast<uint32_t*>(take(slots * 4));
+    P.B.hits = reinterpret_cast<uint4*>(take(slots * 32));
+    P.B.colour = reinterpret_cast<float4*>(take(pix * 16));
+    P.B.shade = reinterpret_cast<float4*>(take(pix * 48));
+    P.B.lit = reinterpret_cast<uint32_t*>(take(pix * 4));
+    P.B.shadow_list = reinterpret_cast<uint32_t*>(take(pix * 4));
+    P.B.heat = reinterpret_cast<unsigned long long*>(take(pix * 8));
+    cudaError_t err = cudaMemsetAsync(P.B.ctr, 0, sizeof(WfCounters), stream);
+    if (err == cudaSuccess) err = cudaMemsetAsync(P.B.lit, 0, pix * 4, stream);
+    if (err == cudaSuccess) err = cudaMemsetAsync(P.B.heat, 0, pix * 8, stream);
     if (err != cudaSuccess) return err;
     const bool stats = (p.desc.flags & RT_TRACE_FLAG_COLLECT_STATS) != 0;
-    if (stats) {
-        int blocks = persistent_blocks(k_trace_rays<true>, 128, num_sms);
-        note_launch(), k_trace_rays<true><<<blocks, 128, 0, stream>>>(P);
-    } else {
-        int blocks = persistent_blocks(k_trace_rays<false>, 128, num_sms);
-        note_launch(), k_trace_rays<false><<<blocks, 128, 0, stream>>>(P);
+    note_launch(), k_raygen<<<(uint32_t)((slots + 255) / 256), 256, 0, stream>>>(P);
+    for (uint32_t b = 0; b < p.desc.max_trace_depth; b++) {
+        P.bounce = b;
+        launch_trace_mode<kModeBounce>(P, stats, num_sms, stream);
+        note_launch(), k_shade<<<(uint32_t)((slots + 127) / 128), 128, 0, stream>>>(P);
     }
+    if (p.desc.shadow_ray_count > 0) {
+        launch_trace_mode<kModeShadow>(P, stats, num_sms, stream);
+        note_launch(), k_resolve<<<(uint32_t)((pix + 255) / 256), 256, 0, stream>>>(P);
+    }
+    note_launch(), k_output<<<(uint32_t)((pix + 255) / 256), 256, 0, stream>>>(P);
     return cudaGetLastError();
 }
 
@@ -901,13 +803,16 @@ cudaError_t launch_trace_ray_buffer(const RayBufferLaunch& p, int num_sms, cudaS
     RayBufferParams P;
     P.L = p;
     if (p.count == 0) return cudaSuccess;
-    uint32_t blocks = (p.count + 127) / 128;
+    cudaError_t err = cudaMemsetAsync(p.work, 0, sizeof(uint32_t), stream);
+    if (err != cudaSuccess) return err;
     if (p.collect_stats) {
-        int maxb = persistent_blocks(k_trace_ray_buffer<true>, 128, num_sms);
-        note_launch(), k_trace_ray_buffer<true><<<std::min<uint32_t>(blocks, (uint32_t)maxb * 8u), 128, 0, stream>>>(P);
+        static int blocks = 0;
+        if (!blocks) blocks = persistent_blocks(k_trace_ray_buffer<true>, kTraceThreads, num_sms);
+        note_launch(), k_trace_ray_buffer<true><<<blocks, kTraceThreads, 0, stream>>>(P);
     } else {
-        int maxb = persistent_blocks(k_trace_ray_buffer<false>, 128, num_sms);
-        note_launch(), k_trace_ray_buffer<false><<<std::min<uint32_t>(blocks, (uint32_t)maxb * 8u), 128, 0, stream>>>(P);
+        static int blocks = 0;
+        if (!blocks) blocks = persistent_blocks(k_trace_ray_buffer<false>, kTraceThreads, num_sms);
+        note_launch(), k_trace_ray_buffer<false><<<blocks, kTraceThreads, 0, stream>>>(P);
     }
     return cudaGetLastError();
 }
