@@ -528,14 +528,16 @@ __device__ void write_node(WideNode* dst, const float lo[8][3], const float hi[8
                            const uint32_t meta[8], int cnt) {
     WideNode nd;
     for (int k = 0; k < 8; k++) {
-        bool v = k < cnt;
+        bool v = k < cnt && meta[k] != 0u;
         nd.lox[k] = v ? lo[k][0] : 0.0f;
         nd.loy[k] = v ? lo[k][1] : 0.0f;
         nd.loz[k] = v ? lo[k][2] : 0.0f;
         nd.hix[k] = v ? hi[k][0] : 0.0f;
         nd.hiy[k] = v ? hi[k][1] : 0.0f;
         nd.hiz[k] = v ? hi[k][2] : 0.0f;
-        nd.child_ref[k] = v ? ref[k] : 0u;
+        // the traversal's stack entry: node index, or leaf | (count-1) << 28 | first
+        nd.child_ref[k] = !v ? kChildEmpty
+                             : (meta[k] == kMetaInternal ? ref[k] : (kChildLeaf | ((meta[k] - 1u) << 28) | ref[k]));
     }
     uint32_t m0 = 0, m1 = 0;
     for (int k = 0; k < 4; k++) {
@@ -803,8 +805,11 @@ __global__ void k_refit_nodes(AsHeader* h, const float4* sboxes, uint32_t* count
             uint32_t m = node_meta(m0, m1, k);
             if (m == 0) continue;
             uint32_t r = __ldcg(&nd->child_ref[k]);
+            if (m != kMetaInternal) r &= 0x0FFFFFFFu;  // leaf: first primitive
             float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
-            if (m == kMetaInternal) {
+            if (m == kMetaInternal ? r >= count : (m > 8u || r + m > h->prim_count)) {
+                atomicOr(err, 1u << RT_ERR_BAD_AS);  // malformed child: leave its box empty
+            } else if (m == kMetaInternal) {
                 const WideNode* cn = &nodes[r];
                 uint32_t c0 = __ldcg(&cn->meta[0]), c1 = __ldcg(&cn->meta[1]);
                 for (int q = 0; q < 8; q++) {

@@ -11,7 +11,7 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
-#include "../../include/rtcore.h"
+#include "rtcore.h"
 
 namespace rt {
 
@@ -54,11 +54,15 @@ struct AsHeader {
 static_assert(sizeof(AsHeader) == kHeaderBytes, "header size");
 
 // 8-wide node, SoA child boxes.  Children are packed at the front.
-// child_ref: internal -> node index; leaf -> first primitive (sorted order).
+// child_ref is the traversal's stack entry for the child: an internal child
+// is its node index (< 2^30); a leaf is kChildLeaf | (count - 1) << 28 |
+// first primitive (sorted order, < 2^28); an empty slot is kChildEmpty.
 // meta byte c (meta[0] holds children 0-3, meta[1] children 4-7, low byte
-// first): 0 = empty slot, kMetaInternal = internal child, 1..8 = leaf with
-// that many primitives.
+// first) repeats the kind for the refit: 0 = empty, kMetaInternal =
+// internal, 1..8 = leaf with that many primitives.
 constexpr uint32_t kMetaInternal = 0x80u;
+constexpr uint32_t kChildLeaf = 0x80000000u;
+constexpr uint32_t kChildEmpty = 0xFFFFFFFFu;
 struct alignas(128) WideNode {
     float lox[8], hix[8], loy[8], hiy[8], loz[8], hiz[8];
     uint32_t child_ref[8];

@@ -48,6 +48,11 @@ constexpr uint32_t kNoItem = 0xFFFFFFFFu;
 constexpr uint32_t kMaxTraversalSteps = 1u << 22;
 constexpr int kTraceThreads = 128;
 constexpr int kMaxDepth = 64;
+// Resident 128-thread blocks per SM the trace kernels are compiled for
+// (6 -> at most 80 registers, 24 warps per SM).
+#ifndef RT_TRACE_MIN_BLOCKS
+#define RT_TRACE_MIN_BLOCKS 6
+#endif
 
 constexpr int kModeBounce = 0;   // closest hit of a bounce list -> hit records
 constexpr int kModeShadow = 1;   // any hit of generated shadow rays -> lit counters
@@ -76,6 +81,26 @@ __device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool pred) {
         base = __shfl_sync(m, base, leader);
     }
     return base + __popc(b & lanemask_lt());
+}
+
+// Three-input min / max (one instruction on sm_100 and later).  Like fminf
+// / fmaxf they return the non-NaN operand; the box test never produces NaN.
+__device__ __forceinline__ float fmax3(float a, float b, float c) {
+    float d;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+__device__ __forceinline__ float fmin3(float a, float b, float c) {
+    float d;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+
+// Float4 offsets (within a node) of the near-plane box arrays for each axis,
+// from the signs of the reciprocal direction: x at 0 (lox) or 2 (hix), y at
+// 4 or 6, z at 8 or 10; the far plane is at offset ^ 2.
+__device__ __forceinline__ uint32_t octant_offsets(V3 inv) {
+    return (inv.x < 0.0f ? 2u : 0u) | ((inv.y < 0.0f ? 6u : 4u) << 8) | ((inv.z < 0.0f ? 10u : 8u) << 16);
 }
 
 __device__ __forceinline__ uint32_t pick8(const uint32_t v[8], uint32_t s) {
@@ -109,6 +134,7 @@ __device__ __forceinline__ void sort8(uint32_t k[8]) {
 struct Trav {
     V3 wo, wd;                 // world ray
     V3 o, d, inv;              // ray in the current space (world or object)
+    uint32_t oct;              // octant_offsets(inv)
     WtRay wt;                  // watertight shear of the object-space ray
     float tmin;
     float t, u, v;             // best hit so far (t = tmax before any hit)
@@ -130,6 +156,7 @@ __device__ __forceinline__ void trav_begin(Trav& s, const Env& e, V3 o, V3 d, fl
     s.o = o;
     s.d = d;
     s.inv = safe_inv(d);
+    s.oct = octant_offsets(s.inv);
     s.wt.kx = s.wt.ky = s.wt.kz = 0;
     s.wt.sx = s.wt.sy = s.wt.sz = 0.0f;
     s.tmin = tmin;
@@ -168,6 +195,7 @@ __device__ __forceinline__ void trav_restore_world(Trav& s, const Env& e) {
     s.o = s.wo;
     s.d = s.wd;
     s.inv = safe_inv(s.wd);
+    s.oct = octant_offsets(s.inv);
 }
 
 // (inst, geom, prim) below the best hit's, comparing caller instance indices
@@ -198,34 +226,38 @@ __device__ __forceinline__ bool trav_step(Trav& s, uint2* stack, const Env& e, u
             atomicOr(e.status, 1u << RT_ERR_BAD_AS);  // malformed reference: skip it
         } else {
             if (STATS) cnt.nodes++;
+            // Near / far planes were chosen per ray by the direction signs
+            // (s.oct): the loads fetch them directly, so each child needs
+            // one subtract and one multiply per plane and no per-axis min/max.
             const float4* np = reinterpret_cast<const float4*>(s.nodes + entry);
-            float4 a0 = __ldg(np + 0), a1 = __ldg(np + 1), b0 = __ldg(np + 2), b1 = __ldg(np + 3);
-            float4 c0 = __ldg(np + 4), c1 = __ldg(np + 5), d0 = __ldg(np + 6), d1 = __ldg(np + 7);
-            float4 e0 = __ldg(np + 8), e1 = __ldg(np + 9), f0 = __ldg(np + 10), f1 = __ldg(np + 11);
+            const uint32_t ox = s.oct & 0xFFu, oy = (s.oct >> 8) & 0xFFu, oz = s.oct >> 16;
+            float4 nx0 = __ldg(np + ox), nx1 = __ldg(np + ox + 1), fx0 = __ldg(np + (ox ^ 2u)),
+                   fx1 = __ldg(np + (ox ^ 2u) + 1);
+            float4 ny0 = __ldg(np + oy), ny1 = __ldg(np + oy + 1), fy0 = __ldg(np + (oy ^ 2u)),
+                   fy1 = __ldg(np + (oy ^ 2u) + 1);
+            float4 nz0 = __ldg(np + oz), nz1 = __ldg(np + oz + 1), fz0 = __ldg(np + (oz ^ 2u)),
+                   fz1 = __ldg(np + (oz ^ 2u) + 1);
             uint4 r0 = __ldg(reinterpret_cast<const uint4*>(np + 12));
             uint4 r1 = __ldg(reinterpret_cast<const uint4*>(np + 13));
-            uint2 mm = __ldg(reinterpret_cast<const uint2*>(np + 14));
-            const float lox[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
-            const float hix[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
-            const float loy[8] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y, c1.z, c1.w};
-            const float hiy[8] = {d0.x, d0.y, d0.z, d0.w, d1.x, d1.y, d1.z, d1.w};
-            const float loz[8] = {e0.x, e0.y, e0.z, e0.w, e1.x, e1.y, e1.z, e1.w};
-            const float hiz[8] = {f0.x, f0.y, f0.z, f0.w, f1.x, f1.y, f1.z, f1.w};
+            const float nx[8] = {nx0.x, nx0.y, nx0.z, nx0.w, nx1.x, nx1.y, nx1.z, nx1.w};
+            const float fx[8] = {fx0.x, fx0.y, fx0.z, fx0.w, fx1.x, fx1.y, fx1.z, fx1.w};
+            const float ny[8] = {ny0.x, ny0.y, ny0.z, ny0.w, ny1.x, ny1.y, ny1.z, ny1.w};
+            const float fy[8] = {fy0.x, fy0.y, fy0.z, fy0.w, fy1.x, fy1.y, fy1.z, fy1.w};
+            const float nz[8] = {nz0.x, nz0.y, nz0.z, nz0.w, nz1.x, nz1.y, nz1.z, nz1.w};
+            const float fz[8] = {fz0.x, fz0.y, fz0.z, fz0.w, fz1.x, fz1.y, fz1.z, fz1.w};
             const uint32_t refs[8] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w};
             const float tcap = s.t;
-            uint32_t keys[8], ents[8];
+            uint32_t keys[8];
 #pragma unroll
             for (int k = 0; k < 8; k++) {
-                float t0x = (lox[k] - s.o.x) * s.inv.x, t1x = (hix[k] - s.o.x) * s.inv.x;
-                float t0y = (loy[k] - s.o.y) * s.inv.y, t1y = (hiy[k] - s.o.y) * s.inv.y;
-                float t0z = (loz[k] - s.o.z) * s.inv.z, t1z = (hiz[k] - s.o.z) * s.inv.z;
-                float tn = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fmaxf(fminf(t0z, t1z), s.tmin));
-                float tf = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fminf(fmaxf(t0z, t1z), tcap));
-                uint32_t m = node_meta(mm.x, mm.y, k);
-                bool hit = (m != 0u) && (tn <= tf * kBoxFarScale);
+                float tnx = (nx[k] - s.o.x) * s.inv.x, tfx = (fx[k] - s.o.x) * s.inv.x;
+                float tny = (ny[k] - s.o.y) * s.inv.y, tfy = (fy[k] - s.o.y) * s.inv.y;
+                float tnz = (nz[k] - s.o.z) * s.inv.z, tfz = (fz[k] - s.o.z) * s.inv.z;
+                float tn = fmax3(fmaxf(tnx, s.tmin), tny, tnz);
+                float tf = fmin3(fminf(tfx, tcap), tfy, tfz);
+                bool hit = (refs[k] != kChildEmpty) && (tn <= tf * kBoxFarScale);
                 // key: tnear bits rounded down to 8 ulps | slot (ascending = near first)
                 keys[k] = hit ? ((__float_as_uint(fmaxf(tn, 0.0f)) & ~7u) | (uint32_t)k) : 0xFFFFFFFFu;
-                ents[k] = (m == kMetaInternal) ? refs[k] : (kLeafEntry | ((m - 1u) << 28) | refs[k]);
             }
             sort8(keys);
             if (keys[0] != 0xFFFFFFFFu) {
@@ -236,10 +268,10 @@ __device__ __forceinline__ bool trav_step(Trav& s, uint2* stack, const Env& e, u
                 for (int q = 7; q >= 1; q--) {
                     uint32_t key = keys[q];
                     if (key == 0xFFFFFFFFu) continue;
-                    if (s.sp < (int)kStackSize) stack[s.sp++] = make_uint2(pick8(ents, key & 7u), key & ~7u);
+                    if (s.sp < (int)kStackSize) stack[s.sp++] = make_uint2(pick8(refs, key & 7u), key & ~7u);
                     else atomicOr(e.status, 1u << RT_ERR_STACK_OVERFLOW);
                 }
-                s.entry = pick8(ents, keys[0] & 7u);
+                s.entry = pick8(refs, keys[0] & 7u);
                 return false;
             }
         }
@@ -262,6 +294,7 @@ __device__ __forceinline__ bool trav_step(Trav& s, uint2* stack, const Env& e, u
                 s.o = xform_point(w, s.wo);
                 s.d = xform_dir(w, s.wd);
                 s.inv = safe_inv(s.d);
+                s.oct = octant_offsets(s.inv);
                 s.wt = wt_setup(s.d);
                 const uint8_t* blas = reinterpret_cast<const uint8_t*>(((uint64_t)q0.y << 32) | q0.x);
                 s.nodes = reinterpret_cast<const WideNode*>(blas + kHeaderBytes);
@@ -416,7 +449,7 @@ __global__ void k_raygen(const __grid_constant__ WfParams P) {
 
 // Persistent trace kernel with per-lane ray replacement.
 template <int MODE, bool STATS>
-__global__ void __launch_bounds__(kTraceThreads) k_trace(const __grid_constant__ WfParams P) {
+__global__ void __launch_bounds__(kTraceThreads, RT_TRACE_MIN_BLOCKS) k_trace(const __grid_constant__ WfParams P) {
     const TraceLaunch& L = P.L;
     const Env e = make_env(L.push.acceleration_structure, L.push, &L.sbt, L.textures, L.status);
     const RtUniforms& U = *reinterpret_cast<const RtUniforms*>(L.push.uniforms);
@@ -614,7 +647,8 @@ struct RayBufferParams {
 };
 
 template <bool STATS>
-__global__ void __launch_bounds__(kTraceThreads) k_trace_ray_buffer(const __grid_constant__ RayBufferParams P) {
+__global__ void __launch_bounds__(kTraceThreads, RT_TRACE_MIN_BLOCKS)
+    k_trace_ray_buffer(const __grid_constant__ RayBufferParams P) {
     const RayBufferLaunch& L = P.L;
     const Env e = make_env(L.tlas, L.push, &L.sbt, L.textures, L.status);
     Counters cnt = {0, 0, 0, 0, 0, 0};
