@@ -328,6 +328,27 @@ RTCORE_API int32_t rt_cmd_build_blas(rt_ctx* ctx, const RtGeometryTriangles* geo
                                      uint32_t geometry_count, uint32_t build_flags, uint64_t dst,
                                      uint64_t dst_size, uint64_t scratch, uint64_t scratch_size,
                                      void* stream);
+/* Builds a BLAS exactly like rt_cmd_build_blas, but allocates nothing and
+ * takes no scratch argument: the build scratch is one fixed device array
+ * inside librtcore of RT_STATIC_SCRATCH_BYTES, which every GPU that loads
+ * the library holds until the process exits.  No counterpart in the
+ * reference (its Vulkan path always receives caller-allocated scratch).
+ * It is for callers that may not allocate device memory when they build:
+ * a host whose device memory belongs to another allocator that hands this
+ * library only the destination buffer, or a frame loop whose memory budget
+ * is fixed at start-up.
+ * Limit: geometries whose rt_get_blas_build_sizes().build_scratch_size is
+ * above RT_STATIC_SCRATCH_BYTES (about 400k triangles) are rejected with
+ * RT_ERR_TOO_LARGE before anything is queued.  Every call uses the same
+ * array, so calls whose GPU work can overlap (different streams with no
+ * ordering between them) race and corrupt each other's builds; order them.
+ * The first call on each device looks the array's device address up
+ * (cudaGetSymbolAddress) with that device current; make that first call
+ * before any stream capture. */
+#define RT_STATIC_SCRATCH_BYTES (64ull << 20)
+RTCORE_API int32_t rt_cmd_build_blas_static_scratch(rt_ctx* ctx, const RtGeometryTriangles* geometries,
+                                                    uint32_t geometry_count, uint32_t build_flags, uint64_t dst,
+                                                    uint64_t dst_size, void* stream);
 RTCORE_API int32_t rt_get_tlas_build_sizes(uint32_t instance_count, uint32_t build_flags, RtBuildSizes* out);
 /* `instances` is a DEVICE array of RtAccelerationStructureInstance. */
 RTCORE_API int32_t rt_cmd_build_tlas(rt_ctx* ctx, uint64_t instances, uint32_t instance_count,

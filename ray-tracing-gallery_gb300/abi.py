@@ -26,6 +26,7 @@ RT_MAX_BOUND_IMAGES = 128
 RT_MAX_BLAS_GEOMETRIES = 128
 RT_MAX_HIT_GROUPS = 8
 RT_AS_ALIGNMENT = 256
+RT_STATIC_SCRATCH_BYTES = 64 << 20
 
 RT_INSTANCE_TRIANGLE_FACING_CULL_DISABLE = 0x1
 RT_INSTANCE_TRIANGLE_FLIP_FACING = 0x2
@@ -256,6 +257,8 @@ EXPORTED_FUNCTIONS = {
     "rt_get_blas_build_sizes": (C.c_int32, [C.POINTER(RtGeometryTriangles), C.c_uint32, C.c_uint32, C.POINTER(RtBuildSizes)]),
     "rt_cmd_build_blas": (C.c_int32, [C.c_void_p, C.POINTER(RtGeometryTriangles), C.c_uint32, C.c_uint32, C.c_uint64,
                                        C.c_uint64, C.c_uint64, C.c_uint64, C.c_void_p]),
+    "rt_cmd_build_blas_static_scratch": (C.c_int32, [C.c_void_p, C.POINTER(RtGeometryTriangles), C.c_uint32,
+                                                      C.c_uint32, C.c_uint64, C.c_uint64, C.c_void_p]),
     "rt_get_tlas_build_sizes": (C.c_int32, [C.c_uint32, C.c_uint32, C.POINTER(RtBuildSizes)]),
     "rt_cmd_build_tlas": (C.c_int32, [C.c_void_p, C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint64, C.c_uint64,
                                        C.c_uint64, C.c_uint64, C.c_void_p]),

@@ -277,6 +277,90 @@ RTCORE_API int32_t rt_cmd_build_blas(rt_ctx* ctx, const RtGeometryTriangles* geo
     return RT_OK;
 }
 
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// BLAS build without allocation (rt_cmd_build_blas_static_scratch)
+// ---------------------------------------------------------------------------
+namespace {
+// The scratch of the allocation-free BLAS build.  Host code may not use the
+// symbol's host-side name as a device address; static_scratch_address()
+// looks the device address up once per device.
+static __device__ __align__(256) uint8_t g_static_scratch[RT_STATIC_SCRATCH_BYTES];
+
+struct StaticScratchAddress {
+    int device;
+    uint8_t* ptr;
+};
+std::mutex g_static_scratch_mu;
+std::vector<StaticScratchAddress> g_static_scratch_addrs;
+
+cudaError_t static_scratch_address(uint8_t** out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lk(g_static_scratch_mu);
+    for (const auto& a : g_static_scratch_addrs) {
+        if (a.device == dev) {
+            *out = a.ptr;
+            return cudaSuccess;
+        }
+    }
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_static_scratch);
+    if (e != cudaSuccess) return e;
+    g_static_scratch_addrs.push_back({dev, reinterpret_cast<uint8_t*>(p)});
+    *out = reinterpret_cast<uint8_t*>(p);
+    return cudaSuccess;
+}
+}  // namespace
+
+extern "C" {
+
+RTCORE_API int32_t rt_cmd_build_blas_static_scratch(rt_ctx* ctx, const RtGeometryTriangles* geometries,
+                                                    uint32_t geometry_count, uint32_t build_flags, uint64_t dst,
+                                                    uint64_t dst_size, void* stream) {
+    MaybeLock l(ctx);
+    uint32_t n = 0;
+    int32_t r = blas_prim_count(geometries, geometry_count, &n);
+    if (r) return r;
+    if (build_flags & RT_BUILD_QUANTIZED_NODES)
+        return fail(RT_ERR_UNSUPPORTED, "RT_BUILD_QUANTIZED_NODES is not available in this build");
+    AsLayout al = AsLayout::make(n, false);
+    ScratchLayout sl = ScratchLayout::make(n, false);
+    if (!dst || !aligned(dst, RT_AS_ALIGNMENT)) return fail(RT_ERR_INVALID, "dst must be non-null and 256-byte aligned");
+    if (dst_size < al.total)
+        return fail(RT_ERR_INVALID, "dst_size %llu < required %llu", (unsigned long long)dst_size,
+                    (unsigned long long)al.total);
+    if (sl.build_total > RT_STATIC_SCRATCH_BYTES)
+        return fail(RT_ERR_TOO_LARGE,
+                    "a BLAS of %u triangles needs %llu bytes of build scratch; the static scratch holds %llu "
+                    "(use rt_cmd_build_blas with caller-allocated scratch)",
+                    n, (unsigned long long)sl.build_total, (unsigned long long)RT_STATIC_SCRATCH_BYTES);
+    uint8_t* scratch = nullptr;
+    cudaError_t e = static_scratch_address(&scratch);
+    if (e != cudaSuccess) return cuda_fail(e, "rt_cmd_build_blas_static_scratch (scratch address)");
+    BlasInput in;
+    memset(&in, 0, sizeof in);
+    in.geometry_count = geometry_count ? geometry_count : 1;
+    in.n = n;
+    uint32_t prefix = 0;
+    for (uint32_t i = 0; i < geometry_count; i++) {
+        in.g[i].pos = reinterpret_cast<const float*>(geometries[i].vertex_address);
+        in.g[i].idx = reinterpret_cast<const uint32_t*>(geometries[i].index_address);
+        in.g[i].stride_floats = geometries[i].vertex_stride / 4;
+        in.g[i].max_vertex = geometries[i].max_vertex;
+        in.g[i].prim_count = geometries[i].primitive_count;
+        in.g[i].flags = geometries[i].flags;
+        in.g[i].prefix = prefix;
+        prefix += geometries[i].primitive_count;
+    }
+    e = launch_blas_build(in, build_flags, reinterpret_cast<uint8_t*>(dst), scratch,
+                          reinterpret_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return cuda_fail(e, "rt_cmd_build_blas_static_scratch");
+    return RT_OK;
+}
+
 RTCORE_API int32_t rt_get_tlas_build_sizes(uint32_t instance_count, uint32_t build_flags, RtBuildSizes* out) {
     if (!out) return fail(RT_ERR_INVALID, "out is NULL");
     (void)build_flags;
