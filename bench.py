@@ -70,6 +70,21 @@ def dist_env():
     return rank, world, local
 
 
+def profiled_traffic():
+    """DRAM bytes per traversal launch from the committed ncu summary of this
+    workload (profiles/k_trace_full_1080p.md, line `dram_bytes_per_launch: N`)."""
+    p = ROOT / "profiles" / "k_trace_full_1080p.md"
+    if not p.exists():
+        return None
+    for line in p.read_text().splitlines():
+        if line.strip().startswith("dram_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].strip().split()[0])
+            except ValueError:
+                return None
+    return None
+
+
 def measured_peaks() -> tuple[float, str]:
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -229,17 +244,19 @@ def bench_ours(args):
     sh = host.Device.stream_handle(stream)
     scratch = gs.scratch
 
-    def step(k: int, inst_tensor, ev_trace=None):
+    def step(k: int, inst_tensor, flags: int = 0):
         gs.tlas.rebuild_tlas(dev, inst_tensor, n_inst, scratch, stream)
         push = gs.push_constants(uni_dev[k % FRAMES].data_ptr(), gs.tlas)
         d = abi.RtTraceRaysDesc()
         d.width, d.height, d.max_trace_depth, d.shadow_ray_count = W, H, 2, 4
+        d.flags = flags
         d.image_address = fr.image.data_ptr()
-        if ev_trace is not None:
-            ev_trace[0].record(stream)
         dev.check(lib.rt_cmd_trace_rays(dev.ctx, C.byref(push), None, C.byref(d), sh))
-        if ev_trace is not None:
-            ev_trace[1].record(stream)
+
+    def read_timings() -> dict:
+        tt = abi.RtTraceTimings()
+        dev.check(lib.rt_ctx_read_trace_timings(dev.ctx, C.byref(tt)))
+        return tt.as_dict()
 
     for k in range(args.warmup):
         step(k, frames_dev[k % FRAMES])
@@ -251,22 +268,25 @@ def bench_ours(args):
     clocks.start()
     launches0 = lib.rt_kernel_launch_count()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    evt = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    kernel_times = []
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
     for i in range(args.steps):
         flush.fill_(i & 0xFF)
         ev[i][0].record(stream)
-        step(i, frames_dev[i % FRAMES], evt[i])
+        step(i, frames_dev[i % FRAMES], abi.RT_TRACE_FLAG_KERNEL_TIMINGS)
         ev[i][1].record(stream)
+        kernel_times.append(read_timings())  # waits for this step; outside the device-timed events
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
     launches = lib.rt_kernel_launch_count() - launches0
     clk = clocks.stop()
     step_ms = [a.elapsed_time(b) for a, b in ev]
-    trace_ms = [a.elapsed_time(b) for a, b in evt]
+    trace_ms = [kt["total_ms"] for kt in kernel_times]
+    traversal_ms = [kt["trace_ms"] for kt in kernel_times]
+    traversal_launches = kernel_times[0]["trace_launches"]
     stats = dev.read_stats(reset=True)
     total_ms = sum(step_ms)
     rays_local = stats["traversals"]
@@ -313,18 +333,15 @@ def bench_ours(args):
     d.image_address = fr.image.data_ptr()
     dev.check(lib.rt_cmd_trace_rays(dev.ctx, C.byref(push), None, C.byref(d), sh))
     s = dev.read_stats(reset=True)
-    bytes_per_launch = (s["traversals"] * (RAY_BYTES + HIT_BYTES) + s["nodes_visited"] * NODE_BYTES +
-                        s["triangles_tested"] * TRI_BYTES + s["instances_visited"] * INST_BYTES)
-    avg_trace_s = sum(trace_ms) / len(trace_ms) / 1e3
+    # the traversal kernel (k_trace) is the dominant kernel; per frame it runs
+    # once per bounce (closest hit) and once for the shadow rays
+    bytes_per_frame = (s["traversals"] * (RAY_BYTES + HIT_BYTES) + s["nodes_visited"] * NODE_BYTES +
+                       s["triangles_tested"] * TRI_BYTES + s["instances_visited"] * INST_BYTES)
+    bytes_per_launch = bytes_per_frame / traversal_launches
+    avg_launch_s = sum(traversal_ms) / len(traversal_ms) / traversal_launches / 1e3
     peak, peak_kind = measured_peaks()
-    achieved = bytes_per_launch / avg_trace_s / 1e9
-    traffic = None
-    prof = ROOT / "profiles" / "trace_rays_full_1080p.json"
-    if prof.exists():
-        try:
-            traffic = json.loads(prof.read_text()).get("dram_bytes_per_launch")
-        except Exception:
-            traffic = None
+    achieved = bytes_per_launch / avg_launch_s / 1e9
+    traffic = profiled_traffic()
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -340,15 +357,22 @@ def bench_ours(args):
                        "path": "plain FP32 8-wide BVH", "parallelism": f"replicas x{world}",
                        "l2": "flushed between steps (256 MiB write outside the timed events)",
                        "traversals_per_step": rays_local / args.steps, "blas_build_ms": blas_build_ms,
-                       "trace_ms_per_step": sum(trace_ms) / len(trace_ms),
-                       "tlas_build_ms_per_step": (total_ms - sum(trace_ms)) / args.steps},
+                       "trace_pipeline_ms_per_step": sum(trace_ms) / len(trace_ms),
+                       "traversal_ms_per_step": sum(traversal_ms) / len(traversal_ms),
+                       "shade_ms_per_step": sum(kt["shade_ms"] for kt in kernel_times) / len(kernel_times),
+                       "tlas_build_ms_per_step": (sum(step_ms) - sum(trace_ms)) / args.steps},
             "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": n_inst * 64,
                     "d2h_bytes_per_step": W * H * 4},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
-                         "kernel": "k_trace_rays", "peak_source": peak_kind,
+                         "kernel": "k_trace (traversal; closest-hit per bounce + shadow)",
+                         "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
+                         else "fallback 6.8 TB/s",
+                         "launches_per_step": traversal_launches,
                          "algorithmic_bytes_per_launch": bytes_per_launch,
-                         "bytes_per_ray": bytes_per_launch / max(1, s["traversals"])},
+                         "bytes_per_ray": bytes_per_frame / max(1, s["traversals"]),
+                         "nodes_per_ray": s["nodes_visited"] / max(1, s["traversals"]),
+                         "triangles_per_ray": s["triangles_tested"] / max(1, s["traversals"])},
             "cpu_baseline": cpu,
             "clocks": clk,
             "gpu_launches": int(launches),

@@ -255,6 +255,7 @@ typedef struct RtShaderBindingTable {
 /* ------------------------------------------------------------------------ */
 #define RT_TRACE_FLAG_COLLECT_STATS 0x1u    /* count nodes/triangles visited   */
 #define RT_TRACE_FLAG_LAMBERT_DIFFUSE 0x2u  /* Fd_Lambert instead of Fd_Burley */
+#define RT_TRACE_FLAG_KERNEL_TIMINGS 0x4u   /* record CUDA events around each kernel (rt_ctx_read_trace_timings) */
 
 typedef struct RtTraceRaysDesc {
     uint32_t width;
@@ -287,6 +288,19 @@ typedef struct RtHit {
     uint32_t hit_kind;            /* 0xFE front face, 0xFF back face (gl_HitKind*) */
 } RtHit;
 
+/* Kernel times of the last rt_cmd_trace_rays launched with
+ * RT_TRACE_FLAG_KERNEL_TIMINGS (CUDA events on the launch's stream). */
+typedef struct RtTraceTimings {
+    float total_ms;        /* first kernel start .. last kernel end */
+    float trace_ms;        /* all traversal launches */
+    float closest_ms;      /* closest-hit traversal launches (one per bounce) */
+    float shadow_ms;       /* the shadow-ray traversal launch */
+    float shade_ms;        /* closest-hit / miss program launches */
+    float other_ms;        /* raygen, resolve, output */
+    uint32_t trace_launches;
+    uint32_t _padding;
+} RtTraceTimings;
+
 typedef struct RtStats {
     uint64_t traversals;          /* rays traced (each traceRay counted once) */
     uint64_t primary_rays;        /* first iteration of the bounce loop        */
@@ -315,6 +329,8 @@ RTCORE_API int32_t rt_ctx_destroy(rt_ctx* ctx);
 RTCORE_API int32_t rt_ctx_set_texture(rt_ctx* ctx, uint32_t index, const RtTextureDesc* desc);
 /* Reads (and optionally zeroes) the statistics; synchronises `stream`. */
 RTCORE_API int32_t rt_ctx_read_stats(rt_ctx* ctx, RtStats* out, int32_t reset, void* stream);
+/* Waits for and reads the kernel times of the last timed trace launch. */
+RTCORE_API int32_t rt_ctx_read_trace_timings(rt_ctx* ctx, RtTraceTimings* out);
 RTCORE_API const char* rt_last_error_string(void);
 RTCORE_API const char* rt_version_string(void);
 /* Kernels this library has launched in this process (diagnostics). */
@@ -424,5 +440,6 @@ RT_STATIC_ASSERT(sizeof(RtRay) == 32, "ray is 32 bytes");
 RT_STATIC_ASSERT(sizeof(RtHit) == 32, "hit is 32 bytes");
 RT_STATIC_ASSERT(sizeof(RtShaderBindingTable) == 72, "sbt is 72 bytes");
 RT_STATIC_ASSERT(sizeof(RtTraceRaysDesc) == 40, "trace desc is 40 bytes");
+RT_STATIC_ASSERT(sizeof(RtTraceTimings) == 32, "timings are 32 bytes");
 
 #endif /* RTCORE_H */

@@ -62,6 +62,7 @@ RT_PROGRAM_CLOSEST_HIT_PORTAL = 3
 RT_PROGRAM_ANY_HIT_ALPHA_CLIP = 1
 RT_TRACE_FLAG_COLLECT_STATS = 0x1
 RT_TRACE_FLAG_LAMBERT_DIFFUSE = 0x2
+RT_TRACE_FLAG_KERNEL_TIMINGS = 0x4
 RT_CTX_THREADSAFE = 0x1
 RT_FN_V_SMITH_GGX_CORRELATED = 0
 RT_FN_D_GGX = 1
@@ -215,6 +216,22 @@ class RtHit(C.Structure):
     ]
 
 
+class RtTraceTimings(C.Structure):
+    _fields_ = [
+        ("total_ms", C.c_float),
+        ("trace_ms", C.c_float),
+        ("closest_ms", C.c_float),
+        ("shadow_ms", C.c_float),
+        ("shade_ms", C.c_float),
+        ("other_ms", C.c_float),
+        ("trace_launches", C.c_uint32),
+        ("_padding", C.c_uint32),
+    ]
+
+    def as_dict(self) -> dict:
+        return {f: getattr(self, f) for f, _ in self._fields_ if not f.startswith("_")}
+
+
 class RtStats(C.Structure):
     _fields_ = [
         ("traversals", C.c_uint64),
@@ -251,6 +268,7 @@ EXPORTED_FUNCTIONS = {
     "rt_ctx_destroy": (C.c_int32, [C.c_void_p]),
     "rt_ctx_set_texture": (C.c_int32, [C.c_void_p, C.c_uint32, C.POINTER(RtTextureDesc)]),
     "rt_ctx_read_stats": (C.c_int32, [C.c_void_p, C.POINTER(RtStats), C.c_int32, C.c_void_p]),
+    "rt_ctx_read_trace_timings": (C.c_int32, [C.c_void_p, C.POINTER(RtTraceTimings)]),
     "rt_last_error_string": (C.c_char_p, []),
     "rt_version_string": (C.c_char_p, []),
     "rt_kernel_launch_count": (C.c_uint64, []),
@@ -353,3 +371,4 @@ def check_layouts() -> None:
     assert C.sizeof(RtTextureDesc) == 32
     assert C.sizeof(RtShaderBindingTable) == 72
     assert C.sizeof(RtTraceRaysDesc) == 40
+    assert C.sizeof(RtTraceTimings) == 32

@@ -91,6 +91,7 @@ struct rt_ctx {
     std::atomic<uint32_t> work_slot{0};
     std::mutex mu;
     std::vector<Workspace> workspaces;
+    KernelTimer timer;
 };
 
 namespace {
@@ -157,9 +158,33 @@ RTCORE_API int32_t rt_ctx_create(uint32_t flags, rt_ctx** out) {
     return RT_OK;
 }
 
+RTCORE_API int32_t rt_ctx_read_trace_timings(rt_ctx* ctx, RtTraceTimings* out) {
+    if (!ctx || !out) return fail(RT_ERR_INVALID, "ctx or out is NULL");
+    memset(out, 0, sizeof *out);
+    const KernelTimer& t = ctx->timer;
+    if (!t.created || t.n < 2) return fail(RT_ERR_INVALID, "no trace launch was timed (RT_TRACE_FLAG_KERNEL_TIMINGS)");
+    cudaError_t e = cudaEventSynchronize(t.ev[t.n - 1]);
+    if (e != cudaSuccess) return cuda_fail(e, "rt_ctx_read_trace_timings");
+    for (int i = 1; i < t.n; i++) {
+        float ms = 0.0f;
+        e = cudaEventElapsedTime(&ms, t.ev[i - 1], t.ev[i]);
+        if (e != cudaSuccess) return cuda_fail(e, "rt_ctx_read_trace_timings");
+        out->total_ms += ms;
+        switch (t.kind[i]) {
+            case kKernClosest: out->closest_ms += ms; out->trace_ms += ms; out->trace_launches++; break;
+            case kKernShadow: out->shadow_ms += ms; out->trace_ms += ms; out->trace_launches++; break;
+            case kKernShade: out->shade_ms += ms; break;
+            default: out->other_ms += ms; break;
+        }
+    }
+    return RT_OK;
+}
+
 RTCORE_API int32_t rt_ctx_destroy(rt_ctx* ctx) {
     if (!ctx) return RT_OK;
     cudaDeviceSynchronize();
+    if (ctx->timer.created)
+        for (int i = 0; i < KernelTimer::kMax; i++) cudaEventDestroy(ctx->timer.ev[i]);
     for (auto& w : ctx->workspaces)
         if (w.ptr) cudaFree(w.ptr);
     if (ctx->dev) cudaFree(ctx->dev);
@@ -507,7 +532,16 @@ RTCORE_API int32_t rt_cmd_trace_rays(rt_ctx* ctx, const RtPushConstantBufferAddr
     uint8_t* ws = nullptr;
     cudaError_t e = ctx_workspace(ctx, s, trace_workspace_bytes(desc->width, desc->height), &ws);
     if (e != cudaSuccess) return cuda_fail(e, "rt_cmd_trace_rays (workspace)");
-    e = launch_trace_rays(p, ws, ctx->num_sms, s);
+    KernelTimer* timer = nullptr;
+    if (desc->flags & RT_TRACE_FLAG_KERNEL_TIMINGS) {
+        if (!ctx->timer.created) {
+            for (int i = 0; i < KernelTimer::kMax && e == cudaSuccess; i++) e = cudaEventCreate(&ctx->timer.ev[i]);
+            if (e != cudaSuccess) return cuda_fail(e, "rt_cmd_trace_rays (timing events)");
+            ctx->timer.created = true;
+        }
+        timer = &ctx->timer;
+    }
+    e = launch_trace_rays(p, ws, ctx->num_sms, s, timer);
     if (e != cudaSuccess) return cuda_fail(e, "rt_cmd_trace_rays");
     return RT_OK;
 }

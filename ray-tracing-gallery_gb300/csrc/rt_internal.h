@@ -68,7 +68,19 @@ struct TraceLaunch {
 };
 // Bytes of the wavefront workspace a width x height launch needs.
 uint64_t trace_workspace_bytes(uint32_t width, uint32_t height);
-cudaError_t launch_trace_rays(const TraceLaunch& p, uint8_t* workspace, int num_sms, cudaStream_t stream);
+
+// CUDA events recorded after each kernel of a trace launch
+// (RT_TRACE_FLAG_KERNEL_TIMINGS); kind[i] names the kernel that ended at ev[i].
+enum : uint8_t { kKernStart = 0, kKernOther = 1, kKernClosest = 2, kKernShadow = 3, kKernShade = 4 };
+struct KernelTimer {
+    static constexpr int kMax = 160;
+    cudaEvent_t ev[kMax];
+    uint8_t kind[kMax];
+    int n = 0;
+    bool created = false;
+};
+cudaError_t launch_trace_rays(const TraceLaunch& p, uint8_t* workspace, int num_sms, cudaStream_t stream,
+                              KernelTimer* timer);
 
 struct RayBufferLaunch {
     RtPushConstantBufferAddresses push;  // model_info may be 0

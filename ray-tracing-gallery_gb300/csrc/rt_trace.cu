@@ -788,7 +788,16 @@ uint64_t trace_workspace_bytes(uint32_t width, uint32_t height) {
     return b;
 }
 
-cudaError_t launch_trace_rays(const TraceLaunch& p, uint8_t* ws, int num_sms, cudaStream_t stream) {
+cudaError_t launch_trace_rays(const TraceLaunch& p, uint8_t* ws, int num_sms, cudaStream_t stream,
+                              KernelTimer* timer) {
+    auto mark = [&](uint8_t kind) {
+        if (timer && timer->n < KernelTimer::kMax) {
+            timer->kind[timer->n] = kind;
+            cudaEventRecord(timer->ev[timer->n++], stream);
+        }
+    };
+    if (timer) timer->n = 0;
+    mark(kKernStart);
     const uint32_t W = p.desc.width, H = p.desc.height;
     uint64_t tiles = (uint64_t)((W + 7) / 8) * ((H + 3) / 4);
     uint64_t slots = tiles * 32, pix = (uint64_t)W * H;
@@ -820,16 +829,22 @@ cudaError_t launch_trace_rays(const TraceLaunch& p, uint8_t* ws, int num_sms, cu
     if (err != cudaSuccess) return err;
     const bool stats = (p.desc.flags & RT_TRACE_FLAG_COLLECT_STATS) != 0;
     note_launch(), k_raygen<<<(uint32_t)((slots + 255) / 256), 256, 0, stream>>>(P);
+    mark(kKernOther);
     for (uint32_t b = 0; b < p.desc.max_trace_depth; b++) {
         P.bounce = b;
         launch_trace_mode<kModeBounce>(P, stats, num_sms, stream);
+        mark(kKernClosest);
         note_launch(), k_shade<<<(uint32_t)((slots + 127) / 128), 128, 0, stream>>>(P);
+        mark(kKernShade);
     }
     if (p.desc.shadow_ray_count > 0) {
         launch_trace_mode<kModeShadow>(P, stats, num_sms, stream);
+        mark(kKernShadow);
         note_launch(), k_resolve<<<(uint32_t)((pix + 255) / 256), 256, 0, stream>>>(P);
+        mark(kKernOther);
     }
     note_launch(), k_output<<<(uint32_t)((pix + 255) / 256), 256, 0, stream>>>(P);
+    mark(kKernOther);
     return cudaGetLastError();
 }
 
