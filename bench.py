@@ -49,6 +49,11 @@ WORKLOAD = ("full plain feature set, 1920x1080, 256 instances (torus 64x32 / dis
             "with a TLAS rebuild each frame, 4 blue-noise soft shadows (2 deg), 1 reflection bounce")
 L2_FLUSH_BYTES = 256 << 20
 NODE_BYTES, TRI_BYTES, RAY_BYTES, HIT_BYTES, INST_BYTES = 256, 48, 32, 16, 128
+QNODE_BYTES, RAY_HIT_BYTES = 96, 32
+PRECISION_RAYS = 4 << 20
+PRECISION_WORKLOAD = ("precision: displaced icosphere (level 9, every triangle bisected on its longest edge: "
+                      "10,485,760 triangles, radius 10, 0.5 fbm displacement), 4,194,304 random rays per step "
+                      "(origins U[-15,15]^3, directions uniform on S^2, tmin 0, tmax inf), closest hit")
 
 
 def parse_args():
@@ -60,6 +65,11 @@ def parse_args():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--width", type=int, default=WIDTH)
     p.add_argument("--height", type=int, default=HEIGHT)
+    p.add_argument("--workload", default="frame", choices=["frame", "precision"],
+                   help="frame: the full 1080p frame (default); precision: 10,485,760-triangle icosphere, "
+                        "4M random rays, quantised vs FP32 nodes")
+    p.add_argument("--precision-level", type=int, default=9, help=argparse.SUPPRESS)
+    p.add_argument("--precision-rays", type=int, default=PRECISION_RAYS, help=argparse.SUPPRESS)
     return p.parse_args()
 
 
@@ -70,10 +80,10 @@ def dist_env():
     return rank, world, local
 
 
-def profiled_traffic():
+def profiled_traffic(name: str = "k_trace_full_1080p.md"):
     """DRAM bytes per traversal launch from the committed ncu summary of this
-    workload (profiles/k_trace_full_1080p.md, line `dram_bytes_per_launch: N`)."""
-    p = ROOT / "profiles" / "k_trace_full_1080p.md"
+    workload (profiles/<name>, line `dram_bytes_per_launch: N`)."""
+    p = ROOT / "profiles" / name
     if not p.exists():
         return None
     for line in p.read_text().splitlines():
@@ -383,9 +393,228 @@ def bench_ours(args):
         dist.destroy_process_group()
 
 
+PRECISION_RAY_SEED = 2024
+
+
+def precision_inputs(args):
+    model = scenes.precision_mesh(level=args.precision_level)
+    sc = scenes.single_mesh_scene(model)
+    rays = scenes.random_rays(args.precision_rays, PRECISION_RAY_SEED, 30.0)
+    return sc, rays
+
+
+def precision_cpu(sc, rays, budget_s: float = 12.0) -> dict:
+    """The oracle tracing chunks of the step's rays (FP32, all host threads)
+    until about `budget_s` seconds of CPU work; the BVH build is untimed."""
+    from oracle.oracle import OracleScene, default_threads
+
+    threads = default_threads()
+    o = OracleScene(sc)
+    chunk = 1 << 18
+    done, t_total = 0, 0.0
+    while t_total < budget_s and done < len(rays):
+        part = rays[done:done + chunk]
+        t = time.perf_counter()
+        o.trace(part, with_models=False, threads=threads)
+        t_total += time.perf_counter() - t
+        done += len(part)
+    return {"value": done / t_total / 1e6, "unit": "Mrays/s", "cores": threads, "kind": "port",
+            "sample": f"first {done} of the step's {len(rays)} rays ({t_total:.1f} s; binary SAH host BVH, "
+                      f"build untimed)"}
+
+
+def bench_precision_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    from oracle.oracle import OracleScene, default_threads
+
+    threads = default_threads()
+    sc, rays = precision_inputs(args)
+    o = OracleScene(sc)
+    chunk = max(1, len(rays) // 16)
+    times, traced = [], 0
+    for k in range(args.warmup + args.steps):
+        i0 = (k * chunk) % len(rays)
+        part = rays[i0:i0 + chunk]
+        t = time.perf_counter()
+        o.trace(part, with_models=False, threads=threads)
+        dt = time.perf_counter() - t
+        if k >= args.warmup:
+            times.append(dt)
+            traced += len(part)
+    total = sum(times)
+    value = traced / total / 1e6
+    print(json.dumps({
+        "impl": "reference", "metric": "Mrays/s", "value": value, "unit": "Mrays/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": PRECISION_WORKLOAD, "sample": f"{chunk} of the {len(rays)} rays per step"},
+        "cpu_baseline": {"value": value, "unit": "Mrays/s", "cores": threads, "kind": "port",
+                         "sample": f"{chunk} rays per step, {args.steps} steps"},
+        "e2e": {"value": value, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+
+
+def bench_precision(args):
+    """Quantised (8-bit child boxes) against FP32 nodes over the same mesh and
+    rays: one step = one rt_cmd_trace_ray_buffer launch over all rays."""
+    import torch
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    from rtgallery import host
+
+    dev = host.Device()
+    lib = dev.lib
+    sc, rays = precision_inputs(args)
+    n = len(rays)
+    stream = torch.cuda.current_stream()
+    sh = host.Device.stream_handle(stream)
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    rays_dev = host.Device.upload(rays)
+    hits_dev = torch.empty(n * RAY_HIT_BYTES, dtype=torch.uint8, device="cuda")
+    arms = {}
+    for name, flags in (("fp32", abi.RT_BUILD_PREFER_FAST_TRACE),
+                        ("quantized", abi.RT_BUILD_PREFER_FAST_TRACE | abi.RT_BUILD_QUANTIZED_NODES)):
+        torch.cuda.synchronize()
+        b0, b1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        b0.record(stream)
+        gs = host.GpuScene(dev, sc, blas_flags=flags, stream=stream)
+        b1.record(stream)
+        torch.cuda.synchronize()
+        info = gs.models[0].blas.info(dev)
+        arms[name] = {"scene": gs, "build_ms": b0.elapsed_time(b1), "blas_bytes": int(info.total_size),
+                      "node_bytes": int(info.node_bytes), "nodes": int(info.node_count)}
+
+    def launch(gs, ray_ptr, hit_ptr, ray_flags=0):
+        push = abi.RtPushConstantBufferAddresses()
+        dev.check(lib.rt_cmd_trace_ray_buffer(dev.ctx, gs.tlas.device_address(), C.byref(push), None, ray_flags,
+                                              0xFF, 0, ray_ptr, n, hit_ptr, sh))
+
+    def timed(gs, steps):
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        for i in range(steps):
+            flush.fill_(i & 0xFF)
+            ev[i][0].record(stream)
+            launch(gs, rays_dev.data_ptr(), hits_dev.data_ptr())
+            ev[i][1].record(stream)
+        torch.cuda.synchronize()
+        return [a.elapsed_time(b) for a, b in ev]
+
+    for arm in arms.values():
+        timed(arm["scene"], args.warmup)
+    # both arms' hits must agree bit for bit before anything is reported
+    launch(arms["fp32"]["scene"], rays_dev.data_ptr(), hits_dev.data_ptr())
+    h_fp32 = hits_dev.clone()
+    launch(arms["quantized"]["scene"], rays_dev.data_ptr(), hits_dev.data_ptr())
+    torch.cuda.synchronize()
+    identical = bool(torch.equal(h_fp32, hits_dev))
+    hit_rate = float((h_fp32.view(torch.int32).view(-1, 8)[:, 3] != -1).float().mean())  # instance_id
+    del h_fp32
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    launches0 = lib.rt_kernel_launch_count()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    for name in ("fp32", "quantized"):
+        arms[name]["ms"] = timed(arms[name]["scene"], args.steps)
+    if dist:
+        dist.barrier()
+    launches = lib.rt_kernel_launch_count() - launches0
+    clk = clocks.stop()
+    for arm in arms.values():
+        total_ms = sum(arm["ms"])
+        if dist:
+            t = torch.tensor([total_ms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            total_ms = float(t.item())
+        arm["total_ms"] = total_ms
+        arm["value"] = n * world * args.steps / (total_ms / 1e3) / 1e6
+
+    # algorithmic bytes per launch: an untimed statistics launch per arm
+    for arm in arms.values():
+        dev.read_stats(reset=True)
+        launch(arm["scene"], rays_dev.data_ptr(), hits_dev.data_ptr(), abi.RT_RAY_FLAG_EXT_COLLECT_STATS)
+        s = dev.read_stats(reset=True)
+        arm["stats"] = s
+        arm["bytes_per_launch"] = (n * (RAY_BYTES + RAY_HIT_BYTES) + s["nodes_visited"] * arm["node_bytes"] +
+                                   s["triangles_tested"] * TRI_BYTES + s["instances_visited"] * INST_BYTES)
+        arm["gbs"] = arm["bytes_per_launch"] / (arm["total_ms"] / args.steps / 1e3) / 1e9
+
+    # end to end through the C ABI: rays from pinned host memory in, hits out
+    q = arms["quantized"]["scene"]
+    rays_pinned = torch.from_numpy(rays.view(np.uint8).reshape(-1).copy()).pin_memory()
+    hits_pinned = torch.empty(n * RAY_HIT_BYTES, dtype=torch.uint8).pin_memory()
+    rays_stage = torch.empty(n * RAY_BYTES, dtype=torch.uint8, device="cuda")
+    e2e_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    torch.cuda.synchronize()
+    for i in range(args.steps):
+        flush.fill_(i & 0xFF)
+        e2e_ev[i][0].record(stream)
+        rays_stage.copy_(rays_pinned, non_blocking=True)
+        launch(q, rays_stage.data_ptr(), hits_dev.data_ptr())
+        hits_pinned.copy_(hits_dev, non_blocking=True)
+        e2e_ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = sum(a.elapsed_time(b) for a, b in e2e_ev)
+    e2e_value = n * world * args.steps / (e2e_ms / 1e3) / 1e6
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = precision_cpu(sc, rays)
+    peak, peak_kind = measured_peaks()
+    qa, fa = arms["quantized"], arms["fp32"]
+    if rank == 0:
+        def summary(a):
+            s = a["stats"]
+            return {"mrays_s": a["value"], "ms_per_step": a["total_ms"] / args.steps, "gb_s": a["gbs"],
+                    "bytes_per_ray": a["bytes_per_launch"] / n, "nodes_per_ray": s["nodes_visited"] / n,
+                    "triangles_per_ray": s["triangles_tested"] / n, "node_bytes": a["node_bytes"],
+                    "blas_bytes": a["blas_bytes"], "wide_nodes": a["nodes"], "blas_build_ms": a["build_ms"]}
+
+        print(json.dumps({
+            "metric": "Mrays/s", "value": qa["value"], "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": qa["total_ms"] / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (procedural mesh and rays from seeds)",
+            "config": {"workload": PRECISION_WORKLOAD, "path": "8-bit quantised child boxes (value) vs FP32 boxes",
+                       "rays": n, "triangles": int(sum(len(g.indices) for g in sc.models[0].geometries)),
+                       "parallelism": f"replicas x{world}",
+                       "l2": "flushed between steps (256 MiB write outside the timed events); BVH >> L2",
+                       "hits_identical_quantized_vs_fp32": identical, "hit_rate": hit_rate,
+                       "quantized": summary(qa), "fp32": summary(fa),
+                       "speedup_quantized_over_fp32": qa["value"] / fa["value"]},
+            "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": n * RAY_BYTES,
+                    "d2h_bytes_per_step": n * RAY_HIT_BYTES},
+            "roofline": {"bound": "hbm", "achieved": qa["gbs"], "peak": peak, "unit": "GB/s", "frac": qa["gbs"] / peak,
+                         "traffic": profiled_traffic("k_trace_ray_buffer_precision.md"),
+                         "kernel": "k_trace_ray_buffer (quantised BLAS)",
+                         "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
+                         else "fallback 6.8 TB/s",
+                         "algorithmic_bytes_per_launch": qa["bytes_per_launch"]},
+            "cpu_baseline": cpu,
+            "clocks": clk,
+            "gpu_launches": int(launches),
+        }))
+    dev.close()
+    if dist:
+        dist.destroy_process_group()
+
+
 def main():
     args = parse_args()
-    if args.impl == "reference":
+    if args.workload == "precision":
+        if args.impl == "reference":
+            bench_precision_reference(args)
+        else:
+            bench_precision(args)
+    elif args.impl == "reference":
         bench_reference(args)
     else:
         bench_ours(args)

@@ -193,7 +193,7 @@ typedef struct RtAccelerationStructureInfo {
     uint32_t build_flags;
     uint32_t node_count;        /* wide nodes in use                          */
     uint32_t primitive_count;   /* triangles (BLAS) or instances (TLAS)       */
-    uint32_t node_bytes;        /* 256 (FP32 boxes) or 128 (quantised)        */
+    uint32_t node_bytes;        /* 256 (FP32 boxes) or 96 (quantised)         */
     uint32_t tree_depth;        /* wide levels                                */
     uint64_t total_size;        /* bytes this AS occupies as built            */
     uint64_t compacted_size;    /* bytes a COMPACT copy needs                 */

@@ -28,6 +28,7 @@ struct CtxDevice {
 
 thread_local std::string g_last_error;
 std::atomic<unsigned long long> g_kernel_launches{0};
+std::atomic<uint32_t> g_blas_kinds{0};
 
 int32_t fail(int32_t code, const char* fmt, ...) {
     char buf[512];
@@ -72,6 +73,8 @@ int32_t check_sbt(const RtShaderBindingTable* sbt) {
 }  // namespace
 
 void rt::note_launch() { g_kernel_launches.fetch_add(1, std::memory_order_relaxed); }
+void rt::note_blas_kind(uint32_t kind) { g_blas_kinds.fetch_or(kind, std::memory_order_relaxed); }
+uint32_t rt::blas_kinds_built() { return g_blas_kinds.load(std::memory_order_relaxed); }
 
 // Wavefront workspace of one stream: grown stream-ordered (cudaFreeAsync /
 // cudaMallocAsync on that stream), so launches on one stream reuse it
@@ -249,12 +252,12 @@ static int32_t blas_prim_count(const RtGeometryTriangles* g, uint32_t count, uin
 RTCORE_API int32_t rt_get_blas_build_sizes(const RtGeometryTriangles* geometries, uint32_t geometry_count,
                                            uint32_t build_flags, RtBuildSizes* out) {
     if (!out) return fail(RT_ERR_INVALID, "out is NULL");
-    (void)build_flags;
     uint32_t n = 0;
     int32_t r = blas_prim_count(geometries, geometry_count, &n);
     if (r) return r;
-    AsLayout al = AsLayout::make(n, false);
-    ScratchLayout sl = ScratchLayout::make(n, false);
+    const bool quantized = (build_flags & RT_BUILD_QUANTIZED_NODES) != 0;
+    AsLayout al = AsLayout::make(n, false, quantized);
+    ScratchLayout sl = ScratchLayout::make(n, false, quantized);
     out->acceleration_structure_size = al.total;
     out->build_scratch_size = sl.build_total;
     out->update_scratch_size = sl.update_total;
@@ -268,10 +271,9 @@ RTCORE_API int32_t rt_cmd_build_blas(rt_ctx* ctx, const RtGeometryTriangles* geo
     uint32_t n = 0;
     int32_t r = blas_prim_count(geometries, geometry_count, &n);
     if (r) return r;
-    if (build_flags & RT_BUILD_QUANTIZED_NODES)
-        return fail(RT_ERR_UNSUPPORTED, "RT_BUILD_QUANTIZED_NODES is not available in this build");
-    AsLayout al = AsLayout::make(n, false);
-    ScratchLayout sl = ScratchLayout::make(n, false);
+    const bool quantized = (build_flags & RT_BUILD_QUANTIZED_NODES) != 0;
+    AsLayout al = AsLayout::make(n, false, quantized);
+    ScratchLayout sl = ScratchLayout::make(n, false, quantized);
     if (!dst || !aligned(dst, RT_AS_ALIGNMENT)) return fail(RT_ERR_INVALID, "dst must be non-null and 256-byte aligned");
     if (dst_size < al.total)
         return fail(RT_ERR_INVALID, "dst_size %llu < required %llu", (unsigned long long)dst_size,
@@ -299,6 +301,7 @@ RTCORE_API int32_t rt_cmd_build_blas(rt_ctx* ctx, const RtGeometryTriangles* geo
     cudaError_t e = launch_blas_build(in, build_flags, reinterpret_cast<uint8_t*>(dst),
                                       reinterpret_cast<uint8_t*>(scratch), reinterpret_cast<cudaStream_t>(stream));
     if (e != cudaSuccess) return cuda_fail(e, "rt_cmd_build_blas");
+    note_blas_kind((build_flags & RT_BUILD_QUANTIZED_NODES) ? kBlasKindQ8 : kBlasKindF32);
     return RT_OK;
 }
 
@@ -350,7 +353,7 @@ RTCORE_API int32_t rt_cmd_build_blas_static_scratch(rt_ctx* ctx, const RtGeometr
     int32_t r = blas_prim_count(geometries, geometry_count, &n);
     if (r) return r;
     if (build_flags & RT_BUILD_QUANTIZED_NODES)
-        return fail(RT_ERR_UNSUPPORTED, "RT_BUILD_QUANTIZED_NODES is not available in this build");
+        return fail(RT_ERR_UNSUPPORTED, "RT_BUILD_QUANTIZED_NODES is not supported by the static-scratch build");
     AsLayout al = AsLayout::make(n, false);
     ScratchLayout sl = ScratchLayout::make(n, false);
     if (!dst || !aligned(dst, RT_AS_ALIGNMENT)) return fail(RT_ERR_INVALID, "dst must be non-null and 256-byte aligned");
@@ -383,6 +386,7 @@ RTCORE_API int32_t rt_cmd_build_blas_static_scratch(rt_ctx* ctx, const RtGeometr
     e = launch_blas_build(in, build_flags, reinterpret_cast<uint8_t*>(dst), scratch,
                           reinterpret_cast<cudaStream_t>(stream));
     if (e != cudaSuccess) return cuda_fail(e, "rt_cmd_build_blas_static_scratch");
+    note_blas_kind(kBlasKindF32);
     return RT_OK;
 }
 
@@ -528,6 +532,7 @@ RTCORE_API int32_t rt_cmd_trace_rays(rt_ctx* ctx, const RtPushConstantBufferAddr
     p.stats = &ctx->dev->stats;
     p.status = &ctx->dev->stats.status;
     p.work = nullptr;
+    p.kinds_built = blas_kinds_built();
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     uint8_t* ws = nullptr;
     cudaError_t e = ctx_workspace(ctx, s, trace_workspace_bytes(desc->width, desc->height), &ws);
@@ -576,6 +581,7 @@ RTCORE_API int32_t rt_cmd_trace_ray_buffer(rt_ctx* ctx, uint64_t tlas, const RtP
     p.stats = &ctx->dev->stats;
     p.status = &ctx->dev->stats.status;
     p.work = &ctx->dev->work[ctx->work_slot.fetch_add(1) % kWorkSlots];
+    p.kinds_built = blas_kinds_built();
     cudaError_t e = launch_trace_ray_buffer(p, ctx->num_sms, reinterpret_cast<cudaStream_t>(stream));
     if (e != cudaSuccess) return cuda_fail(e, "rt_cmd_trace_ray_buffer");
     return RT_OK;

@@ -48,6 +48,7 @@ struct BuildState {
     uint32_t frontier_count[kLevels + 2];
     uint32_t error;
     uint32_t depth;
+    uint32_t blas_kinds;  // TLAS: kBlasKind* bits of the BLASes its instances enter
 };
 
 __device__ __forceinline__ uint32_t f2o(float f) {
@@ -110,6 +111,7 @@ __global__ void k_init_state(BuildState* st) {
         for (int k = 0; k < kLevels + 2; k++) st->frontier_count[k] = 0;
         st->error = 0;
         st->depth = 1;
+        st->blas_kinds = 0;
     }
 }
 
@@ -251,7 +253,7 @@ __device__ bool fill_instance(const RtAccelerationStructureInstance& r, uint32_t
             if (!finite3(lo) || !finite3(hi)) valid = false;
             if (valid) {
                 rec->tri_count = bh->prim_count;
-                rec->node_count = bh->node_count;
+                rec->node_count = bh->node_count | (bh->node_bytes == kQNodeBytes ? kQuantizedBlasBit : 0u);
                 rec->prims_off256 = (uint32_t)(bh->prims_offset / 256);
             }
         }
@@ -271,6 +273,7 @@ __global__ void k_tlas_prims(const RtAccelerationStructureInstance* inst, uint32
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     float cmin[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, cmax[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
     float bmin[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, bmax[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    uint32_t kinds = 0;
     if (i < n) {
         RtAccelerationStructureInstance r = inst[i];
         InstRecord rec;
@@ -282,11 +285,14 @@ __global__ void k_tlas_prims(const RtAccelerationStructureInstance* inst, uint32
                 bmin[k] = lo[k];
                 bmax[k] = hi[k];
             }
+            kinds = blas_kind(rec.node_count);
         }
         temp[i] = rec;
         boxes[2 * (size_t)i] = make_float4(lo[0], lo[1], lo[2], 0.0f);
         boxes[2 * (size_t)i + 1] = make_float4(hi[0], hi[1], hi[2], 0.0f);
     }
+    kinds = __reduce_or_sync(0xFFFFFFFFu, kinds);
+    if ((threadIdx.x & 31u) == 0 && kinds) atomicOr(&st->blas_kinds, kinds);
     reduce_bounds(st, cmin, cmax, bmin, bmax);
 }
 
@@ -714,8 +720,79 @@ __global__ void k_write_insts(const InstRecord* temp, const uint32_t* vals, uint
     out[i] = temp[vals[i]];
 }
 
+// ---- 8-bit quantised nodes ----------------------------------------------------
+// Smallest biased exponent e (quantum s = 2^(e-127)) with ext <= 252 s and
+// |floor(L / s)| + 512 < 2^24, so that the grid origin (floor(L/s) - 1) s and
+// every decoded plane origin + q s (q <= 255) are exact floats.
+__device__ uint32_t quantum_exponent(float L, float ext) {
+    uint32_t e = (__float_as_uint(ext / 252.0f) >> 23) & 0xFFu;
+    uint32_t el = (__float_as_uint(fabsf(L)) >> 23) & 0xFFu;
+    e = max(e, el > 23u ? el - 23u : 1u);
+    if (e < 1u) e = 1u;
+    for (; e < 254u; e++) {
+        float s = __uint_as_float(e << 23);
+        if (ext > 252.0f * s) continue;
+        float k = floorf(L / s);
+        if (!(fabsf(k) < 16776704.0f)) continue;
+        return e;
+    }
+    return 254u;
+}
+
+__global__ void k_quantize_nodes(const WideNode* in, const uint32_t* node_count, uint32_t max_nodes, QNode* out) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t count = min(*node_count, max_nodes);
+    if (i >= count) return;
+    const WideNode& nd = in[i];
+    QNode q;
+    float lo[3][8], hi[3][8];
+    bool valid[8];
+    float L[3] = {INFINITY, INFINITY, INFINITY}, H[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int k = 0; k < 8; k++) {
+        q.child_ref[k] = nd.child_ref[k];
+        lo[0][k] = nd.lox[k]; lo[1][k] = nd.loy[k]; lo[2][k] = nd.loz[k];
+        hi[0][k] = nd.hix[k]; hi[1][k] = nd.hiy[k]; hi[2][k] = nd.hiz[k];
+        valid[k] = nd.child_ref[k] != kChildEmpty;
+        for (int a = 0; a < 3; a++) valid[k] = valid[k] && lo[a][k] <= hi[a][k] && fabsf(lo[a][k]) <= FLT_MAX &&
+                                               fabsf(hi[a][k]) <= FLT_MAX;
+        if (!valid[k]) continue;
+        for (int a = 0; a < 3; a++) {
+            L[a] = fminf(L[a], lo[a][k]);
+            H[a] = fmaxf(H[a], hi[a][k]);
+        }
+    }
+    uint8_t* qlo[3] = {q.qlo_x, q.qlo_y, q.qlo_z};
+    uint8_t* qhi[3] = {q.qhi_x, q.qhi_y, q.qhi_z};
+    for (int a = 0; a < 3; a++) {
+        if (!(L[a] <= H[a])) {  // no valid child: any grid, every child empty
+            q.origin[a] = 0.0f;
+            q.exp[a] = 127u;
+            for (int k = 0; k < 8; k++) { qlo[a][k] = 255u; qhi[a][k] = 0u; }
+            continue;
+        }
+        float ext = __fsub_ru(H[a], L[a]);
+        uint32_t e = quantum_exponent(L[a], ext);
+        float s = __uint_as_float(e << 23);
+        float origin = (floorf(L[a] / s) - 1.0f) * s;
+        q.origin[a] = origin;
+        q.exp[a] = (uint8_t)e;
+        for (int k = 0; k < 8; k++) {
+            if (!valid[k]) { qlo[a][k] = 255u; qhi[a][k] = 0u; continue; }
+            // outward rounding plus one quantum of slack on each side
+            float ql = floorf(__fsub_rd(lo[a][k], origin) / s) - 1.0f;
+            float qh = ceilf(__fsub_ru(hi[a][k], origin) / s) + 1.0f;
+            qlo[a][k] = (uint8_t)fminf(fmaxf(ql, 0.0f), 255.0f);
+            qhi[a][k] = (uint8_t)fminf(fmaxf(qh, 0.0f), 255.0f);
+        }
+    }
+    q._pad = 0;
+    const uint4* src = reinterpret_cast<const uint4*>(&q);
+    uint4* dst = reinterpret_cast<uint4*>(&out[i]);
+    for (int w = 0; w < 6; w++) dst[w] = src[w];
+}
+
 struct HeaderStatic {
-    uint32_t type, build_flags, prim_count, max_nodes, geometry_count, leaf_max;
+    uint32_t type, build_flags, prim_count, max_nodes, geometry_count, leaf_max, node_bytes;
     uint64_t total_size, nodes_offset, prims_offset, parents_offset;
     uint64_t prim_bytes;
 };
@@ -738,7 +815,7 @@ __global__ void k_finalize(AsHeader* h, const BuildState* st, HeaderStatic hs) {
     h->node_count = nc;
     h->prim_count = hs.prim_count;
     h->max_nodes = hs.max_nodes;
-    h->node_bytes = kNodeBytes;
+    h->node_bytes = hs.node_bytes;
     h->total_size = hs.total_size;
     h->nodes_offset = hs.nodes_offset;
     h->prims_offset = hs.prims_offset;
@@ -755,7 +832,8 @@ __global__ void k_finalize(AsHeader* h, const BuildState* st, HeaderStatic hs) {
     h->geometry_count = hs.geometry_count;
     h->depth = st->depth;
     h->leaf_max = hs.leaf_max;
-    uint64_t nodes_end = hs.nodes_offset + (uint64_t)nc * kNodeBytes;
+    h->blas_kinds = hs.type == kAsTypeTop ? st->blas_kinds : 0u;
+    uint64_t nodes_end = hs.nodes_offset + (uint64_t)nc * hs.node_bytes;
     uint64_t par = hs.parents_offset ? align_up(nodes_end, 256) : 0;
     uint64_t par_end = par ? par + (uint64_t)nc * 4 : nodes_end;
     h->compacted_size = align_up(align_up(par_end, 256) + hs.prim_count * hs.prim_bytes, 256);
@@ -770,13 +848,18 @@ __global__ void k_refit_insts(const RtAccelerationStructureInstance* inst, uint3
     InstRecord rec = recs[i];
     uint32_t id = rec.instance_id;
     float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    uint32_t kinds = 0;
     if (id < n) {
         RtAccelerationStructureInstance r = inst[id];
-        fill_instance(r, id, &rec, lo, hi, err);
+        if (fill_instance(r, id, &rec, lo, hi, err)) kinds = blas_kind(rec.node_count);
     } else {
         rec.tri_count = 0;
         atomicOr(err, 1u << RT_ERR_INVALID);
     }
+    // the kinds only grow here: a refit may add a BLAS kind, never drop one
+    const uint32_t active = __activemask();
+    kinds = __reduce_or_sync(active, kinds);
+    if ((threadIdx.x & 31u) == (uint32_t)(__ffs(active) - 1) && kinds) atomicOr(&h->blas_kinds, kinds);
     recs[i] = rec;
     sboxes[2 * (size_t)i] = make_float4(lo[0], lo[1], lo[2], 0.0f);
     sboxes[2 * (size_t)i + 1] = make_float4(hi[0], hi[1], hi[2], 0.0f);
@@ -877,7 +960,7 @@ __global__ void k_as_copy(const uint8_t* src, uint8_t* dst, uint64_t dst_size, u
             reinterpret_cast<AsHeader*>(dst)->status = RT_ERR_BAD_AS;
         return;
     }
-    uint64_t nodes_bytes = (uint64_t)h->node_count * kNodeBytes;
+    uint64_t nodes_bytes = (uint64_t)h->node_count * h->node_bytes;
     uint64_t prim_bytes = (uint64_t)h->prim_count * (h->type == kAsTypeTop ? kInstBytes : kTriBytes);
     uint64_t par_bytes = h->parents_offset ? (uint64_t)h->node_count * 4 : 0;
     uint64_t need = mode == RT_COPY_MODE_COMPACT ? h->compacted_size : h->total_size;
@@ -927,11 +1010,12 @@ inline uint32_t blocks_for(uint64_t n, uint32_t t) { return (uint32_t)((n + t - 
 // ---------------------------------------------------------------------------
 // Layouts
 // ---------------------------------------------------------------------------
-AsLayout AsLayout::make(uint32_t n, bool top) {
+AsLayout AsLayout::make(uint32_t n, bool top, bool quantized) {
     AsLayout l;
     l.max_nodes = (uint32_t)max_wide_nodes(n);
+    l.node_bytes = (quantized && !top) ? kQNodeBytes : kNodeBytes;
     l.nodes = kHeaderBytes;
-    uint64_t end = l.nodes + (uint64_t)l.max_nodes * kNodeBytes;
+    uint64_t end = l.nodes + (uint64_t)l.max_nodes * l.node_bytes;
     if (top) {
         l.parents = align_up(end, 256);
         end = l.parents + (uint64_t)l.max_nodes * 4;
@@ -943,7 +1027,7 @@ AsLayout AsLayout::make(uint32_t n, bool top) {
     return l;
 }
 
-ScratchLayout ScratchLayout::make(uint32_t n, bool top) {
+ScratchLayout ScratchLayout::make(uint32_t n, bool top, bool quantized) {
     ScratchLayout s{};
     uint64_t nn = n ? n : 1;
     uint64_t ni = n > 1 ? n - 1 : 1;
@@ -971,6 +1055,7 @@ ScratchLayout ScratchLayout::make(uint32_t n, bool top) {
     s.frontier0 = take(f * 16);
     s.frontier1 = take(f * 16);
     s.temp_inst = top ? take(nn * kInstBytes) : 0;
+    s.fp32_nodes = (quantized && !top) ? take(max_wide_nodes(n) * kNodeBytes) : 0;
     s.refit_counters = 0;
     s.build_total = o;
     // update (refit) scratch: sorted boxes + one counter per node
@@ -990,8 +1075,12 @@ namespace {
 cudaError_t build_common(uint32_t n, bool top, uint32_t build_flags, uint32_t geometry_count, uint8_t* dst,
                          uint8_t* scratch, cudaStream_t stream, const BlasInput* blas,
                          const RtAccelerationStructureInstance* inst) {
-    ScratchLayout sl = ScratchLayout::make(n, top);
-    AsLayout al = AsLayout::make(n, top);
+    const bool quantized = !top && (build_flags & RT_BUILD_QUANTIZED_NODES) != 0;
+    ScratchLayout sl = ScratchLayout::make(n, top, quantized);
+    AsLayout al = AsLayout::make(n, top, quantized);
+    // quantised builds collapse into FP32 nodes in scratch, then quantise
+    WideNode* fp32_nodes = quantized ? reinterpret_cast<WideNode*>(scratch + sl.fp32_nodes)
+                                     : reinterpret_cast<WideNode*>(dst + al.nodes);
     BuildState* st = reinterpret_cast<BuildState*>(scratch + sl.state);
     float4* boxes = reinterpret_cast<float4*>(scratch + sl.boxes);
     float4* sboxes = reinterpret_cast<float4*>(scratch + sl.sboxes);
@@ -1035,7 +1124,7 @@ cudaError_t build_common(uint32_t n, bool top, uint32_t build_flags, uint32_t ge
         cc.inodes = inodes;
         cc.iboxes = iboxes;
         cc.sboxes = sboxes;
-        cc.nodes = reinterpret_cast<WideNode*>(dst + al.nodes);
+        cc.nodes = fp32_nodes;
         cc.parents = top ? reinterpret_cast<uint32_t*>(dst + al.parents) : nullptr;
         cc.st = st;
         cc.leaf_max = top ? kTlasLeafMax : kBlasLeafMax;
@@ -1060,7 +1149,7 @@ cudaError_t build_common(uint32_t n, bool top, uint32_t build_flags, uint32_t ge
         }
     } else {
         CollapseCtx cc{};
-        cc.nodes = reinterpret_cast<WideNode*>(dst + al.nodes);
+        cc.nodes = fp32_nodes;
         cc.parents = top ? reinterpret_cast<uint32_t*>(dst + al.parents) : nullptr;
         cc.st = st;
         cc.leaf_max = 1;
@@ -1068,7 +1157,13 @@ cudaError_t build_common(uint32_t n, bool top, uint32_t build_flags, uint32_t ge
         cc.n = n;
         note_launch(), k_collapse_root<<<1, 32, 0, stream>>>(cc, 0, fr[0]);
     }
+    if (quantized) {
+        uint32_t g = blocks_for(al.max_nodes, 128);
+        note_launch(), k_quantize_nodes<<<g, 128, 0, stream>>>(fp32_nodes, &st->node_counter, al.max_nodes,
+                                                               reinterpret_cast<QNode*>(dst + al.nodes));
+    }
     HeaderStatic hs;
+    hs.node_bytes = al.node_bytes;
     hs.type = top ? kAsTypeTop : kAsTypeBottom;
     hs.build_flags = build_flags;
     hs.prim_count = n;

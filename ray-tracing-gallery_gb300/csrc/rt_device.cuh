@@ -47,7 +47,7 @@ struct AsHeader {
     uint32_t geometry_count;
     uint32_t depth;
     uint32_t leaf_max;
-    uint32_t _pad0;
+    uint32_t blas_kinds;      // TLAS: kBlasKind* bits of the BLASes its instances enter
     uint64_t compacted_size;
     uint8_t _pad[kHeaderBytes - 112];
 };
@@ -72,6 +72,31 @@ struct alignas(128) WideNode {
 static_assert(sizeof(WideNode) == kNodeBytes, "node size");
 __host__ __device__ inline uint32_t node_meta(uint32_t m0, uint32_t m1, int c) {
     return ((c < 4 ? m0 : m1) >> (8 * (c & 3))) & 0xFFu;
+}
+
+// 8-wide node with 8-bit quantised child boxes (RT_BUILD_QUANTIZED_NODES,
+// BLAS only), 96 bytes.  Per axis a: quantum s_a = 2^(exp[a] - 127); child
+// k's planes are origin_a + q * s_a with q = qlo / qhi bytes.  The builder
+// puts origin on the quantum grid one quantum below the node's union box and
+// rounds every child plane outward plus one more quantum, so the decoded box
+// contains the FP32 child box with at least one quantum to spare; an empty
+// child is qlo = 255, qhi = 0 (never hit).  child_ref is as in WideNode.
+constexpr uint32_t kQNodeBytes = 96;
+struct alignas(16) QNode {
+    float origin[3];
+    uint8_t exp[3];
+    uint8_t _pad;
+    uint32_t child_ref[8];
+    uint8_t qlo_x[8], qhi_x[8], qlo_y[8], qhi_y[8], qlo_z[8], qhi_z[8];
+};
+static_assert(sizeof(QNode) == kQNodeBytes, "qnode size");
+// InstRecord.node_count bit marking a BLAS with quantised nodes.
+constexpr uint32_t kQuantizedBlasBit = 0x80000000u;
+// AsHeader.blas_kinds bits of a TLAS: which node formats its instances use
+// (the traversal kernels pick a loop that handles exactly those).
+constexpr uint32_t kBlasKindF32 = 1u, kBlasKindQ8 = 2u;
+__host__ __device__ __forceinline__ uint32_t blas_kind(uint32_t inst_node_count) {
+    return (inst_node_count & kQuantizedBlasBit) ? kBlasKindQ8 : kBlasKindF32;
 }
 
 // Triangle record: v0.w = primitive index, v1.w = geometry index,

@@ -11,6 +11,12 @@ namespace rt {
 // Counts every kernel this library launches (rt_kernel_launch_count).
 void note_launch();
 
+// kBlasKind* bits of every BLAS node format this process has built.  A BLAS
+// blob only comes from a build here (or a copy of one), so a TLAS can only
+// name these formats; the trace launchers pick their kernel variants by it.
+void note_blas_kind(uint32_t kind);
+uint32_t blas_kinds_built();
+
 // One BLAS geometry as the build kernels see it.
 struct BuildGeom {
     const float* pos;
@@ -33,17 +39,19 @@ struct BlasInput {
 struct ScratchLayout {
     uint64_t boxes, sboxes, keys0, keys1, vals0, vals1, hist, inodes, iboxes, iparent, lparent, flags;
     uint64_t frontier0, frontier1, state, temp_inst, refit_counters;
+    uint64_t fp32_nodes;       // quantised builds: FP32 nodes before quantisation
     uint64_t build_total;
     uint64_t update_total;
     uint32_t sort_blocks;
-    static ScratchLayout make(uint32_t n, bool top_level);
+    static ScratchLayout make(uint32_t n, bool top_level, bool quantized = false);
 };
 
 // Byte offsets inside the AS blob.
 struct AsLayout {
     uint64_t nodes, parents, prims, total;
     uint32_t max_nodes;
-    static AsLayout make(uint32_t n, bool top_level);
+    uint32_t node_bytes;
+    static AsLayout make(uint32_t n, bool top_level, bool quantized = false);
 };
 
 constexpr uint32_t kMaxPrimitives = (1u << 28) - 1;  // leaf refs carry 28 bits
@@ -65,6 +73,7 @@ struct TraceLaunch {
     RtStats* stats;            // device
     uint32_t* status;          // device (same block)
     uint32_t* work;            // unused by the wavefront pipeline (kept for layout)
+    uint32_t kinds_built;      // blas_kinds_built() when the launch was recorded
 };
 // Bytes of the wavefront workspace a width x height launch needs.
 uint64_t trace_workspace_bytes(uint32_t width, uint32_t height);
@@ -97,6 +106,7 @@ struct RayBufferLaunch {
     RtStats* stats;
     uint32_t* status;
     uint32_t* work;            // device fetch counter for this launch (zeroed by the launcher)
+    uint32_t kinds_built;      // blas_kinds_built() when the launch was recorded
 };
 cudaError_t launch_trace_ray_buffer(const RayBufferLaunch& p, int num_sms, cudaStream_t stream);
 

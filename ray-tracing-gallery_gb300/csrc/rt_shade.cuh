@@ -30,6 +30,7 @@ struct Env {
     uint32_t* status;
     uint32_t tnode_count;
     uint32_t inst_count;
+    uint32_t blas_kinds;         // kBlasKind* bits (which traversal loop to run)
 };
 
 __device__ __forceinline__ Env make_env(uint64_t tlas, const RtPushConstantBufferAddresses& push,
@@ -42,6 +43,7 @@ __device__ __forceinline__ Env make_env(uint64_t tlas, const RtPushConstantBuffe
     bool ok = h->magic == kAsMagic && h->type == kAsTypeTop;
     e.tnode_count = ok ? h->node_count : 0u;
     e.inst_count = ok ? h->prim_count : 0u;
+    e.blas_kinds = ok ? h->blas_kinds : 0u;
     if (!ok) atomicOr(status, 1u << RT_ERR_BAD_AS);
     e.models = reinterpret_cast<const RtModelInfo*>(push.model_info);
     e.sbt = sbt;

@@ -25,6 +25,8 @@
 // warp-aggregated (one atomic per warp), which compacts the wavefronts.
 #include <algorithm>
 
+#include <type_traits>
+
 #include "rt_internal.h"
 #include "rt_shade.cuh"
 
@@ -141,6 +143,7 @@ struct Trav {
     uint32_t hit_inst;         // sorted TLAS index of the best hit, kNoHit if none
     uint32_t hit_geom, hit_prim;
     bool front, in_blas;
+    bool quant;                // current nodes are QNodes (a quantised BLAS)
     uint32_t entry;            // what the next step processes
     int sp;
     const WideNode* nodes;
@@ -170,6 +173,7 @@ __device__ __forceinline__ void trav_begin(Trav& s, const Env& e, V3 o, V3 d, fl
     s.nodes = e.tnodes;
     s.tris = nullptr;
     s.node_count = e.tnode_count;
+    s.quant = false;
     s.tri_count = 0;
     s.c_inst = 0;
     s.c_sbt_flags = 0;
@@ -192,10 +196,135 @@ __device__ __forceinline__ void trav_restore_world(Trav& s, const Env& e) {
     s.in_blas = false;
     s.nodes = e.tnodes;
     s.node_count = e.tnode_count;
+    s.quant = false;
     s.o = s.wo;
     s.d = s.wd;
     s.inv = safe_inv(s.wd);
     s.oct = octant_offsets(s.inv);
+}
+
+// Sort key of a child: tnear bits rounded down to 8 ulps | slot (ascending =
+// near first); 0xFFFFFFFF when the child is missed or empty.
+__device__ __forceinline__ uint32_t child_key(float tn, float tf, uint32_t ref, int k) {
+    bool hit = (ref != kChildEmpty) && (tn <= tf * kBoxFarScale);
+    return hit ? ((__float_as_uint(fmaxf(tn, 0.0f)) & ~7u) | (uint32_t)k) : 0xFFFFFFFFu;
+}
+
+// Slab tests of an FP32 8-wide node.  Near / far planes were chosen per ray
+// by the direction signs (s.oct): the loads fetch them directly, so each
+// child needs one subtract and one multiply per plane and no per-axis min/max.
+__device__ __forceinline__ void fnode_keys(const Trav& s, uint32_t entry, uint32_t keys[8], uint32_t refs[8]) {
+    const float4* np = reinterpret_cast<const float4*>(s.nodes + entry);
+    const uint32_t ox = s.oct & 0xFFu, oy = (s.oct >> 8) & 0xFFu, oz = s.oct >> 16;
+    float4 nx0 = __ldg(np + ox), nx1 = __ldg(np + ox + 1), fx0 = __ldg(np + (ox ^ 2u)), fx1 = __ldg(np + (ox ^ 2u) + 1);
+    float4 ny0 = __ldg(np + oy), ny1 = __ldg(np + oy + 1), fy0 = __ldg(np + (oy ^ 2u)), fy1 = __ldg(np + (oy ^ 2u) + 1);
+    float4 nz0 = __ldg(np + oz), nz1 = __ldg(np + oz + 1), fz0 = __ldg(np + (oz ^ 2u)), fz1 = __ldg(np + (oz ^ 2u) + 1);
+    uint4 r0 = __ldg(reinterpret_cast<const uint4*>(np + 12));
+    uint4 r1 = __ldg(reinterpret_cast<const uint4*>(np + 13));
+    const float nx[8] = {nx0.x, nx0.y, nx0.z, nx0.w, nx1.x, nx1.y, nx1.z, nx1.w};
+    const float fx[8] = {fx0.x, fx0.y, fx0.z, fx0.w, fx1.x, fx1.y, fx1.z, fx1.w};
+    const float ny[8] = {ny0.x, ny0.y, ny0.z, ny0.w, ny1.x, ny1.y, ny1.z, ny1.w};
+    const float fy[8] = {fy0.x, fy0.y, fy0.z, fy0.w, fy1.x, fy1.y, fy1.z, fy1.w};
+    const float nz[8] = {nz0.x, nz0.y, nz0.z, nz0.w, nz1.x, nz1.y, nz1.z, nz1.w};
+    const float fz[8] = {fz0.x, fz0.y, fz0.z, fz0.w, fz1.x, fz1.y, fz1.z, fz1.w};
+    refs[0] = r0.x; refs[1] = r0.y; refs[2] = r0.z; refs[3] = r0.w;
+    refs[4] = r1.x; refs[5] = r1.y; refs[6] = r1.z; refs[7] = r1.w;
+    const float tcap = s.t;
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        float tnx = (nx[k] - s.o.x) * s.inv.x, tfx = (fx[k] - s.o.x) * s.inv.x;
+        float tny = (ny[k] - s.o.y) * s.inv.y, tfy = (fy[k] - s.o.y) * s.inv.y;
+        float tnz = (nz[k] - s.o.z) * s.inv.z, tfz = (fz[k] - s.o.z) * s.inv.z;
+        keys[k] = child_key(fmax3(fmaxf(tnx, s.tmin), tny, tnz), fmin3(fminf(tfx, tcap), tfy, tfz), refs[k], k);
+    }
+}
+
+// Byte j of w as the float 1 + q 2^-15: q lands in mantissa bits 8..15 of
+// 1.0f (one PRMT).  The constant offset 2^15 quanta is folded into the
+// per-node term below, where it costs 2^-9 of a quantum at most.
+__device__ __forceinline__ float qbyte(uint32_t w, int j) {
+    return __int_as_float((int)__byte_perm(w, 0x3F800000u, 0x7604u | ((uint32_t)j << 4)));
+}
+
+// Exact decode (plane = origin + q s is an exact float by construction; then
+// the FP32 node's arithmetic, so the test is at least as wide as the FP32
+// node's).  Used when the ray origin is more than 2^20 quanta from the node,
+// where the fast form could lose the quantum of slack the builder adds.
+struct Keys8 {
+    uint32_t k[8];
+};
+__device__ __noinline__ Keys8 qnode_keys_exact(const uint8_t* node, float ox, float oy, float oz, float ix, float iy,
+                                               float iz, float tmin, float tmax) {
+    const QNode* q = reinterpret_cast<const QNode*>(node);
+    const float o[3] = {ox, oy, oz}, inv[3] = {ix, iy, iz};
+    const uint8_t* qlo[3] = {q->qlo_x, q->qlo_y, q->qlo_z};
+    const uint8_t* qhi[3] = {q->qhi_x, q->qhi_y, q->qhi_z};
+    Keys8 out;
+    for (int k = 0; k < 8; k++) {
+        float tn = tmin, tf = tmax;
+        for (int a = 0; a < 3; a++) {
+            const float sc = __uint_as_float((uint32_t)q->exp[a] << 23);
+            const bool pos = inv[a] >= 0.0f;
+            float pn = fmaf((float)(pos ? qlo[a][k] : qhi[a][k]), sc, q->origin[a]);
+            float pf = fmaf((float)(pos ? qhi[a][k] : qlo[a][k]), sc, q->origin[a]);
+            tn = fmaxf(tn, (pn - o[a]) * inv[a]);
+            tf = fminf(tf, (pf - o[a]) * inv[a]);
+        }
+        out.k[k] = child_key(tn, tf, q->child_ref[k], k);
+    }
+    return out;
+}
+
+// Slab tests of a quantised node.  With A = s inv and B = (origin - o) inv
+// per axis, plane t = q A + B = (1 + q 2^-15) (2^15 A) + (B - 2^15 A): one
+// PRMT and one FMA per plane.  The near / far byte words are fetched by the
+// ray's octant (s.oct) like the FP32 node's planes.  Error of the fast form
+// against exact arithmetic: under 0.26 quanta while |B| <= 2^20 |A| (0.125
+// from B, 0.0625 each from the B - 2^15 A and final roundings), and the
+// FP32 node's own rounding adds at most 0.125 more; the builder's quantum
+// of slack covers both, so the fast test is never narrower than the FP32
+// node's and the hits are identical.
+__device__ __forceinline__ void qnode_keys(const Trav& s, uint32_t entry, uint32_t keys[8], uint32_t refs[8]) {
+    const uint8_t* node = reinterpret_cast<const uint8_t*>(s.nodes) + (size_t)entry * kQNodeBytes;
+    const uint4* qp = reinterpret_cast<const uint4*>(node);
+    const uint2* q2 = reinterpret_cast<const uint2*>(node);
+    uint4 h = __ldg(qp), r0 = __ldg(qp + 1), r1 = __ldg(qp + 2);
+    // uint2 index of the near-plane words: qlo at 6 + 2a, qhi at 7 + 2a
+    const uint32_t ix = 6u + ((s.oct & 0xFFu) >> 1), iy = 6u + (((s.oct >> 8) & 0xFFu) >> 1),
+                   iz = 6u + ((s.oct >> 16) >> 1);
+    uint2 nx = __ldg(q2 + ix), fx = __ldg(q2 + (ix ^ 1u));
+    uint2 ny = __ldg(q2 + iy), fy = __ldg(q2 + (iy ^ 1u));
+    uint2 nz = __ldg(q2 + iz), fz = __ldg(q2 + (iz ^ 1u));
+    refs[0] = r0.x; refs[1] = r0.y; refs[2] = r0.z; refs[3] = r0.w;
+    refs[4] = r1.x; refs[5] = r1.y; refs[6] = r1.z; refs[7] = r1.w;
+    const float Ax = __uint_as_float((h.w & 0xFFu) << 23) * s.inv.x;
+    const float Ay = __uint_as_float(((h.w >> 8) & 0xFFu) << 23) * s.inv.y;
+    const float Az = __uint_as_float(((h.w >> 16) & 0xFFu) << 23) * s.inv.z;
+    const float Bx = (__uint_as_float(h.x) - s.o.x) * s.inv.x;
+    const float By = (__uint_as_float(h.y) - s.o.y) * s.inv.y;
+    const float Bz = (__uint_as_float(h.z) - s.o.z) * s.inv.z;
+    const float lim = 1048576.0f, amin = 7.88860905e-31f;  // 2^20 quanta; 2^-100
+    const float ax = fabsf(Ax), ay = fabsf(Ay), az = fabsf(Az);
+    if (!(fabsf(Bx) <= lim * ax && fabsf(By) <= lim * ay && fabsf(Bz) <= lim * az && fmin3(ax, ay, az) >= amin)) {
+        Keys8 kk = qnode_keys_exact(node, s.o.x, s.o.y, s.o.z, s.inv.x, s.inv.y, s.inv.z, s.tmin, s.t);
+#pragma unroll
+        for (int k = 0; k < 8; k++) keys[k] = kk.k[k];
+        return;
+    }
+    const float Sx = Ax * 32768.0f, Sy = Ay * 32768.0f, Sz = Az * 32768.0f;
+    const float Cx = fmaf(-32768.0f, Ax, Bx), Cy = fmaf(-32768.0f, Ay, By), Cz = fmaf(-32768.0f, Az, Bz);
+    const float tcap = s.t;
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        const int j = k & 3;
+        const uint32_t wnx = k < 4 ? nx.x : nx.y, wfx = k < 4 ? fx.x : fx.y;
+        const uint32_t wny = k < 4 ? ny.x : ny.y, wfy = k < 4 ? fy.x : fy.y;
+        const uint32_t wnz = k < 4 ? nz.x : nz.y, wfz = k < 4 ? fz.x : fz.y;
+        float tnx = fmaf(qbyte(wnx, j), Sx, Cx), tfx = fmaf(qbyte(wfx, j), Sx, Cx);
+        float tny = fmaf(qbyte(wny, j), Sy, Cy), tfy = fmaf(qbyte(wfy, j), Sy, Cy);
+        float tnz = fmaf(qbyte(wnz, j), Sz, Cz), tfz = fmaf(qbyte(wfz, j), Sz, Cz);
+        keys[k] = child_key(fmax3(fmaxf(tnx, s.tmin), tny, tnz), fmin3(fminf(tfx, tcap), tfy, tfz), refs[k], k);
+    }
 }
 
 // (inst, geom, prim) below the best hit's, comparing caller instance indices
@@ -210,7 +339,11 @@ __device__ __noinline__ bool ids_below_best(const InstRecord* insts, uint32_t c_
 
 // One traversal step.  Returns true when the ray is finished (s.t/hit_* hold
 // the result; with terminate-on-first-hit, any accepted hit finishes it).
-template <bool STATS>
+// KINDS (kBlasKind* bits) are the BLAS node formats this instantiation
+// decodes: a loop for FP32-only or quantised-only scenes carries no code for
+// the other format, so neither pays the other's registers.  An instance of a
+// format outside KINDS is reported (RT_ERR_BAD_AS) and skipped.
+template <bool STATS, uint32_t KINDS>
 __device__ __forceinline__ bool trav_step(Trav& s, uint2* stack, const Env& e, uint32_t ray_flags, uint32_t cull_mask,
                                           uint32_t ray_sbt_offset, Counters& cnt) {
     const uint32_t entry = s.entry;
@@ -226,39 +359,12 @@ __device__ __forceinline__ bool trav_step(Trav& s, uint2* stack, const Env& e, u
             atomicOr(e.status, 1u << RT_ERR_BAD_AS);  // malformed reference: skip it
         } else {
             if (STATS) cnt.nodes++;
-            // Near / far planes were chosen per ray by the direction signs
-            // (s.oct): the loads fetch them directly, so each child needs
-            // one subtract and one multiply per plane and no per-axis min/max.
-            const float4* np = reinterpret_cast<const float4*>(s.nodes + entry);
-            const uint32_t ox = s.oct & 0xFFu, oy = (s.oct >> 8) & 0xFFu, oz = s.oct >> 16;
-            float4 nx0 = __ldg(np + ox), nx1 = __ldg(np + ox + 1), fx0 = __ldg(np + (ox ^ 2u)),
-                   fx1 = __ldg(np + (ox ^ 2u) + 1);
-            float4 ny0 = __ldg(np + oy), ny1 = __ldg(np + oy + 1), fy0 = __ldg(np + (oy ^ 2u)),
-                   fy1 = __ldg(np + (oy ^ 2u) + 1);
-            float4 nz0 = __ldg(np + oz), nz1 = __ldg(np + oz + 1), fz0 = __ldg(np + (oz ^ 2u)),
-                   fz1 = __ldg(np + (oz ^ 2u) + 1);
-            uint4 r0 = __ldg(reinterpret_cast<const uint4*>(np + 12));
-            uint4 r1 = __ldg(reinterpret_cast<const uint4*>(np + 13));
-            const float nx[8] = {nx0.x, nx0.y, nx0.z, nx0.w, nx1.x, nx1.y, nx1.z, nx1.w};
-            const float fx[8] = {fx0.x, fx0.y, fx0.z, fx0.w, fx1.x, fx1.y, fx1.z, fx1.w};
-            const float ny[8] = {ny0.x, ny0.y, ny0.z, ny0.w, ny1.x, ny1.y, ny1.z, ny1.w};
-            const float fy[8] = {fy0.x, fy0.y, fy0.z, fy0.w, fy1.x, fy1.y, fy1.z, fy1.w};
-            const float nz[8] = {nz0.x, nz0.y, nz0.z, nz0.w, nz1.x, nz1.y, nz1.z, nz1.w};
-            const float fz[8] = {fz0.x, fz0.y, fz0.z, fz0.w, fz1.x, fz1.y, fz1.z, fz1.w};
-            const uint32_t refs[8] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w};
-            const float tcap = s.t;
-            uint32_t keys[8];
-#pragma unroll
-            for (int k = 0; k < 8; k++) {
-                float tnx = (nx[k] - s.o.x) * s.inv.x, tfx = (fx[k] - s.o.x) * s.inv.x;
-                float tny = (ny[k] - s.o.y) * s.inv.y, tfy = (fy[k] - s.o.y) * s.inv.y;
-                float tnz = (nz[k] - s.o.z) * s.inv.z, tfz = (fz[k] - s.o.z) * s.inv.z;
-                float tn = fmax3(fmaxf(tnx, s.tmin), tny, tnz);
-                float tf = fmin3(fminf(tfx, tcap), tfy, tfz);
-                bool hit = (refs[k] != kChildEmpty) && (tn <= tf * kBoxFarScale);
-                // key: tnear bits rounded down to 8 ulps | slot (ascending = near first)
-                keys[k] = hit ? ((__float_as_uint(fmaxf(tn, 0.0f)) & ~7u) | (uint32_t)k) : 0xFFFFFFFFu;
-            }
+            uint32_t keys[8], refs[8];
+            // TLAS nodes are always FP32
+            if ((KINDS & kBlasKindQ8) && s.in_blas && (KINDS == kBlasKindQ8 || s.quant))
+                qnode_keys(s, entry, keys, refs);
+            else
+                fnode_keys(s, entry, keys, refs);
             sort8(keys);
             if (keys[0] != 0xFFFFFFFFu) {
                 // push the other hit children farthest first; the nearest is
@@ -286,7 +392,12 @@ __device__ __forceinline__ bool trav_step(Trav& s, uint2* stack, const Env& e, u
             const uint4* tail = reinterpret_cast<const uint4*>(&ir->blas);
             uint4 q0 = __ldg(tail), q1 = __ldg(tail + 1);
             // q0 = blas lo, blas hi, instance_id, custom_mask; q1 = sbt_flags, tri_count, node_count, prims_off256
-            if (q1.y != 0u && ((q0.w >> 24) & cull_mask) != 0u) {
+            bool enter = q1.y != 0u && ((q0.w >> 24) & cull_mask) != 0u;
+            if (enter && (blas_kind(q1.z) & KINDS) == 0u) {
+                atomicOr(e.status, 1u << RT_ERR_BAD_AS);  // the TLAS header does not list this format
+                enter = false;
+            }
+            if (enter) {
                 if (STATS) cnt.insts++;
                 const float4* wp = reinterpret_cast<const float4*>(ir->w2o);
                 float4 w0 = __ldg(wp), w1 = __ldg(wp + 1), w2 = __ldg(wp + 2);
@@ -299,7 +410,8 @@ __device__ __forceinline__ bool trav_step(Trav& s, uint2* stack, const Env& e, u
                 const uint8_t* blas = reinterpret_cast<const uint8_t*>(((uint64_t)q0.y << 32) | q0.x);
                 s.nodes = reinterpret_cast<const WideNode*>(blas + kHeaderBytes);
                 s.tris = reinterpret_cast<const TriRecord*>(blas + (uint64_t)q1.w * 256u);
-                s.node_count = q1.z;
+                s.node_count = q1.z & ~kQuantizedBlasBit;
+                s.quant = (q1.z & kQuantizedBlasBit) != 0u;
                 s.tri_count = q1.y;
                 s.c_inst = first;
                 s.c_sbt_flags = q1.x;
@@ -447,11 +559,10 @@ __global__ void k_raygen(const __grid_constant__ WfParams P) {
     if (i == 0) P.B.ctr->ray_count[0] = P.total;
 }
 
-// Persistent trace kernel with per-lane ray replacement.
-template <int MODE, bool STATS>
-__global__ void __launch_bounds__(kTraceThreads, RT_TRACE_MIN_BLOCKS) k_trace(const __grid_constant__ WfParams P) {
+// Persistent trace loop with per-lane ray replacement.
+template <int MODE, bool STATS, uint32_t KINDS>
+__device__ __forceinline__ void trace_wavefront(const WfParams& P, const Env& e) {
     const TraceLaunch& L = P.L;
-    const Env e = make_env(L.push.acceleration_structure, L.push, &L.sbt, L.textures, L.status);
     const RtUniforms& U = *reinterpret_cast<const RtUniforms*>(L.push.uniforms);
     const uint32_t b = P.bounce;
     const uint32_t nshadow = L.desc.shadow_ray_count;
@@ -500,7 +611,7 @@ __global__ void __launch_bounds__(kTraceThreads, RT_TRACE_MIN_BLOCKS) k_trace(co
             }
             if (heat) t0 = clock64();
         }
-        if (!trav_step<STATS>(s, stack, e, ray_flags, 0xFFu, sbt_offset, cnt)) continue;
+        if (!trav_step<STATS, KINDS>(s, stack, e, ray_flags, 0xFFu, sbt_offset, cnt)) continue;
         // the ray is finished
         if (MODE == kModeBounce) {
             P.B.hits[2 * (size_t)item] = make_uint4(__float_as_uint(s.t), __float_as_uint(s.u), __float_as_uint(s.v),
@@ -513,6 +624,22 @@ __global__ void __launch_bounds__(kTraceThreads, RT_TRACE_MIN_BLOCKS) k_trace(co
         item = kNoItem;
     }
     flush_counters(L.stats, cnt);
+}
+
+// One traversal kernel per BLAS node-format set KINDS, each with its own
+// register allocation (one kernel holding all three loops spills far more).
+// The host launches the variant for the formats this process has built; when
+// it has built both, it launches all three and each runs only if the TLAS
+// header names exactly its set.
+__device__ __forceinline__ bool kinds_selected(uint32_t kinds_built, uint32_t tlas_kinds, uint32_t kinds) {
+    if (kinds_built != (kBlasKindF32 | kBlasKindQ8)) return true;  // the only launch
+    return (tlas_kinds ? tlas_kinds : kBlasKindF32) == kinds;
+}
+
+template <int MODE, bool STATS, uint32_t KINDS>
+__global__ void __launch_bounds__(kTraceThreads, RT_TRACE_MIN_BLOCKS) k_trace(const __grid_constant__ WfParams P) {
+    const Env e = make_env(P.L.push.acceleration_structure, P.L.push, &P.L.sbt, P.L.textures, P.L.status);
+    if (kinds_selected(P.L.kinds_built, e.blas_kinds, KINDS)) trace_wavefront<MODE, STATS, KINDS>(P, e);
 }
 
 // The closest-hit and miss programs for every ray of bounce b.
@@ -646,11 +773,9 @@ struct RayBufferParams {
     RayBufferLaunch L;
 };
 
-template <bool STATS>
-__global__ void __launch_bounds__(kTraceThreads, RT_TRACE_MIN_BLOCKS)
-    k_trace_ray_buffer(const __grid_constant__ RayBufferParams P) {
+template <bool STATS, uint32_t KINDS>
+__device__ __forceinline__ void trace_ray_buffer(const RayBufferParams& P, const Env& e) {
     const RayBufferLaunch& L = P.L;
-    const Env e = make_env(L.tlas, L.push, &L.sbt, L.textures, L.status);
     Counters cnt = {0, 0, 0, 0, 0, 0};
     uint2 stack[kStackSize];
     Trav s;
@@ -665,7 +790,7 @@ __global__ void __launch_bounds__(kTraceThreads, RT_TRACE_MIN_BLOCKS)
             trav_begin(s, e, mk3(a.x, a.y, a.z), mk3(c.x, c.y, c.z), a.w, c.w);
             cnt.primary++;
         }
-        if (!trav_step<STATS>(s, stack, e, L.ray_flags, L.cull_mask, L.sbt_offset, cnt)) continue;
+        if (!trav_step<STATS, KINDS>(s, stack, e, L.ray_flags, L.cull_mask, L.sbt_offset, cnt)) continue;
         RtHit o;
         if (s.hit_inst != kNoHit) {
             const InstRecord* ir = &e.insts[s.hit_inst];
@@ -690,6 +815,13 @@ __global__ void __launch_bounds__(kTraceThreads, RT_TRACE_MIN_BLOCKS)
         item = kNoItem;
     }
     flush_counters(L.stats, cnt);
+}
+
+template <bool STATS, uint32_t KINDS>
+__global__ void __launch_bounds__(kTraceThreads, RT_TRACE_MIN_BLOCKS)
+    k_trace_ray_buffer(const __grid_constant__ RayBufferParams P) {
+    const Env e = make_env(P.L.tlas, P.L.push, &P.L.sbt, P.L.textures, P.L.status);
+    if (kinds_selected(P.L.kinds_built, e.blas_kinds, KINDS)) trace_ray_buffer<STATS, KINDS>(P, e);
 }
 
 __global__ void k_debug_eval(uint32_t fn, const float* in, float* out, uint32_t count) {
@@ -754,17 +886,45 @@ int persistent_blocks(K kernel, int threads, int num_sms) {
     return per_sm * num_sms;
 }
 
+// Calls f(std::integral_constant<uint32_t, KINDS>) for each traversal
+// variant to launch, given the BLAS formats built so far (kinds_selected).
+template <class F>
+void for_each_variant(uint32_t kinds_built, F&& f) {
+    using F32 = std::integral_constant<uint32_t, kBlasKindF32>;
+    using Q8 = std::integral_constant<uint32_t, kBlasKindQ8>;
+    using Both = std::integral_constant<uint32_t, kBlasKindF32 | kBlasKindQ8>;
+    if (kinds_built == (kBlasKindF32 | kBlasKindQ8)) {
+        f(F32{});
+        f(Q8{});
+        f(Both{});
+    } else if (kinds_built == kBlasKindQ8) {
+        f(Q8{});
+    } else {
+        f(F32{});
+    }
+}
+
+template <int MODE, bool STATS, uint32_t KINDS>
+void launch_trace_kernel(const WfParams& P, int num_sms, cudaStream_t stream) {
+    static int blocks = 0;
+    if (!blocks) blocks = persistent_blocks(k_trace<MODE, STATS, KINDS>, kTraceThreads, num_sms);
+    note_launch(), k_trace<MODE, STATS, KINDS><<<blocks, kTraceThreads, 0, stream>>>(P);
+}
+
 template <int MODE>
 void launch_trace_mode(const WfParams& P, bool stats, int num_sms, cudaStream_t stream) {
-    if (stats) {
-        static int blocks = 0;
-        if (!blocks) blocks = persistent_blocks(k_trace<MODE, true>, kTraceThreads, num_sms);
-        note_launch(), k_trace<MODE, true><<<blocks, kTraceThreads, 0, stream>>>(P);
-    } else {
-        static int blocks = 0;
-        if (!blocks) blocks = persistent_blocks(k_trace<MODE, false>, kTraceThreads, num_sms);
-        note_launch(), k_trace<MODE, false><<<blocks, kTraceThreads, 0, stream>>>(P);
-    }
+    for_each_variant(P.L.kinds_built, [&](auto k) {
+        constexpr uint32_t K = decltype(k)::value;
+        if (stats) launch_trace_kernel<MODE, true, K>(P, num_sms, stream);
+        else launch_trace_kernel<MODE, false, K>(P, num_sms, stream);
+    });
+}
+
+template <bool STATS, uint32_t KINDS>
+void launch_ray_buffer_kernel(const RayBufferParams& P, int num_sms, cudaStream_t stream) {
+    static int blocks = 0;
+    if (!blocks) blocks = persistent_blocks(k_trace_ray_buffer<STATS, KINDS>, kTraceThreads, num_sms);
+    note_launch(), k_trace_ray_buffer<STATS, KINDS><<<blocks, kTraceThreads, 0, stream>>>(P);
 }
 
 }  // namespace
@@ -854,15 +1014,11 @@ cudaError_t launch_trace_ray_buffer(const RayBufferLaunch& p, int num_sms, cudaS
     if (p.count == 0) return cudaSuccess;
     cudaError_t err = cudaMemsetAsync(p.work, 0, sizeof(uint32_t), stream);
     if (err != cudaSuccess) return err;
-    if (p.collect_stats) {
-        static int blocks = 0;
-        if (!blocks) blocks = persistent_blocks(k_trace_ray_buffer<true>, kTraceThreads, num_sms);
-        note_launch(), k_trace_ray_buffer<true><<<blocks, kTraceThreads, 0, stream>>>(P);
-    } else {
-        static int blocks = 0;
-        if (!blocks) blocks = persistent_blocks(k_trace_ray_buffer<false>, kTraceThreads, num_sms);
-        note_launch(), k_trace_ray_buffer<false><<<blocks, kTraceThreads, 0, stream>>>(P);
-    }
+    for_each_variant(p.kinds_built, [&](auto k) {
+        constexpr uint32_t K = decltype(k)::value;
+        if (p.collect_stats) launch_ray_buffer_kernel<true, K>(P, num_sms, stream);
+        else launch_ray_buffer_kernel<false, K>(P, num_sms, stream);
+    });
     return cudaGetLastError();
 }
 

@@ -256,11 +256,13 @@ class GpuScene:
     the ModelInfo array, textures, the instance buffer and its TLAS."""
 
     def __init__(self, device: Device, scene: Scene, scratch: ScratchBuffer | None = None,
-                 tlas_flags: int = abi.RT_BUILD_PREFER_FAST_TRACE | abi.RT_BUILD_ALLOW_UPDATE, stream=None):
+                 tlas_flags: int = abi.RT_BUILD_PREFER_FAST_TRACE | abi.RT_BUILD_ALLOW_UPDATE, stream=None,
+                 blas_flags: int = abi.RT_BUILD_PREFER_FAST_TRACE):
         self.device = device
         self.scene = scene
         self.scratch = scratch or ScratchBuffer("scene scratch")
-        self.models = [GpuModel(device, m, self.scratch, i, stream=stream) for i, m in enumerate(scene.models)]
+        self.models = [GpuModel(device, m, self.scratch, i, build_flags=blas_flags, stream=stream)
+                       for i, m in enumerate(scene.models)]
         infos = np.array([m.model_info() for m in self.models], abi.MODEL_INFO_DTYPE)
         self.model_info_buffer = Device.upload(infos)
         ImageManager(device).push_images(scene.textures)
@@ -322,9 +324,10 @@ class PerFrameResources:
                                                             Device.stream_handle(stream)))
 
 
-def render(device: Device, scene: Scene, radiance: bool = True, flags: int = 0):
-    """Builds a scene, renders one frame and returns (image, radiance, stats)."""
-    gs = GpuScene(device, scene)
+def render(device: Device, scene: Scene, radiance: bool = True, flags: int = 0, gpu_scene: GpuScene | None = None):
+    """Builds a scene (unless `gpu_scene` is given), renders one frame and
+    returns (image, radiance, stats)."""
+    gs = gpu_scene or GpuScene(device, scene)
     fr = PerFrameResources(device, gs, scene.width, scene.height, radiance=radiance)
     fr.write_uniforms(scene.uniforms)
     device.read_stats(reset=True)
