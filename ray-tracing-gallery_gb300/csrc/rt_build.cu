@@ -778,9 +778,11 @@ __global__ void k_quantize_nodes(const WideNode* in, const uint32_t* node_count,
         q.exp[a] = (uint8_t)e;
         for (int k = 0; k < 8; k++) {
             if (!valid[k]) { qlo[a][k] = 255u; qhi[a][k] = 0u; continue; }
-            // outward rounding plus one quantum of slack on each side
-            float ql = floorf(__fsub_rd(lo[a][k], origin) / s) - 1.0f;
-            float qh = ceilf(__fsub_ru(hi[a][k], origin) / s) + 1.0f;
+            // outward to the grid with at least kQuantSlack of a quantum to
+            // spare on each side (origin + ql s <= lo - slack s); the
+            // division by the power of two s is exact
+            float ql = floorf(__fsub_rd(__fsub_rd(lo[a][k], origin) / s, kQuantSlack));
+            float qh = ceilf(__fadd_ru(__fsub_ru(hi[a][k], origin) / s, kQuantSlack));
             qlo[a][k] = (uint8_t)fminf(fmaxf(ql, 0.0f), 255.0f);
             qhi[a][k] = (uint8_t)fminf(fmaxf(qh, 0.0f), 255.0f);
         }

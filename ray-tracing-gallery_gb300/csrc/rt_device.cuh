@@ -78,10 +78,15 @@ __host__ __device__ inline uint32_t node_meta(uint32_t m0, uint32_t m1, int c) {
 // BLAS only), 96 bytes.  Per axis a: quantum s_a = 2^(exp[a] - 127); child
 // k's planes are origin_a + q * s_a with q = qlo / qhi bytes.  The builder
 // puts origin on the quantum grid one quantum below the node's union box and
-// rounds every child plane outward plus one more quantum, so the decoded box
-// contains the FP32 child box with at least one quantum to spare; an empty
-// child is qlo = 255, qhi = 0 (never hit).  child_ref is as in WideNode.
+// rounds every child plane outward to the grid with at least kQuantSlack of
+// a quantum to spare, so the decoded box contains the FP32 child box with
+// that margin (the traversal's fast decode and the FP32 node test together
+// err by under 0.2 of a quantum while the ray origin is within 2^19 quanta
+// of the node); an empty child is qlo = 255, qhi = 0 (never hit).
+// child_ref is as in WideNode.
 constexpr uint32_t kQNodeBytes = 96;
+constexpr float kQuantSlack = 0.25f;
+constexpr float kQuantFastLimit = 524288.0f;  // 2^19 quanta
 struct alignas(16) QNode {
     float origin[3];
     uint8_t exp[3];

@@ -55,6 +55,16 @@ constexpr int kMaxDepth = 64;
 #ifndef RT_TRACE_MIN_BLOCKS
 #define RT_TRACE_MIN_BLOCKS 6
 #endif
+// Warp phase scheduling.  Each iteration of the traversal loop runs either
+// node steps (lanes whose next entry is an internal node) or the other steps
+// (leaves, instance entries, TLAS returns), so a warp never pays for both
+// branch bodies in one iteration.  Lanes wait for their phase: the warp
+// switches to the leaf phase once RT_TRACE_LEAF_WAIT/32 of its active lanes
+// wait on one (or no lane has a node).  -1 = no phases: every lane takes its
+// own step each iteration.
+#ifndef RT_TRACE_LEAF_WAIT
+#define RT_TRACE_LEAF_WAIT 20
+#endif
 
 constexpr int kModeBounce = 0;   // closest hit of a bounce list -> hit records
 constexpr int kModeShadow = 1;   // any hit of generated shadow rays -> lit counters
@@ -248,8 +258,8 @@ __device__ __forceinline__ float qbyte(uint32_t w, int j) {
 
 // Exact decode (plane = origin + q s is an exact float by construction; then
 // the FP32 node's arithmetic, so the test is at least as wide as the FP32
-// node's).  Used when the ray origin is more than 2^20 quanta from the node,
-// where the fast form could lose the quantum of slack the builder adds.
+// node's).  Used when the ray origin is more than 2^19 quanta from the node,
+// where the fast form could lose the slack the builder adds.
 struct Keys8 {
     uint32_t k[8];
 };
@@ -279,11 +289,12 @@ __device__ __noinline__ Keys8 qnode_keys_exact(const uint8_t* node, float ox, fl
 // per axis, plane t = q A + B = (1 + q 2^-15) (2^15 A) + (B - 2^15 A): one
 // PRMT and one FMA per plane.  The near / far byte words are fetched by the
 // ray's octant (s.oct) like the FP32 node's planes.  Error of the fast form
-// against exact arithmetic: under 0.26 quanta while |B| <= 2^20 |A| (0.125
-// from B, 0.0625 each from the B - 2^15 A and final roundings), and the
-// FP32 node's own rounding adds at most 0.125 more; the builder's quantum
-// of slack covers both, so the fast test is never narrower than the FP32
-// node's and the hits are identical.
+// against exact arithmetic, in quanta, while |B| <= 2^19 |A|: 2^19 2^-23
+// from the two roundings of B, (2^19 + 2^15) 2^-24 from B - 2^15 A, about
+// 2^19 2^-24 from the final FMA and 255 2^-24 from A: under 0.128.  The
+// FP32 node test of the same plane errs by at most (2^19 + 256) 2^-23, under
+// 0.063.  The builder's slack (kQuantSlack = 0.25) covers both, so the fast
+// test is never narrower than the FP32 node's and the hits are identical.
 __device__ __forceinline__ void qnode_keys(const Trav& s, uint32_t entry, uint32_t keys[8], uint32_t refs[8]) {
     const uint8_t* node = reinterpret_cast<const uint8_t*>(s.nodes) + (size_t)entry * kQNodeBytes;
     const uint4* qp = reinterpret_cast<const uint4*>(node);
@@ -303,7 +314,7 @@ __device__ __forceinline__ void qnode_keys(const Trav& s, uint32_t entry, uint32
     const float Bx = (__uint_as_float(h.x) - s.o.x) * s.inv.x;
     const float By = (__uint_as_float(h.y) - s.o.y) * s.inv.y;
     const float Bz = (__uint_as_float(h.z) - s.o.z) * s.inv.z;
-    const float lim = 1048576.0f, amin = 7.88860905e-31f;  // 2^20 quanta; 2^-100
+    const float lim = kQuantFastLimit, amin = 7.88860905e-31f;  // 2^-100
     const float ax = fabsf(Ax), ay = fabsf(Ay), az = fabsf(Az);
     if (!(fabsf(Bx) <= lim * ax && fabsf(By) <= lim * ay && fabsf(Bz) <= lim * az && fmin3(ax, ay, az) >= amin)) {
         Keys8 kk = qnode_keys_exact(node, s.o.x, s.o.y, s.o.z, s.inv.x, s.inv.y, s.inv.z, s.tmin, s.t);
@@ -343,11 +354,26 @@ __device__ __noinline__ bool ids_below_best(const InstRecord* insts, uint32_t c_
 // decodes: a loop for FP32-only or quantised-only scenes carries no code for
 // the other format, so neither pays the other's registers.  An instance of a
 // format outside KINDS is reported (RT_ERR_BAD_AS) and skipped.
+__device__ __forceinline__ bool is_node_entry(uint32_t entry) {
+    return entry != kMarker && (entry & kLeafEntry) == 0u;  // kNoEntry has the leaf bit
+}
+
+// The phase of this iteration for the calling (converged) lanes.
+__device__ __forceinline__ bool node_phase(uint32_t entry) {
+    const unsigned act = __activemask();
+    const unsigned nm = __ballot_sync(act, is_node_entry(entry));
+    if (nm == 0u) return false;
+    if (nm == act) return true;
+    return (uint32_t)__popc(act & ~nm) * 32u < (uint32_t)RT_TRACE_LEAF_WAIT * (uint32_t)__popc(act);
+}
+
+// `phase`: 1 = node steps only, 0 = non-node steps only, -1 = any step.
 template <bool STATS, uint32_t KINDS>
 __device__ __forceinline__ bool trav_step(Trav& s, uint2* stack, const Env& e, uint32_t ray_flags, uint32_t cull_mask,
-                                          uint32_t ray_sbt_offset, Counters& cnt) {
+                                          uint32_t ray_sbt_offset, Counters& cnt, int phase) {
     const uint32_t entry = s.entry;
     if (entry == kNoEntry) return true;
+    if (phase >= 0 && is_node_entry(entry) != (phase == 1)) return false;  // waits for its phase
     if (++s.steps > kMaxTraversalSteps) {
         atomicOr(e.status, 1u << RT_ERR_TIMEOUT);
         return true;
@@ -611,7 +637,12 @@ __device__ __forceinline__ void trace_wavefront(const WfParams& P, const Env& e)
             }
             if (heat) t0 = clock64();
         }
-        if (!trav_step<STATS, KINDS>(s, stack, e, ray_flags, 0xFFu, sbt_offset, cnt)) continue;
+#if RT_TRACE_LEAF_WAIT < 0
+        const int phase = -1;
+#else
+        const int phase = node_phase(s.entry) ? 1 : 0;
+#endif
+        if (!trav_step<STATS, KINDS>(s, stack, e, ray_flags, 0xFFu, sbt_offset, cnt, phase)) continue;
         // the ray is finished
         if (MODE == kModeBounce) {
             P.B.hits[2 * (size_t)item] = make_uint4(__float_as_uint(s.t), __float_as_uint(s.u), __float_as_uint(s.v),
@@ -790,7 +821,12 @@ __device__ __forceinline__ void trace_ray_buffer(const RayBufferParams& P, const
             trav_begin(s, e, mk3(a.x, a.y, a.z), mk3(c.x, c.y, c.z), a.w, c.w);
             cnt.primary++;
         }
-        if (!trav_step<STATS, KINDS>(s, stack, e, L.ray_flags, L.cull_mask, L.sbt_offset, cnt)) continue;
+#if RT_TRACE_LEAF_WAIT < 0
+        const int phase = -1;
+#else
+        const int phase = node_phase(s.entry) ? 1 : 0;
+#endif
+        if (!trav_step<STATS, KINDS>(s, stack, e, L.ray_flags, L.cull_mask, L.sbt_offset, cnt, phase)) continue;
         RtHit o;
         if (s.hit_inst != kNoHit) {
             const InstRecord* ir = &e.insts[s.hit_inst];

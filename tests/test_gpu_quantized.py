@@ -1,10 +1,10 @@
 """BLASes built with RT_BUILD_QUANTIZED_NODES (8-bit child boxes).
 
 A quantised node stores each child box as bytes on a per-node power-of-two
-grid, rounded outwards with one grid step to spare, so the boxes only grow:
-traversal may visit more nodes, never fewer, and the closest hit is decided by
-the same watertight triangle test and the same (t, instance, geometry,
-primitive) order.  Every hit must therefore be bit-identical to the FP32-node
+grid, rounded outwards with a quarter grid step to spare, so the boxes only
+grow: traversal may visit more nodes, never fewer, and the closest hit is
+decided by the same watertight triangle test and the same (t, instance,
+geometry, primitive) order.  Every hit must therefore be bit-identical to the FP32-node
 build and to the oracle.  Rays from far away take the exact plane decode
 instead of the fast one; both are covered.
 """
@@ -33,7 +33,7 @@ def _same(g, o, what):
 
 def _aimed_rays(count, seed, distance, radius):
     """Origins on a sphere of `distance`, aimed at points within `radius` of
-    the centre (the exact-decode case once distance / grid step > 2^20)."""
+    the centre (the exact-decode case once distance / grid step > 2^19)."""
     rng = scenes.Pcg32(seed, 0x51)
     u = rng.uniform_array(count * 6).reshape(count, 6)
     def on_sphere(a, b):
@@ -100,7 +100,7 @@ def test_quantized_render_matches_oracle(device):
 @pytest.mark.parametrize("distance", [30.0, 3.0e5])
 def test_quantized_mesh_near_and_far_rays(device, distance):
     """655,360 triangles; rays from 30 units use the fast plane decode, rays
-    from 3e5 units the exact one (the origin is over 2^20 grid steps away)."""
+    from 3e5 units the exact one (the origin is over 2^19 grid steps away)."""
     host = _host()
     sc = scenes.single_mesh_scene(scenes.precision_mesh(level=7))
     gq = host.GpuScene(device, sc, blas_flags=Q)
