@@ -391,6 +391,32 @@ RTCORE_API uint64_t rt_get_acceleration_structure_device_address(uint64_t as_mem
 RTCORE_API int32_t rt_cmd_trace_rays(rt_ctx* ctx, const RtPushConstantBufferAddresses* push,
                                      const RtShaderBindingTable* sbt, const RtTraceRaysDesc* desc,
                                      void* stream);
+
+/* One scene of rt_cmd_trace_rays_batched: the arguments of one
+ * rt_cmd_trace_rays call, plus the scene's own bindless texture table. */
+typedef struct RtBatchScene {
+    RtPushConstantBufferAddresses push;  /* model_info, uniforms, acceleration_structure */
+    uint32_t texture_count;              /* entries at texture_table (1..RT_MAX_BOUND_IMAGES) */
+    uint32_t _padding;
+    uint64_t texture_table;              /* device RtTextureDesc[texture_count]; 0 = the context's table */
+    RtTraceRaysDesc desc;                /* size, depth, shadow rays, outputs; desc.flags: LAMBERT only */
+} RtBatchScene;
+#define RT_MAX_BATCH_SCENES 65536u
+/* Many scenes (each its own TLAS, uniforms, textures, size, depth and shadow
+ * count) rendered by one set of persistent launches: the primary, shadow and
+ * reflection wavefronts of all scenes share each traversal launch, so a batch
+ * of small frames fills the GPU that one small frame cannot.  Every scene's
+ * image is identical to what rt_cmd_trace_rays gives for it alone.  No
+ * counterpart in the reference, which records one vkCmdTraceRaysKHR per
+ * frame (src/command_buffer_recording.rs:116-126).  `flags`:
+ * RT_TRACE_FLAG_COLLECT_STATS / RT_TRACE_FLAG_KERNEL_TIMINGS.  The launch
+ * sequence is fixed by the scenes' sizes alone (ray counts stay on the
+ * device), so it can be captured into a CUDA graph and replayed; trace the
+ * same sizes once outside the capture first, since the per-stream workspace
+ * cannot grow inside one (RT_ERR_INVALID then).  At most 2^31 ray slots and
+ * 2^31 shadow rays per batch. */
+RTCORE_API int32_t rt_cmd_trace_rays_batched(rt_ctx* ctx, const RtBatchScene* scenes, uint32_t scene_count,
+                                             const RtShaderBindingTable* sbt, uint32_t flags, void* stream);
 /* Traversal only: one traceRay per RtRay against `tlas`, writing RtHit.
  * `push` may be NULL (then any-hit programs cannot run and candidates are
  * accepted as if opaque). */
@@ -440,6 +466,8 @@ RT_STATIC_ASSERT(sizeof(RtRay) == 32, "ray is 32 bytes");
 RT_STATIC_ASSERT(sizeof(RtHit) == 32, "hit is 32 bytes");
 RT_STATIC_ASSERT(sizeof(RtShaderBindingTable) == 72, "sbt is 72 bytes");
 RT_STATIC_ASSERT(sizeof(RtTraceRaysDesc) == 40, "trace desc is 40 bytes");
+RT_STATIC_ASSERT(sizeof(RtBatchScene) == 80, "batch scene is 80 bytes");
+RT_STATIC_ASSERT(offsetof(RtBatchScene, desc) == 40, "RtBatchScene.desc @40");
 RT_STATIC_ASSERT(sizeof(RtTraceTimings) == 32, "timings are 32 bytes");
 
 #endif /* RTCORE_H */

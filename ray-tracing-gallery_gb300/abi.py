@@ -199,6 +199,19 @@ class RtTraceRaysDesc(C.Structure):
     ]
 
 
+class RtBatchScene(C.Structure):
+    _fields_ = [
+        ("push", RtPushConstantBufferAddresses),
+        ("texture_count", C.c_uint32),
+        ("_padding", C.c_uint32),
+        ("texture_table", C.c_uint64),
+        ("desc", RtTraceRaysDesc),
+    ]
+
+
+RT_MAX_BATCH_SCENES = 65536
+
+
 class RtRay(C.Structure):
     _fields_ = [("origin", C.c_float * 3), ("tmin", C.c_float), ("direction", C.c_float * 3), ("tmax", C.c_float)]
 
@@ -288,6 +301,8 @@ EXPORTED_FUNCTIONS = {
     "rt_get_acceleration_structure_device_address": (C.c_uint64, [C.c_uint64]),
     "rt_cmd_trace_rays": (C.c_int32, [C.c_void_p, C.POINTER(RtPushConstantBufferAddresses),
                                        C.POINTER(RtShaderBindingTable), C.POINTER(RtTraceRaysDesc), C.c_void_p]),
+    "rt_cmd_trace_rays_batched": (C.c_int32, [C.c_void_p, C.POINTER(RtBatchScene), C.c_uint32,
+                                               C.POINTER(RtShaderBindingTable), C.c_uint32, C.c_void_p]),
     "rt_cmd_trace_ray_buffer": (C.c_int32, [C.c_void_p, C.c_uint64, C.POINTER(RtPushConstantBufferAddresses),
                                              C.POINTER(RtShaderBindingTable), C.c_uint32, C.c_uint32, C.c_uint32,
                                              C.c_uint64, C.c_uint32, C.c_uint64, C.c_void_p]),
@@ -372,3 +387,4 @@ def check_layouts() -> None:
     assert C.sizeof(RtShaderBindingTable) == 72
     assert C.sizeof(RtTraceRaysDesc) == 40
     assert C.sizeof(RtTraceTimings) == 32
+    assert C.sizeof(RtBatchScene) == 80 and RtBatchScene.desc.offset == 40

@@ -98,10 +98,19 @@ struct rt_ctx {
 };
 
 namespace {
+bool stream_capturing(cudaStream_t s) {
+    cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+    return cudaStreamIsCapturing(s, &st) == cudaSuccess && st != cudaStreamCaptureStatusNone;
+}
+
+// Returns cudaErrorStreamCaptureUnsupported when the workspace would have to
+// grow while `s` is being captured into a CUDA graph (memory allocated in a
+// capture belongs to the graph): trace once outside the capture first.
 cudaError_t ctx_workspace(rt_ctx* c, cudaStream_t s, uint64_t need, uint8_t** out) {
     for (auto& w : c->workspaces) {
         if (w.stream != s) continue;
         if (w.size < need) {
+            if (stream_capturing(s)) return cudaErrorStreamCaptureUnsupported;
             cudaError_t e = cudaFreeAsync(w.ptr, s);
             w.ptr = nullptr;
             w.size = 0;
@@ -112,6 +121,7 @@ cudaError_t ctx_workspace(rt_ctx* c, cudaStream_t s, uint64_t need, uint8_t** ou
         *out = reinterpret_cast<uint8_t*>(w.ptr);
         return cudaSuccess;
     }
+    if (stream_capturing(s)) return cudaErrorStreamCaptureUnsupported;
     Workspace w{s, nullptr, need};
     cudaError_t e = cudaMallocAsync(&w.ptr, need, s);
     if (e != cudaSuccess) return e;
@@ -503,52 +513,115 @@ RTCORE_API uint64_t rt_get_acceleration_structure_device_address(uint64_t as_mem
 // ---------------------------------------------------------------------------
 // Dispatch
 // ---------------------------------------------------------------------------
-RTCORE_API int32_t rt_cmd_trace_rays(rt_ctx* ctx, const RtPushConstantBufferAddresses* push,
-                                     const RtShaderBindingTable* sbt, const RtTraceRaysDesc* desc, void* stream) {
-    if (!ctx || !push || !desc) return fail(RT_ERR_INVALID, "ctx, push or desc is NULL");
+}  // extern "C"
+
+namespace {
+int32_t check_scene(const RtPushConstantBufferAddresses* push, const RtTraceRaysDesc* desc, uint32_t index) {
     if (!push->uniforms || !push->acceleration_structure)
-        return fail(RT_ERR_INVALID, "push constants need uniforms and acceleration_structure");
+        return fail(RT_ERR_INVALID, "scene %u: push constants need uniforms and acceleration_structure", index);
     if (!aligned(push->acceleration_structure, RT_AS_ALIGNMENT) || !aligned(push->uniforms, 16) ||
         !aligned(push->model_info, 8))
-        return fail(RT_ERR_INVALID, "misaligned push-constant address");
-    if (desc->width == 0 || desc->height == 0) return fail(RT_ERR_INVALID, "empty launch %ux%u", desc->width, desc->height);
+        return fail(RT_ERR_INVALID, "scene %u: misaligned push-constant address", index);
+    if (desc->width == 0 || desc->height == 0)
+        return fail(RT_ERR_INVALID, "scene %u: empty launch %ux%u", index, desc->width, desc->height);
     if ((uint64_t)desc->width * desc->height > (1ull << 31))
-        return fail(RT_ERR_TOO_LARGE, "launch %ux%u too large", desc->width, desc->height);
+        return fail(RT_ERR_TOO_LARGE, "scene %u: launch %ux%u too large", index, desc->width, desc->height);
     if (desc->max_trace_depth == 0 || desc->max_trace_depth > 64)
-        return fail(RT_ERR_INVALID, "max_trace_depth %u (need 1..64)", desc->max_trace_depth);
-    if (desc->shadow_ray_count > 256) return fail(RT_ERR_INVALID, "shadow_ray_count %u > 256", desc->shadow_ray_count);
-    if (!desc->image_address && !desc->radiance_address) return fail(RT_ERR_INVALID, "no output buffer");
+        return fail(RT_ERR_INVALID, "scene %u: max_trace_depth %u (need 1..64)", index, desc->max_trace_depth);
+    if (desc->shadow_ray_count > 256)
+        return fail(RT_ERR_INVALID, "scene %u: shadow_ray_count %u > 256", index, desc->shadow_ray_count);
+    if (!desc->image_address && !desc->radiance_address) return fail(RT_ERR_INVALID, "scene %u: no output buffer", index);
     if (!aligned(desc->image_address, 4) || !aligned(desc->radiance_address, 16))
-        return fail(RT_ERR_INVALID, "misaligned output buffer");
+        return fail(RT_ERR_INVALID, "scene %u: misaligned output buffer", index);
+    return RT_OK;
+}
+
+int32_t trace_scenes(rt_ctx* ctx, const std::vector<TraceScene>& scenes, const RtShaderBindingTable* sbt,
+                     uint32_t flags, void* stream, const char* what) {
     RtShaderBindingTable table = sbt ? *sbt : reference_sbt();
     int32_t r = check_sbt(&table);
     if (r) return r;
+    uint64_t slots = 0, shadow_rays = 0;
+    for (const TraceScene& t : scenes) {
+        slots += (uint64_t)((t.desc.width + 7) / 8) * ((t.desc.height + 3) / 4) * 32;
+        shadow_rays += (uint64_t)t.desc.width * t.desc.height * t.desc.shadow_ray_count;
+    }
+    if (slots > (1ull << 31) || shadow_rays > (1ull << 31))
+        return fail(RT_ERR_TOO_LARGE, "%s: %llu ray slots / %llu shadow rays exceed 2^31", what,
+                    (unsigned long long)slots, (unsigned long long)shadow_rays);
     MaybeLock l(ctx);
-    TraceLaunch p;
-    p.push = *push;
-    p.sbt = table;
-    p.desc = *desc;
-    memcpy(p.textures, ctx->textures, sizeof p.textures);
-    p.stats = &ctx->dev->stats;
-    p.status = &ctx->dev->stats.status;
-    p.work = nullptr;
-    p.kinds_built = blas_kinds_built();
+    TraceBatch b;
+    b.scenes = scenes.data();
+    b.count = (uint32_t)scenes.size();
+    b.stats = (flags & RT_TRACE_FLAG_COLLECT_STATS) ? 1u : 0u;
+    b.sbt = table;
+    b.ctx_textures = ctx->textures;
+    b.stats_dev = &ctx->dev->stats;
+    b.status = &ctx->dev->stats.status;
+    b.kinds_built = blas_kinds_built();
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     uint8_t* ws = nullptr;
-    cudaError_t e = ctx_workspace(ctx, s, trace_workspace_bytes(desc->width, desc->height), &ws);
-    if (e != cudaSuccess) return cuda_fail(e, "rt_cmd_trace_rays (workspace)");
+    cudaError_t e = ctx_workspace(ctx, s, trace_workspace_bytes(b.scenes, b.count), &ws);
+    if (e == cudaErrorStreamCaptureUnsupported)
+        return fail(RT_ERR_INVALID, "%s: the workspace must grow, which a stream capture cannot do; "
+                    "trace the same scenes once outside the capture first", what);
+    if (e != cudaSuccess) return cuda_fail(e, what);
     KernelTimer* timer = nullptr;
-    if (desc->flags & RT_TRACE_FLAG_KERNEL_TIMINGS) {
+    if (flags & RT_TRACE_FLAG_KERNEL_TIMINGS) {
         if (!ctx->timer.created) {
             for (int i = 0; i < KernelTimer::kMax && e == cudaSuccess; i++) e = cudaEventCreate(&ctx->timer.ev[i]);
-            if (e != cudaSuccess) return cuda_fail(e, "rt_cmd_trace_rays (timing events)");
+            if (e != cudaSuccess) return cuda_fail(e, what);
             ctx->timer.created = true;
         }
         timer = &ctx->timer;
     }
-    e = launch_trace_rays(p, ws, ctx->num_sms, s, timer);
-    if (e != cudaSuccess) return cuda_fail(e, "rt_cmd_trace_rays");
+    e = launch_trace_batch(b, ws, ctx->num_sms, s, timer);
+    if (e != cudaSuccess) return cuda_fail(e, what);
     return RT_OK;
+}
+}  // namespace
+
+extern "C" {
+
+RTCORE_API int32_t rt_cmd_trace_rays(rt_ctx* ctx, const RtPushConstantBufferAddresses* push,
+                                     const RtShaderBindingTable* sbt, const RtTraceRaysDesc* desc, void* stream) {
+    if (!ctx || !push || !desc) return fail(RT_ERR_INVALID, "ctx, push or desc is NULL");
+    int32_t r = check_scene(push, desc, 0);
+    if (r) return r;
+    std::vector<TraceScene> one(1);
+    one[0].push = *push;
+    one[0].desc = *desc;
+    one[0].textures = nullptr;
+    one[0].texture_count = 0;
+    one[0]._pad = 0;
+    return trace_scenes(ctx, one, sbt, desc->flags, stream, "rt_cmd_trace_rays");
+}
+
+RTCORE_API int32_t rt_cmd_trace_rays_batched(rt_ctx* ctx, const RtBatchScene* scenes, uint32_t scene_count,
+                                             const RtShaderBindingTable* sbt, uint32_t flags, void* stream) {
+    if (!ctx || (!scenes && scene_count)) return fail(RT_ERR_INVALID, "ctx or scenes is NULL");
+    if (scene_count == 0) return RT_OK;
+    if (scene_count > RT_MAX_BATCH_SCENES)
+        return fail(RT_ERR_TOO_LARGE, "%u scenes > RT_MAX_BATCH_SCENES", scene_count);
+    if (flags & ~(RT_TRACE_FLAG_COLLECT_STATS | RT_TRACE_FLAG_KERNEL_TIMINGS))
+        return fail(RT_ERR_INVALID, "unknown batch flags 0x%x", flags);
+    std::vector<TraceScene> v(scene_count);
+    for (uint32_t i = 0; i < scene_count; i++) {
+        const RtBatchScene& b = scenes[i];
+        int32_t r = check_scene(&b.push, &b.desc, i);
+        if (r) return r;
+        if (b.texture_table && (b.texture_count == 0 || b.texture_count > RT_MAX_BOUND_IMAGES ||
+                                !aligned(b.texture_table, 16)))
+            return fail(RT_ERR_INVALID, "scene %u: texture table needs 1..%u entries, 16-byte aligned", i,
+                        RT_MAX_BOUND_IMAGES);
+        v[i].push = b.push;
+        v[i].desc = b.desc;
+        v[i].desc.flags &= RT_TRACE_FLAG_LAMBERT_DIFFUSE;
+        v[i].textures = reinterpret_cast<const RtTextureDesc*>(b.texture_table);
+        v[i].texture_count = b.texture_table ? b.texture_count : 0u;
+        v[i]._pad = 0;
+    }
+    return trace_scenes(ctx, v, sbt, flags, stream, "rt_cmd_trace_rays_batched");
 }
 
 RTCORE_API int32_t rt_cmd_trace_ray_buffer(rt_ctx* ctx, uint64_t tlas, const RtPushConstantBufferAddresses* push,

@@ -65,18 +65,26 @@ cudaError_t launch_tlas_update(const RtAccelerationStructureInstance* instances,
 cudaError_t launch_as_copy(const uint8_t* src, uint8_t* dst, uint64_t dst_size, uint32_t mode, cudaStream_t stream);
 
 // Trace entry points (rt_trace.cu).
-struct TraceLaunch {
+// One scene of a wavefront launch (rt_cmd_trace_rays is a batch of one).
+struct TraceScene {
     RtPushConstantBufferAddresses push;
-    RtShaderBindingTable sbt;
     RtTraceRaysDesc desc;
-    RtTextureDesc textures[RT_MAX_BOUND_IMAGES];
-    RtStats* stats;            // device
-    uint32_t* status;          // device (same block)
-    uint32_t* work;            // unused by the wavefront pipeline (kept for layout)
-    uint32_t kinds_built;      // blas_kinds_built() when the launch was recorded
+    const RtTextureDesc* textures;  // device table of texture_count; nullptr = the context's table
+    uint32_t texture_count;
+    uint32_t _pad;
 };
-// Bytes of the wavefront workspace a width x height launch needs.
-uint64_t trace_workspace_bytes(uint32_t width, uint32_t height);
+struct TraceBatch {
+    const TraceScene* scenes;       // host array
+    uint32_t count;
+    uint32_t stats;                 // collect RtStats traversal counters
+    RtShaderBindingTable sbt;
+    const RtTextureDesc* ctx_textures;  // host copy of the context's RT_MAX_BOUND_IMAGES table
+    RtStats* stats_dev;             // device
+    uint32_t* status;               // device (same block)
+    uint32_t kinds_built;           // blas_kinds_built() when the launch was recorded
+};
+// Bytes of the wavefront workspace a batch needs.
+uint64_t trace_workspace_bytes(const TraceScene* scenes, uint32_t count);
 
 // CUDA events recorded after each kernel of a trace launch
 // (RT_TRACE_FLAG_KERNEL_TIMINGS); kind[i] names the kernel that ended at ev[i].
@@ -88,8 +96,8 @@ struct KernelTimer {
     int n = 0;
     bool created = false;
 };
-cudaError_t launch_trace_rays(const TraceLaunch& p, uint8_t* workspace, int num_sms, cudaStream_t stream,
-                              KernelTimer* timer);
+cudaError_t launch_trace_batch(const TraceBatch& b, uint8_t* workspace, int num_sms, cudaStream_t stream,
+                               KernelTimer* timer);
 
 struct RayBufferLaunch {
     RtPushConstantBufferAddresses push;  // model_info may be 0

@@ -19,36 +19,35 @@ namespace {
 constexpr float kPi = 3.141592653589793f;
 constexpr uint32_t kNoHit = 0xFFFFFFFFu;
 
-// What every device program needs about the launch: the TLAS, the program
-// table, the bindless textures and the push-constant buffers.
+// What the device programs need about one scene: its TLAS, the push-constant
+// model table and its bindless textures.  A batched launch keeps one per
+// scene in device memory; the ray-buffer query holds its one in registers.
 struct Env {
     const WideNode* tnodes;
     const InstRecord* insts;
-    const RtModelInfo* models;   // may be null (no any-hit / closest-hit programs then)
-    const RtShaderBindingTable* sbt;
-    const RtTextureDesc* textures;
-    uint32_t* status;
+    const RtModelInfo* models;      // may be null (no any-hit / closest-hit programs then)
+    const RtTextureDesc* textures;  // texture_count entries
     uint32_t tnode_count;
     uint32_t inst_count;
-    uint32_t blas_kinds;         // kBlasKind* bits (which traversal loop to run)
+    uint32_t texture_count;
+    uint32_t blas_kinds;            // kBlasKind* bits of the TLAS's instances
 };
 
-__device__ __forceinline__ Env make_env(uint64_t tlas, const RtPushConstantBufferAddresses& push,
-                                        const RtShaderBindingTable* sbt, const RtTextureDesc* tex, uint32_t* status) {
+__device__ __forceinline__ Env make_env(uint64_t tlas, uint64_t model_info, const RtTextureDesc* tex,
+                                        uint32_t texture_count, uint32_t* status) {
     Env e;
     const uint8_t* base = reinterpret_cast<const uint8_t*>(tlas);
     const AsHeader* h = reinterpret_cast<const AsHeader*>(base);
-    e.tnodes = reinterpret_cast<const WideNode*>(base + h->nodes_offset);
-    e.insts = reinterpret_cast<const InstRecord*>(base + h->prims_offset);
-    bool ok = h->magic == kAsMagic && h->type == kAsTypeTop;
+    const bool ok = base != nullptr && h->magic == kAsMagic && h->type == kAsTypeTop;
+    e.tnodes = ok ? reinterpret_cast<const WideNode*>(base + h->nodes_offset) : nullptr;
+    e.insts = ok ? reinterpret_cast<const InstRecord*>(base + h->prims_offset) : nullptr;
     e.tnode_count = ok ? h->node_count : 0u;
     e.inst_count = ok ? h->prim_count : 0u;
     e.blas_kinds = ok ? h->blas_kinds : 0u;
     if (!ok) atomicOr(status, 1u << RT_ERR_BAD_AS);
-    e.models = reinterpret_cast<const RtModelInfo*>(push.model_info);
-    e.sbt = sbt;
+    e.models = reinterpret_cast<const RtModelInfo*>(model_info);
     e.textures = tex;
-    e.status = status;
+    e.texture_count = tex ? texture_count : 0u;
     return e;
 }
 
@@ -108,16 +107,18 @@ __device__ float4 tex_sample(const RtTextureDesc& t, float u, float v) {
     return texel_fetch(t, ix, iy);
 }
 
-__device__ __forceinline__ const RtHitGroup* hit_group(const Env& e, uint32_t sbt_flags, uint32_t ray_sbt_offset) {
-    if (!e.sbt) return nullptr;
+__device__ __forceinline__ const RtHitGroup* hit_group(const RtShaderBindingTable* sbt, uint32_t sbt_flags,
+                                                       uint32_t ray_sbt_offset) {
+    if (!sbt) return nullptr;
     uint32_t gi = (sbt_flags & 0xFFFFFFu) + ray_sbt_offset;
-    if (gi >= e.sbt->hit_group_count || gi >= RT_MAX_HIT_GROUPS) return nullptr;
-    return &e.sbt->hit_groups[gi];
+    if (gi >= sbt->hit_group_count || gi >= RT_MAX_HIT_GROUPS) return nullptr;
+    return &sbt->hit_groups[gi];
 }
 
 // any_hit_alpha_clip.glsl:11-29
 __device__ __noinline__ bool alpha_clip_accepts(const RtModelInfo* models, const RtTextureDesc* textures,
-                                                uint32_t custom, uint32_t geom, uint32_t prim, float u, float v) {
+                                                uint32_t texture_count, uint32_t custom, uint32_t geom, uint32_t prim,
+                                                float u, float v) {
     const RtModelInfo m = models[custom];
     const RtGeometryInfo* gis = reinterpret_cast<const RtGeometryInfo*>(m.geometry_info_address);
     const RtGeometryInfo gi = gis[geom];
@@ -128,7 +129,7 @@ __device__ __noinline__ bool alpha_clip_accepts(const RtModelInfo* models, const
     float uvx = (uvs[2 * i0] * w0 + uvs[2 * i1] * u) + uvs[2 * i2] * v;
     float uvy = (uvs[2 * i0 + 1] * w0 + uvs[2 * i1 + 1] * u) + uvs[2 * i2 + 1] * v;
     uint32_t ti = gi.images.diffuse_image_index;
-    if (ti >= RT_MAX_BOUND_IMAGES) return true;
+    if (ti >= texture_count) return true;
     float4 c = tex_sample(textures[ti], uvx, uvy);
     return !(c.w < 0.5f);
 }
@@ -259,7 +260,7 @@ __device__ __forceinline__ V3 project_onto_tangent_plane(V3 point, V3 vp, V3 vn)
 // closest_hit_textured.glsl:99-111 (nearest-sampled texel of a 64-wide tile)
 __device__ __forceinline__ float blue_noise_r(const Env& e, uint32_t tex, uint32_t x, uint32_t y, uint32_t ox,
                                               uint32_t oy) {
-    if (tex >= RT_MAX_BOUND_IMAGES) return 0.0f;
+    if (tex >= e.texture_count) return 0.0f;
     float4 c = tex_sample(e.textures[tex], (float)(x + ox) / 64.0f, (float)(y + oy) / 64.0f);
     return c.x;
 }
@@ -286,15 +287,15 @@ __device__ void shade_textured(const Env& e, const TriData& td, V3 inrm, float u
                                V3 dir, V3 sun_dir, bool lambert, float* NoL, V3* comb, V3* amb) {
     const RtGeometryInfo& gi = td.gi;
     float4 dtex = make_float4(0, 0, 0, 0), mr = make_float4(0, 0, 0, 0);
-    if (gi.images.diffuse_image_index < RT_MAX_BOUND_IMAGES)
+    if (gi.images.diffuse_image_index < e.texture_count)
         dtex = tex_sample(e.textures[gi.images.diffuse_image_index], u_, v_);
-    if (gi.images.metallic_roughness_image_index < RT_MAX_BOUND_IMAGES)
+    if (gi.images.metallic_roughness_image_index < e.texture_count)
         mr = tex_sample(e.textures[gi.images.metallic_roughness_image_index], u_, v_);
     float metallic = mr.z, roughness = mr.y;
     V3 base = mk3(dtex.x, dtex.y, dtex.z);
     V3 normal;
     int nmi = gi.images.normal_map_image_index;
-    if (nmi < 0 || (uint32_t)nmi >= RT_MAX_BOUND_IMAGES) {
+    if (nmi < 0 || (uint32_t)nmi >= e.texture_count) {
         normal = normalize3(xform_normal_w2o_t(w2o, inrm));
     } else {
         float4 nm = tex_sample(e.textures[nmi], u_, v_);

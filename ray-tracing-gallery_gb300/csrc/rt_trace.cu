@@ -24,8 +24,10 @@
 // shadow origin and append the pixel to the shadow list.  Appends are
 // warp-aggregated (one atomic per warp), which compacts the wavefronts.
 #include <algorithm>
-
+#include <cstring>
+#include <mutex>
 #include <type_traits>
+#include <vector>
 
 #include "rt_internal.h"
 #include "rt_shade.cuh"
@@ -70,8 +72,8 @@ constexpr int kModeBounce = 0;   // closest hit of a bounce list -> hit records
 constexpr int kModeShadow = 1;   // any hit of generated shadow rays -> lit counters
 constexpr int kModeRayBuf = 2;   // the API's RtRay -> RtHit query
 
+// Work counters of one lane (RT_TRACE_FLAG_COLLECT_STATS launches only).
 struct Counters {
-    uint32_t primary, secondary, shadow;
     uint32_t nodes, tris, insts;
 };
 
@@ -161,6 +163,7 @@ struct Trav {
     uint32_t node_count, tri_count;
     uint32_t c_inst, c_sbt_flags;  // the instance being traversed
     uint32_t steps;
+    uint32_t scene;            // the ray's scene in a batched launch
 };
 
 __device__ __forceinline__ void trav_begin(Trav& s, const Env& e, V3 o, V3 d, float tmin, float tmax) {
@@ -368,21 +371,48 @@ __device__ __forceinline__ bool node_phase(uint32_t entry) {
 }
 
 // `phase`: 1 = node steps only, 0 = non-node steps only, -1 = any step.
-template <bool STATS, uint32_t KINDS>
-__device__ __forceinline__ bool trav_step(Trav& s, uint2* stack, const Env& e, uint32_t ray_flags, uint32_t cull_mask,
+// One scene of a wavefront launch, in device memory (written by k_setup).
+struct alignas(128) SceneRec {
+    Env env;
+    const RtUniforms* uniforms;
+    uint32_t* image;           // RGBA8, may be null
+    float4* radiance;          // may be null
+    uint32_t width, height, max_depth, shadow_count;
+    uint32_t flags;            // RT_TRACE_FLAG_* of this scene
+    uint32_t tiles_x;          // 8x4 tiles per row
+    uint32_t tile_begin;       // first tile of the batch's tile list
+    uint32_t pixel_begin;      // first pixel of the batch's pixel list
+};
+static_assert(sizeof(SceneRec) == 128, "scene record size");
+
+struct OneScene {
+    Env e;
+    __device__ __forceinline__ const Env& operator()(uint32_t) const { return e; }
+};
+struct SceneTable {
+    const SceneRec* recs;
+    __device__ __forceinline__ Env operator()(uint32_t i) const { return recs[i].env; }
+};
+
+// SV maps the ray's scene index to its Env: OneScene (the ray-buffer query,
+// registers) or SceneTable (the wavefront pipeline, one device record per
+// scene; loaded only on instance entry / exit and in leaves).
+template <bool STATS, uint32_t KINDS, class SV>
+__device__ __forceinline__ bool trav_step(Trav& s, uint2* stack, const SV& sv, const RtShaderBindingTable* sbt,
+                                          uint32_t* status, uint32_t ray_flags, uint32_t cull_mask,
                                           uint32_t ray_sbt_offset, Counters& cnt, int phase) {
     const uint32_t entry = s.entry;
     if (entry == kNoEntry) return true;
     if (phase >= 0 && is_node_entry(entry) != (phase == 1)) return false;  // waits for its phase
     if (++s.steps > kMaxTraversalSteps) {
-        atomicOr(e.status, 1u << RT_ERR_TIMEOUT);
+        atomicOr(status, 1u << RT_ERR_TIMEOUT);
         return true;
     }
     if (entry == kMarker) {
-        trav_restore_world(s, e);
+        trav_restore_world(s, sv(s.scene));
     } else if ((entry & kLeafEntry) == 0) {
         if (entry >= s.node_count) {
-            atomicOr(e.status, 1u << RT_ERR_BAD_AS);  // malformed reference: skip it
+            atomicOr(status, 1u << RT_ERR_BAD_AS);  // malformed reference: skip it
         } else {
             if (STATS) cnt.nodes++;
             uint32_t keys[8], refs[8];
@@ -401,7 +431,7 @@ __device__ __forceinline__ bool trav_step(Trav& s, uint2* stack, const Env& e, u
                     uint32_t key = keys[q];
                     if (key == 0xFFFFFFFFu) continue;
                     if (s.sp < (int)kStackSize) stack[s.sp++] = make_uint2(pick8(refs, key & 7u), key & ~7u);
-                    else atomicOr(e.status, 1u << RT_ERR_STACK_OVERFLOW);
+                    else atomicOr(status, 1u << RT_ERR_STACK_OVERFLOW);
                 }
                 s.entry = pick8(refs, keys[0] & 7u);
                 return false;
@@ -410,17 +440,17 @@ __device__ __forceinline__ bool trav_step(Trav& s, uint2* stack, const Env& e, u
     } else {
         const uint32_t first = entry & 0x0FFFFFFFu;
         const uint32_t count = ((entry >> 28) & 7u) + 1u;
-        if (first + count > (s.in_blas ? s.tri_count : e.inst_count)) {
-            atomicOr(e.status, 1u << RT_ERR_BAD_AS);  // malformed leaf: skip it
+        if (first + count > (s.in_blas ? s.tri_count : sv(s.scene).inst_count)) {
+            atomicOr(status, 1u << RT_ERR_BAD_AS);  // malformed leaf: skip it
         } else if (!s.in_blas) {
             // instance leaf: the record's last 32 bytes hold the BLAS fields
-            const InstRecord* ir = &e.insts[first];
+            const InstRecord* ir = &sv(s.scene).insts[first];
             const uint4* tail = reinterpret_cast<const uint4*>(&ir->blas);
             uint4 q0 = __ldg(tail), q1 = __ldg(tail + 1);
             // q0 = blas lo, blas hi, instance_id, custom_mask; q1 = sbt_flags, tri_count, node_count, prims_off256
             bool enter = q1.y != 0u && ((q0.w >> 24) & cull_mask) != 0u;
             if (enter && (blas_kind(q1.z) & KINDS) == 0u) {
-                atomicOr(e.status, 1u << RT_ERR_BAD_AS);  // the TLAS header does not list this format
+                atomicOr(status, 1u << RT_ERR_BAD_AS);  // the TLAS header does not list this format
                 enter = false;
             }
             if (enter) {
@@ -447,8 +477,8 @@ __device__ __forceinline__ bool trav_step(Trav& s, uint2* stack, const Env& e, u
                     s.entry = 0;  // BLAS root
                     return false;
                 }
-                atomicOr(e.status, 1u << RT_ERR_STACK_OVERFLOW);
-                trav_restore_world(s, e);
+                atomicOr(status, 1u << RT_ERR_STACK_OVERFLOW);
+                trav_restore_world(s, sv(s.scene));
             }
         } else {
             const uint32_t iflags = s.c_sbt_flags >> 24;
@@ -475,13 +505,14 @@ __device__ __forceinline__ bool trav_step(Trav& s, uint2* stack, const Env& e, u
                     if ((ray_flags & RT_RAY_FLAG_CULL_FRONT_FACING) && front) continue;
                 }
                 if (t == s.t && s.hit_inst != kNoHit &&
-                    !ids_below_best(e.insts, s.c_inst, s.hit_inst, geom, prim, s.hit_geom, s.hit_prim))
+                    !ids_below_best(sv(s.scene).insts, s.c_inst, s.hit_inst, geom, prim, s.hit_geom, s.hit_prim))
                     continue;
-                if (!opaque && e.models) {
-                    const RtHitGroup* g = hit_group(e, s.c_sbt_flags, ray_sbt_offset);
+                if (!opaque) {
+                    const Env e = sv(s.scene);
+                    const RtHitGroup* g = e.models ? hit_group(sbt, s.c_sbt_flags, ray_sbt_offset) : nullptr;
                     if (g && g->any_hit == RT_PROGRAM_ANY_HIT_ALPHA_CLIP &&
-                        !alpha_clip_accepts(e.models, e.textures, e.insts[s.c_inst].custom_mask & 0xFFFFFFu, geom,
-                                            prim, u, v))
+                        !alpha_clip_accepts(e.models, e.textures, e.texture_count,
+                                            e.insts[s.c_inst].custom_mask & 0xFFFFFFu, geom, prim, u, v))
                         continue;
                 }
                 s.t = t;
@@ -503,13 +534,6 @@ __device__ __forceinline__ bool trav_step(Trav& s, uint2* stack, const Env& e, u
 }
 
 __device__ __forceinline__ void flush_counters(RtStats* st, const Counters& c) {
-    unsigned long long tr = (unsigned long long)c.primary + c.secondary + c.shadow;
-    if (tr) {
-        atomicAdd(reinterpret_cast<unsigned long long*>(&st->traversals), tr);
-        atomicAdd(reinterpret_cast<unsigned long long*>(&st->primary_rays), (unsigned long long)c.primary);
-        atomicAdd(reinterpret_cast<unsigned long long*>(&st->secondary_rays), (unsigned long long)c.secondary);
-        atomicAdd(reinterpret_cast<unsigned long long*>(&st->shadow_rays), (unsigned long long)c.shadow);
-    }
     if (c.nodes | c.tris | c.insts) {
         atomicAdd(reinterpret_cast<unsigned long long*>(&st->nodes_visited), (unsigned long long)c.nodes);
         atomicAdd(reinterpret_cast<unsigned long long*>(&st->triangles_tested), (unsigned long long)c.tris);
@@ -517,51 +541,148 @@ __device__ __forceinline__ void flush_counters(RtStats* st, const Counters& c) {
     }
 }
 
+// Rays counted where they are created (one atomic per warp), so the
+// traversal loops carry no counters: every created ray is traced.
+__device__ __forceinline__ void count_rays(RtStats* st, uint32_t primary, uint32_t secondary, uint32_t shadow) {
+    const uint32_t lane = threadIdx.x & 31u;
+    uint32_t v[3] = {primary, secondary, shadow};
+#pragma unroll
+    for (int k = 0; k < 3; k++)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xFFFFFFFFu, v[k], o);
+    if (lane == 0 && (v[0] | v[1] | v[2])) {
+        atomicAdd(reinterpret_cast<unsigned long long*>(&st->traversals), (unsigned long long)v[0] + v[1] + v[2]);
+        if (v[0]) atomicAdd(reinterpret_cast<unsigned long long*>(&st->primary_rays), (unsigned long long)v[0]);
+        if (v[1]) atomicAdd(reinterpret_cast<unsigned long long*>(&st->secondary_rays), (unsigned long long)v[1]);
+        if (v[2]) atomicAdd(reinterpret_cast<unsigned long long*>(&st->shadow_rays), (unsigned long long)v[2]);
+    }
+}
+
 // ---------------------------------------------------------------------------
-// Wavefront buffers (the per-stream workspace of the context)
+// Wavefront buffers (the per-stream workspace of the context).  A launch
+// traces a batch of scenes: their 8x4 pixel tiles and their pixels are
+// concatenated into one list each, and every ray carries its scene index,
+// so one persistent launch per wavefront serves all scenes.
 // ---------------------------------------------------------------------------
 struct WfCounters {
     uint32_t ray_count[kMaxDepth + 1];  // rays of each bounce list
-    uint32_t shadow_count;              // pixels with a textured hit
+    uint32_t shade_count;               // pixels with a textured hit
+    uint32_t shadow_count;              // shadow rays
     uint32_t work[kMaxDepth + 2];       // fetch counters of the persistent trace launches
+    uint32_t kinds;                     // union of the scenes' TLAS kinds (k_setup)
 };
 
 struct WfBuffers {
     float4* rays[2];           // per ray: (origin, tmin), (direction, tmax)
-    uint32_t* ray_pixel[2];    // pixel of each ray, kNoPixel for padding
+    uint32_t* ray_pixel[2];    // batch pixel of each ray, kNoPixel for padding
+    uint32_t* ray_scene[2];    // scene of each ray
     uint4* hits;               // per ray: (t, u, v, inst), (geom, prim, front, 0)
-    float4* colour;            // per pixel, linear
+    float4* colour;            // per batch pixel, linear
     float4* shade;             // per pixel: (so.xyz, NoL), (comb.xyz, amb.x), (amb.yz, 0, 0)
     uint32_t* lit;             // per pixel: shadow rays that missed
-    uint32_t* shadow_list;     // pixels with a textured hit
+    uint32_t* shade_list;      // pixels with a textured hit
+    float4* shadow_rays;       // per shadow ray: (origin, tmin), (direction, tmax)
+    uint32_t* shadow_pixel;    // per shadow ray: its pixel
+    uint32_t* shadow_scene;    // per shadow ray: its scene
     unsigned long long* heat;  // per pixel traversal clock cycles (heatmap)
     WfCounters* ctr;
+    SceneRec* scenes;
+    RtTextureDesc* ctx_textures;  // the context's texture table, copied by k_setup
 };
 
 struct WfParams {
-    TraceLaunch L;
     WfBuffers B;
-    uint32_t tiles_x;
-    uint32_t total;            // ray slots of the primary list (tiles * 32)
+    RtShaderBindingTable sbt;
+    RtStats* stats;
+    uint32_t* status;
+    uint32_t scene_count;
+    uint32_t total_slots;      // ray slots of the primary list (tiles * 32)
+    uint32_t total_pixels;
     uint32_t bounce;
+    uint32_t kinds_built;
 };
 
-__device__ __forceinline__ void tile_pixel(uint32_t i, uint32_t tiles_x, uint32_t* x, uint32_t* y) {
-    uint32_t tile = i >> 5, l = i & 31u;
-    *x = (tile % tiles_x) * 8u + (l & 7u);
-    *y = (tile / tiles_x) * 4u + (l >> 3);
+// Scene of batch tile / pixel v: the last scene whose first tile / pixel is <= v.
+template <bool PIXEL>
+__device__ __forceinline__ uint32_t scene_of(const WfParams& P, uint32_t v) {
+    uint32_t lo = 0, hi = P.scene_count;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        const uint32_t first = PIXEL ? P.B.scenes[mid].pixel_begin : P.B.scenes[mid].tile_begin;
+        if (first <= v) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// Warp-aggregated append of n items per lane; all 32 lanes must call it.
+__device__ __forceinline__ uint32_t warp_append_n(uint32_t* counter, uint32_t n) {
+    const uint32_t lane = threadIdx.x & 31u;
+    uint32_t x = n;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+        if (lane >= (uint32_t)o) x += y;
+    }
+    const uint32_t total = __shfl_sync(0xFFFFFFFFu, x, 31);
+    uint32_t base = 0;
+    if (lane == 31u && total) base = atomicAdd(counter, total);
+    base = __shfl_sync(0xFFFFFFFFu, base, 31);
+    return base + x - n;
+}
+
+constexpr uint32_t kSetupChunk = 64;
+struct SceneLayout {
+    uint32_t tiles_x, tile_begin, pixel_begin;
+};
+struct SetupParams {
+    TraceScene d[kSetupChunk];
+    SceneLayout lay[kSetupChunk];
+    RtTextureDesc textures[RT_MAX_BOUND_IMAGES];  // the context's table
+    WfBuffers B;
+    uint32_t* status;
+    uint32_t first, count;
+    uint32_t copy_textures;
+};
+
+// Scene records of one chunk of the batch (TLAS header -> Env).
+__global__ void k_setup(const __grid_constant__ SetupParams P) {
+    const uint32_t t = threadIdx.x;
+    if (P.copy_textures)
+        for (uint32_t i = t; i < RT_MAX_BOUND_IMAGES; i += blockDim.x) P.B.ctx_textures[i] = P.textures[i];
+    if (t >= P.count) return;
+    const TraceScene& d = P.d[t];
+    SceneRec r;
+    const bool own = d.textures != nullptr;
+    r.env = make_env(d.push.acceleration_structure, d.push.model_info, own ? d.textures : P.B.ctx_textures,
+                     own ? d.texture_count : RT_MAX_BOUND_IMAGES, P.status);
+    r.uniforms = reinterpret_cast<const RtUniforms*>(d.push.uniforms);
+    r.image = reinterpret_cast<uint32_t*>(d.desc.image_address);
+    r.radiance = reinterpret_cast<float4*>(d.desc.radiance_address);
+    r.width = d.desc.width;
+    r.height = d.desc.height;
+    r.max_depth = d.desc.max_trace_depth;
+    r.shadow_count = d.desc.shadow_ray_count;
+    r.flags = d.desc.flags;
+    r.tiles_x = P.lay[t].tiles_x;
+    r.tile_begin = P.lay[t].tile_begin;
+    r.pixel_begin = P.lay[t].pixel_begin;
+    P.B.scenes[P.first + t] = r;
+    atomicOr(&P.B.ctr->kinds, r.env.blas_kinds ? r.env.blas_kinds : kBlasKindF32);
 }
 
 // ray_generation, lib.rs:126-142 (camera ray, fixed operation order)
 __global__ void k_raygen(const __grid_constant__ WfParams P) {
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= P.total) return;
-    const RtUniforms& U = *reinterpret_cast<const RtUniforms*>(P.L.push.uniforms);
-    const uint32_t W = P.L.desc.width, H = P.L.desc.height;
-    uint32_t x, y;
-    tile_pixel(i, P.tiles_x, &x, &y);
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.total_slots) return;
+    const uint32_t tile = i >> 5, l = i & 31u;
+    const uint32_t sc = scene_of<false>(P, tile);
+    const SceneRec& S = P.B.scenes[sc];
+    const uint32_t lt = tile - S.tile_begin, W = S.width, H = S.height;
+    const uint32_t x = (lt % S.tiles_x) * 8u + (l & 7u), y = (lt / S.tiles_x) * 4u + (l >> 3);
     float4* R = P.B.rays[0];
     if (x < W && y < H) {
+        const RtUniforms& U = *S.uniforms;
         float pcx = (float)x + 0.5f, pcy = (float)y + 0.5f;
         float tcx = pcx / (float)W, tcy = pcy / (float)H;
         float rx = tcx * 2.0f - 1.0f, ry = tcy * 2.0f - 1.0f;
@@ -576,92 +697,92 @@ __global__ void k_raygen(const __grid_constant__ WfParams P) {
                     mat4_row(VI, 2, local.x, local.y, local.z, 0.0f));
         R[2 * (size_t)i] = make_float4(ro.x, ro.y, ro.z, 0.01f);
         R[2 * (size_t)i + 1] = make_float4(rd.x, rd.y, rd.z, 10000.0f);
-        P.B.ray_pixel[0][i] = y * W + x;
+        P.B.ray_pixel[0][i] = S.pixel_begin + y * W + x;
     } else {
         R[2 * (size_t)i] = make_float4(0.0f, 0.0f, 0.0f, 1.0f);  // tmin > tmax: never traversed
         R[2 * (size_t)i + 1] = make_float4(0.0f, 0.0f, 1.0f, 0.0f);
         P.B.ray_pixel[0][i] = kNoPixel;
     }
-    if (i == 0) P.B.ctr->ray_count[0] = P.total;
+    P.B.ray_scene[0][i] = sc;
+    if (i == 0) P.B.ctr->ray_count[0] = P.total_slots;
+    count_rays(P.stats, x < W && y < H ? 1u : 0u, 0u, 0u);
 }
 
 // Persistent trace loop with per-lane ray replacement.
 template <int MODE, bool STATS, uint32_t KINDS>
-__device__ __forceinline__ void trace_wavefront(const WfParams& P, const Env& e) {
-    const TraceLaunch& L = P.L;
-    const RtUniforms& U = *reinterpret_cast<const RtUniforms*>(L.push.uniforms);
+__device__ __forceinline__ void trace_wavefront(const WfParams& P) {
+    const SceneTable sv{P.B.scenes};
     const uint32_t b = P.bounce;
-    const uint32_t nshadow = L.desc.shadow_ray_count;
-    const bool heat = MODE != kModeRayBuf && U.show_heatmap != 0;
     uint32_t total;
     uint32_t* work;
     if (MODE == kModeBounce) {
         total = P.B.ctr->ray_count[b];
         work = &P.B.ctr->work[b];
     } else {
-        total = P.B.ctr->shadow_count * nshadow;
+        total = P.B.ctr->shadow_count;
         work = &P.B.ctr->work[kMaxDepth + 1];
     }
     const uint32_t ray_flags = MODE == kModeShadow
                                    ? (RT_RAY_FLAG_TERMINATE_ON_FIRST_HIT | RT_RAY_FLAG_SKIP_CLOSEST_HIT_SHADER)
                                    : RT_RAY_FLAG_NONE;
     const uint32_t sbt_offset = MODE == kModeShadow ? 1u : 0u;
-    const V3 sun_dir = mk3(U.sun_dir[0], U.sun_dir[1], U.sun_dir[2]);
-    const uint32_t W = L.desc.width;
 
-    Counters cnt = {0, 0, 0, 0, 0, 0};
+    Counters cnt = {0, 0, 0};
     uint2 stack[kStackSize];
     Trav s;
-    uint32_t item = kNoItem, pix = kNoPixel;
-    long long t0 = 0;
+    uint32_t item = kNoItem;
+    bool heat = false;
+    uint32_t t0 = 0;  // clock() at the ray's start (heatmap only)
     for (;;) {
         uint32_t my = warp_append(work, item == kNoItem);
         if (item == kNoItem) {
             if (my >= total) break;
             item = my;
+            uint32_t sc, pix;
             if (MODE == kModeBounce) {
                 float4 a = P.B.rays[b & 1][2 * (size_t)item], c = P.B.rays[b & 1][2 * (size_t)item + 1];
                 pix = P.B.ray_pixel[b & 1][item];
-                trav_begin(s, e, mk3(a.x, a.y, a.z), mk3(c.x, c.y, c.z), a.w, c.w);
-                if (pix != kNoPixel) {
-                    if (b == 0) cnt.primary++;
-                    else cnt.secondary++;
-                }
+                sc = P.B.ray_scene[b & 1][item];
+                trav_begin(s, sv(sc), mk3(a.x, a.y, a.z), mk3(c.x, c.y, c.z), a.w, c.w);
             } else {
-                pix = P.B.shadow_list[item / nshadow];
-                uint32_t si = item % nshadow;
-                float4 so = P.B.shade[3 * (size_t)pix];
-                V3 sd = shadow_direction(e, U, pix % W, pix / W, si, sun_dir);
-                trav_begin(s, e, mk3(so.x, so.y, so.z), sd, 0.001f, 10000.0f);
-                cnt.shadow++;
+                float4 a = P.B.shadow_rays[2 * (size_t)item], c = P.B.shadow_rays[2 * (size_t)item + 1];
+                pix = P.B.shadow_pixel[item];
+                sc = P.B.shadow_scene[item];
+                trav_begin(s, sv(sc), mk3(a.x, a.y, a.z), mk3(c.x, c.y, c.z), a.w, c.w);
             }
-            if (heat) t0 = clock64();
+            s.scene = sc;
+            heat = pix != kNoPixel && P.B.scenes[sc].uniforms->show_heatmap != 0;
+            if (heat) t0 = (uint32_t)clock();
         }
 #if RT_TRACE_LEAF_WAIT < 0
         const int phase = -1;
 #else
         const int phase = node_phase(s.entry) ? 1 : 0;
 #endif
-        if (!trav_step<STATS, KINDS>(s, stack, e, ray_flags, 0xFFu, sbt_offset, cnt, phase)) continue;
+        if (!trav_step<STATS, KINDS>(s, stack, sv, &P.sbt, P.status, ray_flags, 0xFFu, sbt_offset, cnt, phase))
+            continue;
         // the ray is finished
         if (MODE == kModeBounce) {
             P.B.hits[2 * (size_t)item] = make_uint4(__float_as_uint(s.t), __float_as_uint(s.u), __float_as_uint(s.v),
                                                     s.hit_inst);
             P.B.hits[2 * (size_t)item + 1] = make_uint4(s.hit_geom, s.hit_prim, s.front ? 1u : 0u, 0u);
         } else if (s.hit_inst == kNoHit) {
-            atomicAdd(&P.B.lit[pix], 1u);  // shadow_ray_miss clears `shadowed`
+            atomicAdd(&P.B.lit[P.B.shadow_pixel[item]], 1u);  // shadow_ray_miss clears `shadowed`
         }
-        if (heat && pix != kNoPixel) atomicAdd(&P.B.heat[pix], (unsigned long long)(clock64() - t0));
+        if (heat) {
+            const uint32_t pix = MODE == kModeBounce ? P.B.ray_pixel[b & 1][item] : P.B.shadow_pixel[item];
+            atomicAdd(&P.B.heat[pix], (unsigned long long)((uint32_t)clock() - t0));
+        }
         item = kNoItem;
     }
-    flush_counters(L.stats, cnt);
+    flush_counters(P.stats, cnt);
 }
 
 // One traversal kernel per BLAS node-format set KINDS, each with its own
 // register allocation (one kernel holding all three loops spills far more).
 // The host launches the variant for the formats this process has built; when
-// it has built both, it launches all three and each runs only if the TLAS
-// header names exactly its set.
+// it has built both, it launches all three and each runs only if the
+// scenes' TLAS headers name exactly its set.
 __device__ __forceinline__ bool kinds_selected(uint32_t kinds_built, uint32_t tlas_kinds, uint32_t kinds) {
     if (kinds_built != (kBlasKindF32 | kBlasKindQ8)) return true;  // the only launch
     return (tlas_kinds ? tlas_kinds : kBlasKindF32) == kinds;
@@ -669,134 +790,153 @@ __device__ __forceinline__ bool kinds_selected(uint32_t kinds_built, uint32_t tl
 
 template <int MODE, bool STATS, uint32_t KINDS>
 __global__ void __launch_bounds__(kTraceThreads, RT_TRACE_MIN_BLOCKS) k_trace(const __grid_constant__ WfParams P) {
-    const Env e = make_env(P.L.push.acceleration_structure, P.L.push, &P.L.sbt, P.L.textures, P.L.status);
-    if (kinds_selected(P.L.kinds_built, e.blas_kinds, KINDS)) trace_wavefront<MODE, STATS, KINDS>(P, e);
+    if (kinds_selected(P.kinds_built, P.B.ctr->kinds, KINDS)) trace_wavefront<MODE, STATS, KINDS>(P);
 }
 
-// The closest-hit and miss programs for every ray of bounce b.
+// The closest-hit and miss programs for every ray of bounce b.  Every lane
+// of the (full) warps reaches the appends at the end.
 __global__ void k_shade(const __grid_constant__ WfParams P) {
     const uint32_t b = P.bounce;
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= P.B.ctr->ray_count[b]) return;
-    uint32_t p = P.B.ray_pixel[b & 1][i];
-    if (p == kNoPixel) return;
-    const TraceLaunch& L = P.L;
-    const Env e = make_env(L.push.acceleration_structure, L.push, &L.sbt, L.textures, L.status);
-    const RtUniforms& U = *reinterpret_cast<const RtUniforms*>(L.push.uniforms);
-    const V3 sun_dir = mk3(U.sun_dir[0], U.sun_dir[1], U.sun_dir[2]);
-    const uint32_t nshadow = L.desc.shadow_ray_count;
-    float4 ra = P.B.rays[b & 1][2 * (size_t)i], rb = P.B.rays[b & 1][2 * (size_t)i + 1];
-    V3 ro = mk3(ra.x, ra.y, ra.z), rd = mk3(rb.x, rb.y, rb.z);
-    uint4 h0 = P.B.hits[2 * (size_t)i], h1 = P.B.hits[2 * (size_t)i + 1];
-    const float t = __uint_as_float(h0.x), hu = __uint_as_float(h0.y), hv = __uint_as_float(h0.z);
-    const uint32_t inst = h0.w;
-    bool emit_shadow = false, emit_ray = false, write_colour = false;
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t p = kNoPixel, sc = 0, nshadow = 0;
+    bool emit_ray = false, write_colour = false;
     V3 col = mk3(0.0f, 0.0f, 0.0f), nd = mk3(0, 0, 0), no = mk3(0, 0, 0);
-    if (inst == kNoHit) {
-        // primary_ray_miss (lib.rs:40-51)
-        float sun_s, sun_c;
-        rt_sincos(U.sun_radius, &sun_s, &sun_c);
-        col = dot3(rd, sun_dir) > sun_c ? mk3(1.0f, 1.0f, 1.0f) : mk3(0.0f, 0.0f, 0.05f);
-        write_colour = true;
-    } else {
-        const InstRecord* ir = &e.insts[inst];
-        const uint32_t sbt_flags = ir->sbt_flags, custom = ir->custom_mask & 0xFFFFFFu;
-        const RtHitGroup* g = hit_group(e, sbt_flags, 0u);
-        const uint32_t prog = g ? g->closest_hit : RT_PROGRAM_NONE;
-        const V3 bary = mk3((1.0f - hu) - hv, hu, hv);
-        TriData td;
-        if (prog == RT_PROGRAM_CLOSEST_HIT_MIRROR && load_triangle(e, custom, h1.x, h1.y, &td)) {
-            // closest_hit_mirror.glsl:11-29
-            V3 ni = interp3(td.n[0], td.n[1], td.n[2], bary);
-            V3 n = normalize3(xform_normal_w2o_t(ir->w2o, ni));
-            float k = 2.0f * dot3(n, rd);
-            nd = sub3(rd, mul3s(n, k));
-            no = add3(ro, mul3s(rd, t));
-        } else if (prog == RT_PROGRAM_CLOSEST_HIT_PORTAL) {
-            // lib.rs:300-312
-            nd = rd;
-            no = add3(add3(ro, mul3s(rd, t)), mk3(0.0f, 5.0f, 0.0f));
-        } else if (prog == RT_PROGRAM_CLOSEST_HIT_TEXTURED && load_triangle(e, custom, h1.x, h1.y, &td)) {
-            // closest_hit_textured.glsl:174-226
-            V3 ip = interp3(td.p[0], td.p[1], td.p[2], bary);
-            V3 inrm = interp3(td.n[0], td.n[1], td.n[2], bary);
-            float iu = (td.uv[0][0] * bary.x + td.uv[1][0] * bary.y) + td.uv[2][0] * bary.z;
-            float iv = (td.uv[0][1] * bary.x + td.uv[1][1] * bary.y) + td.uv[2][1] * bary.z;
-            V3 oa = project_onto_tangent_plane(ip, td.p[0], td.n[0]);
-            V3 ob = project_onto_tangent_plane(ip, td.p[1], td.n[1]);
-            V3 oc = project_onto_tangent_plane(ip, td.p[2], td.n[2]);
-            V3 off = interp3(oa, ob, oc, bary);
-            V3 so = xform_point(ir->o2w, add3(ip, off));
-            float NoL;
-            V3 comb, amb;
-            const bool lambert = (L.desc.flags & RT_TRACE_FLAG_LAMBERT_DIFFUSE) != 0;
-            shade_textured(e, td, inrm, iu, iv, ir->w2o, rd, sun_dir, lambert, &NoL, &comb, &amb);
-            if (nshadow > 0) {
-                float4* sh = P.B.shade + 3 * (size_t)p;
-                sh[0] = make_float4(so.x, so.y, so.z, NoL);
-                sh[1] = make_float4(comb.x, comb.y, comb.z, amb.x);
-                sh[2] = make_float4(amb.y, amb.z, 0.0f, 0.0f);
-                emit_shadow = true;
-            } else {
-                float sf = 0.0f;
-                col = mk3((sf * NoL) * comb.x + amb.x, (sf * NoL) * comb.y + amb.y, (sf * NoL) * comb.z + amb.z);
-                write_colour = true;
+    if (i < P.B.ctr->ray_count[b]) p = P.B.ray_pixel[b & 1][i];
+    if (p != kNoPixel) {
+        sc = P.B.ray_scene[b & 1][i];
+        const SceneRec& S = P.B.scenes[sc];
+        const Env& e = S.env;
+        const RtUniforms& U = *S.uniforms;
+        const V3 sun_dir = mk3(U.sun_dir[0], U.sun_dir[1], U.sun_dir[2]);
+        float4 ra = P.B.rays[b & 1][2 * (size_t)i], rb = P.B.rays[b & 1][2 * (size_t)i + 1];
+        V3 ro = mk3(ra.x, ra.y, ra.z), rd = mk3(rb.x, rb.y, rb.z);
+        uint4 h0 = P.B.hits[2 * (size_t)i], h1 = P.B.hits[2 * (size_t)i + 1];
+        const float t = __uint_as_float(h0.x), hu = __uint_as_float(h0.y), hv = __uint_as_float(h0.z);
+        const uint32_t inst = h0.w;
+        if (inst == kNoHit) {
+            // primary_ray_miss (lib.rs:40-51)
+            float sun_s, sun_c;
+            rt_sincos(U.sun_radius, &sun_s, &sun_c);
+            col = dot3(rd, sun_dir) > sun_c ? mk3(1.0f, 1.0f, 1.0f) : mk3(0.0f, 0.0f, 0.05f);
+            write_colour = true;
+        } else {
+            const InstRecord* ir = &e.insts[inst];
+            const uint32_t sbt_flags = ir->sbt_flags, custom = ir->custom_mask & 0xFFFFFFu;
+            const RtHitGroup* g = hit_group(&P.sbt, sbt_flags, 0u);
+            const uint32_t prog = g ? g->closest_hit : RT_PROGRAM_NONE;
+            const V3 bary = mk3((1.0f - hu) - hv, hu, hv);
+            TriData td;
+            if (prog == RT_PROGRAM_CLOSEST_HIT_MIRROR && load_triangle(e, custom, h1.x, h1.y, &td)) {
+                // closest_hit_mirror.glsl:11-29
+                V3 ni = interp3(td.n[0], td.n[1], td.n[2], bary);
+                V3 n = normalize3(xform_normal_w2o_t(ir->w2o, ni));
+                float k = 2.0f * dot3(n, rd);
+                nd = sub3(rd, mul3s(n, k));
+                no = add3(ro, mul3s(rd, t));
+            } else if (prog == RT_PROGRAM_CLOSEST_HIT_PORTAL) {
+                // lib.rs:300-312
+                nd = rd;
+                no = add3(add3(ro, mul3s(rd, t)), mk3(0.0f, 5.0f, 0.0f));
+            } else if (prog == RT_PROGRAM_CLOSEST_HIT_TEXTURED && load_triangle(e, custom, h1.x, h1.y, &td)) {
+                // closest_hit_textured.glsl:174-226
+                V3 ip = interp3(td.p[0], td.p[1], td.p[2], bary);
+                V3 inrm = interp3(td.n[0], td.n[1], td.n[2], bary);
+                float iu = (td.uv[0][0] * bary.x + td.uv[1][0] * bary.y) + td.uv[2][0] * bary.z;
+                float iv = (td.uv[0][1] * bary.x + td.uv[1][1] * bary.y) + td.uv[2][1] * bary.z;
+                V3 oa = project_onto_tangent_plane(ip, td.p[0], td.n[0]);
+                V3 ob = project_onto_tangent_plane(ip, td.p[1], td.n[1]);
+                V3 oc = project_onto_tangent_plane(ip, td.p[2], td.n[2]);
+                V3 off = interp3(oa, ob, oc, bary);
+                V3 so = xform_point(ir->o2w, add3(ip, off));
+                float NoL;
+                V3 comb, amb;
+                const bool lambert = (S.flags & RT_TRACE_FLAG_LAMBERT_DIFFUSE) != 0;
+                shade_textured(e, td, inrm, iu, iv, ir->w2o, rd, sun_dir, lambert, &NoL, &comb, &amb);
+                if (S.shadow_count > 0) {
+                    float4* sh = P.B.shade + 3 * (size_t)p;
+                    sh[0] = make_float4(so.x, so.y, so.z, NoL);
+                    sh[1] = make_float4(comb.x, comb.y, comb.z, amb.x);
+                    sh[2] = make_float4(amb.y, amb.z, 0.0f, 0.0f);
+                    nshadow = S.shadow_count;
+                } else {
+                    float sf = 0.0f;
+                    col = mk3((sf * NoL) * comb.x + amb.x, (sf * NoL) * comb.y + amb.y, (sf * NoL) * comb.z + amb.z);
+                    write_colour = true;
+                }
             }
-        }
-        if (!emit_shadow && !write_colour) {
-            // payload: break when new_ray_direction == 0 (lib.rs:165-171),
-            // and after the last iteration the colour stays reset (black)
-            if ((nd.x == 0.0f && nd.y == 0.0f && nd.z == 0.0f) || b + 1 >= L.desc.max_trace_depth) {
-                col = mk3(0.0f, 0.0f, 0.0f);
-                write_colour = true;
-            } else {
-                emit_ray = true;
+            if (nshadow == 0 && !write_colour) {
+                // payload: break when new_ray_direction == 0 (lib.rs:165-171),
+                // and after the last iteration the colour stays reset (black)
+                if ((nd.x == 0.0f && nd.y == 0.0f && nd.z == 0.0f) || b + 1 >= S.max_depth) {
+                    col = mk3(0.0f, 0.0f, 0.0f);
+                    write_colour = true;
+                } else {
+                    emit_ray = true;
+                }
             }
         }
     }
     if (write_colour) P.B.colour[p] = make_float4(col.x, col.y, col.z, 1.0f);
-    uint32_t si = warp_append(&P.B.ctr->shadow_count, emit_shadow);
-    if (emit_shadow) P.B.shadow_list[si] = p;
-    uint32_t ri = warp_append(&P.B.ctr->ray_count[b + 1], emit_ray);
+    const uint32_t si = warp_append(&P.B.ctr->shade_count, nshadow > 0);
+    if (nshadow > 0) P.B.shade_list[si] = p;
+    const uint32_t first = warp_append_n(&P.B.ctr->shadow_count, nshadow);
+    if (nshadow > 0) {
+        // the textured hit's shadow rays (closest_hit_textured.glsl:159-172)
+        const SceneRec& S = P.B.scenes[sc];
+        const RtUniforms& U = *S.uniforms;
+        const V3 sun_dir = mk3(U.sun_dir[0], U.sun_dir[1], U.sun_dir[2]);
+        const uint32_t lp = p - S.pixel_begin, x = lp % S.width, y = lp / S.width;
+        const float4 so = P.B.shade[3 * (size_t)p];
+        for (uint32_t k = 0; k < nshadow; k++) {
+            const V3 sd = shadow_direction(S.env, U, x, y, k, sun_dir);
+            float4* R = P.B.shadow_rays + 2 * (size_t)(first + k);
+            R[0] = make_float4(so.x, so.y, so.z, 0.001f);
+            R[1] = make_float4(sd.x, sd.y, sd.z, 10000.0f);
+            P.B.shadow_pixel[first + k] = p;
+            P.B.shadow_scene[first + k] = sc;
+        }
+    }
+    count_rays(P.stats, 0u, emit_ray ? 1u : 0u, nshadow);
+    const uint32_t ri = warp_append(&P.B.ctr->ray_count[b + 1], emit_ray);
     if (emit_ray) {
         float4* R = P.B.rays[(b + 1) & 1];
         R[2 * (size_t)ri] = make_float4(no.x, no.y, no.z, 0.01f);
         R[2 * (size_t)ri + 1] = make_float4(nd.x, nd.y, nd.z, 10000.0f);
         P.B.ray_pixel[(b + 1) & 1][ri] = p;
+        P.B.ray_scene[(b + 1) & 1][ri] = sc;
     }
 }
 
 // sun_factor = lit / N; colour = brdf * sun_factor + ambient.
 __global__ void k_resolve(const __grid_constant__ WfParams P) {
-    uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= P.B.ctr->shadow_count) return;
-    uint32_t p = P.B.shadow_list[k];
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= P.B.ctr->shade_count) return;
+    const uint32_t p = P.B.shade_list[k];
+    const SceneRec& S = P.B.scenes[scene_of<true>(P, p)];
     const float4* sh = P.B.shade + 3 * (size_t)p;
     float4 s0 = sh[0], s1 = sh[1], s2 = sh[2];
-    float sf = (float)P.B.lit[p] / (float)P.L.desc.shadow_ray_count;
+    float sf = (float)P.B.lit[p] / (float)S.shadow_count;
     float NoL = s0.w;
     P.B.colour[p] = make_float4((sf * NoL) * s1.x + s1.w, (sf * NoL) * s1.y + s2.x, (sf * NoL) * s1.z + s2.y, 1.0f);
 }
 
 // Heatmap (lib.rs:174-186), linear_to_srgb and the RGBA8 image write.
 __global__ void k_output(const __grid_constant__ WfParams P) {
-    const uint32_t W = P.L.desc.width, H = P.L.desc.height;
-    uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= W * H) return;
-    const RtUniforms& U = *reinterpret_cast<const RtUniforms*>(P.L.push.uniforms);
-    float4 c4 = P.B.colour[p];
+    const uint32_t gp = blockIdx.x * blockDim.x + threadIdx.x;
+    if (gp >= P.total_pixels) return;
+    const SceneRec& S = P.B.scenes[scene_of<true>(P, gp)];
+    const uint32_t p = gp - S.pixel_begin;
+    float4 c4 = P.B.colour[gp];
     V3 c = mk3(c4.x, c4.y, c4.z);
-    if (U.show_heatmap) {
-        V3 hm = heatmap_temperature((float)P.B.heat[p] / 1000000.0f);
+    if (S.uniforms->show_heatmap) {
+        V3 hm = heatmap_temperature((float)P.B.heat[gp] / 1000000.0f);
         c = add3(hm, mul3s(c, 0.000001f));
     }
-    float4* rad = reinterpret_cast<float4*>(P.L.desc.radiance_address);
-    uint32_t* img = reinterpret_cast<uint32_t*>(P.L.desc.image_address);
-    if (rad) rad[p] = make_float4(c.x, c.y, c.z, 1.0f);
-    if (img) {
+    if (S.radiance) S.radiance[p] = make_float4(c.x, c.y, c.z, 1.0f);
+    if (S.image) {
         uint32_t r = to_unorm8(linear_to_srgb(c.x)), g = to_unorm8(linear_to_srgb(c.y));
         uint32_t bl = to_unorm8(linear_to_srgb(c.z));
-        img[p] = r | (g << 8) | (bl << 16) | (255u << 24);
+        S.image[p] = r | (g << 8) | (bl << 16) | (255u << 24);
     }
 }
 
@@ -807,10 +947,15 @@ struct RayBufferParams {
 template <bool STATS, uint32_t KINDS>
 __device__ __forceinline__ void trace_ray_buffer(const RayBufferParams& P, const Env& e) {
     const RayBufferLaunch& L = P.L;
-    Counters cnt = {0, 0, 0, 0, 0, 0};
+    const OneScene sv{e};
+    Counters cnt = {0, 0, 0};
     uint2 stack[kStackSize];
     Trav s;
     uint32_t item = kNoItem;
+    if (blockIdx.x == 0 && threadIdx.x == 0 && L.count) {
+        atomicAdd(reinterpret_cast<unsigned long long*>(&L.stats->traversals), (unsigned long long)L.count);
+        atomicAdd(reinterpret_cast<unsigned long long*>(&L.stats->primary_rays), (unsigned long long)L.count);
+    }
     for (;;) {
         uint32_t my = warp_append(L.work, item == kNoItem);
         if (item == kNoItem) {
@@ -819,14 +964,16 @@ __device__ __forceinline__ void trace_ray_buffer(const RayBufferParams& P, const
             const float4* rp = reinterpret_cast<const float4*>(L.rays + item);
             float4 a = __ldg(rp), c = __ldg(rp + 1);
             trav_begin(s, e, mk3(a.x, a.y, a.z), mk3(c.x, c.y, c.z), a.w, c.w);
-            cnt.primary++;
+            s.scene = 0;
         }
 #if RT_TRACE_LEAF_WAIT < 0
         const int phase = -1;
 #else
         const int phase = node_phase(s.entry) ? 1 : 0;
 #endif
-        if (!trav_step<STATS, KINDS>(s, stack, e, L.ray_flags, L.cull_mask, L.sbt_offset, cnt, phase)) continue;
+        if (!trav_step<STATS, KINDS>(s, stack, sv, &L.sbt, L.status, L.ray_flags, L.cull_mask, L.sbt_offset, cnt,
+                                     phase))
+            continue;
         RtHit o;
         if (s.hit_inst != kNoHit) {
             const InstRecord* ir = &e.insts[s.hit_inst];
@@ -856,7 +1003,7 @@ __device__ __forceinline__ void trace_ray_buffer(const RayBufferParams& P, const
 template <bool STATS, uint32_t KINDS>
 __global__ void __launch_bounds__(kTraceThreads, RT_TRACE_MIN_BLOCKS)
     k_trace_ray_buffer(const __grid_constant__ RayBufferParams P) {
-    const Env e = make_env(P.L.tlas, P.L.push, &P.L.sbt, P.L.textures, P.L.status);
+    const Env e = make_env(P.L.tlas, P.L.push.model_info, P.L.textures, RT_MAX_BOUND_IMAGES, P.L.status);
     if (kinds_selected(P.L.kinds_built, e.blas_kinds, KINDS)) trace_ray_buffer<STATS, KINDS>(P, e);
 }
 
@@ -949,7 +1096,7 @@ void launch_trace_kernel(const WfParams& P, int num_sms, cudaStream_t stream) {
 
 template <int MODE>
 void launch_trace_mode(const WfParams& P, bool stats, int num_sms, cudaStream_t stream) {
-    for_each_variant(P.L.kinds_built, [&](auto k) {
+    for_each_variant(P.kinds_built, [&](auto k) {
         constexpr uint32_t K = decltype(k)::value;
         if (stats) launch_trace_kernel<MODE, true, K>(P, num_sms, stream);
         else launch_trace_kernel<MODE, false, K>(P, num_sms, stream);
@@ -965,27 +1112,66 @@ void launch_ray_buffer_kernel(const RayBufferParams& P, int num_sms, cudaStream_
 
 }  // namespace
 
-uint64_t trace_workspace_bytes(uint32_t width, uint32_t height) {
-    uint64_t tiles = (uint64_t)((width + 7) / 8) * ((height + 3) / 4);
-    uint64_t slots = tiles * 32, pix = (uint64_t)width * height;
-    uint64_t b = 0;
-    auto take = [&](uint64_t n) { b = align_up(b + n, 256); };
-    take(sizeof(WfCounters));
-    take(slots * 32);  // rays[0]
-    take(slots * 32);  // rays[1]
-    take(slots * 4);   // ray_pixel[0]
-    take(slots * 4);   // ray_pixel[1]
-    take(slots * 32);  // hits
-    take(pix * 16);    // colour
-    take(pix * 48);    // shade
-    take(pix * 4);     // lit
-    take(pix * 4);     // shadow_list
-    take(pix * 8);     // heat
-    return b;
+namespace {
+
+// Host-side layout of a batch: tiles and pixels concatenated scene by scene,
+// and the workspace regions.
+struct BatchLayout {
+    std::vector<SceneLayout> lay;
+    uint64_t slots = 0, pixels = 0, shadow_rays = 0;
+    uint32_t max_depth = 0;
+    bool any_shadow = false;
+    uint64_t off_ctr, off_scenes, off_tex, off_rays0, off_rays1, off_pix0, off_pix1, off_sc0, off_sc1, off_hits,
+        off_colour, off_shade, off_lit, off_shade_list, off_shadow_rays, off_shadow_pix, off_shadow_scene, off_heat,
+        total;
+
+    explicit BatchLayout(const TraceScene* sc, uint32_t n) : lay(n) {
+        for (uint32_t i = 0; i < n; i++) {
+            const uint32_t W = sc[i].desc.width, H = sc[i].desc.height;
+            const uint32_t tx = (W + 7) / 8, ty = (H + 3) / 4;
+            lay[i] = {tx, (uint32_t)(slots / 32), (uint32_t)pixels};
+            slots += (uint64_t)tx * ty * 32;
+            pixels += (uint64_t)W * H;
+            shadow_rays += (uint64_t)W * H * sc[i].desc.shadow_ray_count;
+            max_depth = std::max(max_depth, sc[i].desc.max_trace_depth);
+            any_shadow = any_shadow || sc[i].desc.shadow_ray_count > 0;
+        }
+        uint64_t b = 0;
+        auto take = [&](uint64_t bytes) {
+            uint64_t r = b;
+            b = align_up(b + bytes, 256);
+            return r;
+        };
+        off_ctr = take(sizeof(WfCounters));
+        off_scenes = take((uint64_t)n * sizeof(SceneRec));
+        off_tex = take(RT_MAX_BOUND_IMAGES * sizeof(RtTextureDesc));
+        off_rays0 = take(slots * 32);
+        off_rays1 = take(slots * 32);
+        off_pix0 = take(slots * 4);
+        off_pix1 = take(slots * 4);
+        off_sc0 = take(slots * 4);
+        off_sc1 = take(slots * 4);
+        off_hits = take(slots * 32);
+        off_colour = take(pixels * 16);
+        off_shade = take(pixels * 48);
+        off_lit = take(pixels * 4);
+        off_shade_list = take(pixels * 4);
+        off_shadow_rays = take(shadow_rays * 32);
+        off_shadow_pix = take(shadow_rays * 4);
+        off_shadow_scene = take(shadow_rays * 4);
+        off_heat = take(pixels * 8);
+        total = b;
+    }
+};
+
+}  // namespace
+
+uint64_t trace_workspace_bytes(const TraceScene* scenes, uint32_t count) {
+    return BatchLayout(scenes, count).total;
 }
 
-cudaError_t launch_trace_rays(const TraceLaunch& p, uint8_t* ws, int num_sms, cudaStream_t stream,
-                              KernelTimer* timer) {
+cudaError_t launch_trace_batch(const TraceBatch& tb, uint8_t* ws, int num_sms, cudaStream_t stream,
+                               KernelTimer* timer) {
     auto mark = [&](uint8_t kind) {
         if (timer && timer->n < KernelTimer::kMax) {
             timer->kind[timer->n] = kind;
@@ -994,52 +1180,75 @@ cudaError_t launch_trace_rays(const TraceLaunch& p, uint8_t* ws, int num_sms, cu
     };
     if (timer) timer->n = 0;
     mark(kKernStart);
-    const uint32_t W = p.desc.width, H = p.desc.height;
-    uint64_t tiles = (uint64_t)((W + 7) / 8) * ((H + 3) / 4);
-    uint64_t slots = tiles * 32, pix = (uint64_t)W * H;
+    const BatchLayout L(tb.scenes, tb.count);
     WfParams P;
-    P.L = p;
-    P.tiles_x = (W + 7) / 8;
-    P.total = (uint32_t)slots;
+    P.B.ctr = reinterpret_cast<WfCounters*>(ws + L.off_ctr);
+    P.B.scenes = reinterpret_cast<SceneRec*>(ws + L.off_scenes);
+    P.B.ctx_textures = reinterpret_cast<RtTextureDesc*>(ws + L.off_tex);
+    P.B.rays[0] = reinterpret_cast<float4*>(ws + L.off_rays0);
+    P.B.rays[1] = reinterpret_cast<float4*>(ws + L.off_rays1);
+    P.B.ray_pixel[0] = reinterpret_cast<uint32_t*>(ws + L.off_pix0);
+    P.B.ray_pixel[1] = reinterpret_cast<uint32_t*>(ws + L.off_pix1);
+    P.B.ray_scene[0] = reinterpret_cast<uint32_t*>(ws + L.off_sc0);
+    P.B.ray_scene[1] = reinterpret_cast<uint32_t*>(ws + L.off_sc1);
+    P.B.hits = reinterpret_cast<uint4*>(ws + L.off_hits);
+    P.B.colour = reinterpret_cast<float4*>(ws + L.off_colour);
+    P.B.shade = reinterpret_cast<float4*>(ws + L.off_shade);
+    P.B.lit = reinterpret_cast<uint32_t*>(ws + L.off_lit);
+    P.B.shade_list = reinterpret_cast<uint32_t*>(ws + L.off_shade_list);
+    P.B.shadow_rays = reinterpret_cast<float4*>(ws + L.off_shadow_rays);
+    P.B.shadow_pixel = reinterpret_cast<uint32_t*>(ws + L.off_shadow_pix);
+    P.B.shadow_scene = reinterpret_cast<uint32_t*>(ws + L.off_shadow_scene);
+    P.B.heat = reinterpret_cast<unsigned long long*>(ws + L.off_heat);
+    P.sbt = tb.sbt;
+    P.stats = tb.stats_dev;
+    P.status = tb.status;
+    P.scene_count = tb.count;
+    P.total_slots = (uint32_t)L.slots;
+    P.total_pixels = (uint32_t)L.pixels;
     P.bounce = 0;
-    uint64_t off = 0;
-    auto take = [&](uint64_t n) {
-        uint8_t* r = ws + off;
-        off = align_up(off + n, 256);
-        return r;
-    };
-    P.B.ctr = reinterpret_cast<WfCounters*>(take(sizeof(WfCounters)));
-    P.B.rays[0] = reinterpret_cast<float4*>(take(slots * 32));
-    P.B.rays[1] = reinterpret_cast<float4*>(take(slots * 32));
-    P.B.ray_pixel[0] = reinterpret_cast<uint32_t*>(take(slots * 4));
-    P.B.ray_pixel[1] = reinterpret_cast<uint32_t*>(take(slots * 4));
-    P.B.hits = reinterpret_cast<uint4*>(take(slots * 32));
-    P.B.colour = reinterpret_cast<float4*>(take(pix * 16));
-    P.B.shade = reinterpret_cast<float4*>(take(pix * 48));
-    P.B.lit = reinterpret_cast<uint32_t*>(take(pix * 4));
-    P.B.shadow_list = reinterpret_cast<uint32_t*>(take(pix * 4));
-    P.B.heat = reinterpret_cast<unsigned long long*>(take(pix * 8));
+    P.kinds_built = tb.kinds_built;
     cudaError_t err = cudaMemsetAsync(P.B.ctr, 0, sizeof(WfCounters), stream);
-    if (err == cudaSuccess) err = cudaMemsetAsync(P.B.lit, 0, pix * 4, stream);
-    if (err == cudaSuccess) err = cudaMemsetAsync(P.B.heat, 0, pix * 8, stream);
+    if (err == cudaSuccess) err = cudaMemsetAsync(P.B.lit, 0, L.pixels * 4, stream);
+    if (err == cudaSuccess) err = cudaMemsetAsync(P.B.heat, 0, L.pixels * 8, stream);
     if (err != cudaSuccess) return err;
-    const bool stats = (p.desc.flags & RT_TRACE_FLAG_COLLECT_STATS) != 0;
-    note_launch(), k_raygen<<<(uint32_t)((slots + 255) / 256), 256, 0, stream>>>(P);
+    // scene records, kSetupChunk scenes per launch (their descriptions travel as kernel parameters)
+    static SetupParams sp;  // 10 KB: kept off the stack; launches copy it
+    static std::mutex sp_mu;
+    {
+        std::lock_guard<std::mutex> lk(sp_mu);
+        for (uint32_t first = 0; first < tb.count; first += kSetupChunk) {
+            const uint32_t n = std::min(kSetupChunk, tb.count - first);
+            for (uint32_t i = 0; i < n; i++) {
+                sp.d[i] = tb.scenes[first + i];
+                sp.lay[i] = L.lay[first + i];
+            }
+            sp.copy_textures = first == 0;
+            if (first == 0) memcpy(sp.textures, tb.ctx_textures, sizeof sp.textures);
+            sp.B = P.B;
+            sp.status = tb.status;
+            sp.first = first;
+            sp.count = n;
+            note_launch(), k_setup<<<1, 128, 0, stream>>>(sp);
+        }
+    }
+    const bool stats = tb.stats != 0;
+    note_launch(), k_raygen<<<(uint32_t)((L.slots + 255) / 256), 256, 0, stream>>>(P);
     mark(kKernOther);
-    for (uint32_t b = 0; b < p.desc.max_trace_depth; b++) {
+    for (uint32_t b = 0; b < L.max_depth; b++) {
         P.bounce = b;
         launch_trace_mode<kModeBounce>(P, stats, num_sms, stream);
         mark(kKernClosest);
-        note_launch(), k_shade<<<(uint32_t)((slots + 127) / 128), 128, 0, stream>>>(P);
+        note_launch(), k_shade<<<(uint32_t)((L.slots + 127) / 128), 128, 0, stream>>>(P);
         mark(kKernShade);
     }
-    if (p.desc.shadow_ray_count > 0) {
+    if (L.any_shadow) {
         launch_trace_mode<kModeShadow>(P, stats, num_sms, stream);
         mark(kKernShadow);
-        note_launch(), k_resolve<<<(uint32_t)((pix + 255) / 256), 256, 0, stream>>>(P);
+        note_launch(), k_resolve<<<(uint32_t)((L.pixels + 255) / 256), 256, 0, stream>>>(P);
         mark(kKernOther);
     }
-    note_launch(), k_output<<<(uint32_t)((pix + 255) / 256), 256, 0, stream>>>(P);
+    note_launch(), k_output<<<(uint32_t)((L.pixels + 255) / 256), 256, 0, stream>>>(P);
     mark(kKernOther);
     return cudaGetLastError();
 }

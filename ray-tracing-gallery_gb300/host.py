@@ -73,14 +73,20 @@ class Device:
         t = torch.from_numpy(a.view(np.uint8).reshape(-1).copy()).to("cuda")
         return t
 
-    def set_texture(self, index: int, tex: Texture) -> None:
-        buf = self.upload(tex.texels)
+    @classmethod
+    def texture_desc(cls, tex: Texture) -> tuple[abi.RtTextureDesc, "torch.Tensor"]:
+        """Uploads a texture; returns its descriptor and the buffer to keep alive."""
+        buf = cls.upload(tex.texels)
         d = abi.RtTextureDesc()
         d.address = buf.data_ptr()
         d.height, d.width = tex.texels.shape[0], tex.texels.shape[1]
         d.row_pitch = tex.row_pitch
         d.format = tex.format
         d.filter = tex.filter
+        return d, buf
+
+    def set_texture(self, index: int, tex: Texture) -> None:
+        d, buf = self.texture_desc(tex)
         self.check(self.lib.rt_ctx_set_texture(self.ctx, index, C.byref(d)))
         self._texture_refs[index] = buf
 
@@ -257,7 +263,10 @@ class GpuScene:
 
     def __init__(self, device: Device, scene: Scene, scratch: ScratchBuffer | None = None,
                  tlas_flags: int = abi.RT_BUILD_PREFER_FAST_TRACE | abi.RT_BUILD_ALLOW_UPDATE, stream=None,
-                 blas_flags: int = abi.RT_BUILD_PREFER_FAST_TRACE):
+                 blas_flags: int = abi.RT_BUILD_PREFER_FAST_TRACE, own_textures: bool = False):
+        """own_textures: keep the scene's bindless table in its own device array
+        (for batched rendering of scenes with different textures) instead of
+        binding the textures into the context's table."""
         self.device = device
         self.scene = scene
         self.scratch = scratch or ScratchBuffer("scene scratch")
@@ -265,7 +274,17 @@ class GpuScene:
                        for i, m in enumerate(scene.models)]
         infos = np.array([m.model_info() for m in self.models], abi.MODEL_INFO_DTYPE)
         self.model_info_buffer = Device.upload(infos)
-        ImageManager(device).push_images(scene.textures)
+        self.texture_table, self.texture_count, self._texture_refs = None, 0, []
+        if own_textures:
+            n = max(scene.textures) + 1 if scene.textures else 1
+            table = (abi.RtTextureDesc * n)()
+            for idx, tex in scene.textures.items():
+                table[idx], buf = Device.texture_desc(tex)
+                self._texture_refs.append(buf)
+            self.texture_table = Device.upload(np.frombuffer(bytes(table), np.uint8))
+            self.texture_count = n
+        else:
+            ImageManager(device).push_images(scene.textures)
         self.num_instances = len(scene.instances)
         self.instances_host = self.patch_instances(scene.instances)
         self.instances_buffer = Device.upload(self.instances_host)
@@ -322,6 +341,34 @@ class PerFrameResources:
         sbt_p = C.byref(sbt) if sbt is not None else None
         self.device.check(self.device.lib.rt_cmd_trace_rays(self.device.ctx, C.byref(push), sbt_p, C.byref(d),
                                                             Device.stream_handle(stream)))
+
+
+def batch_scene(frame: PerFrameResources, max_trace_depth: int, shadow_ray_count: int,
+                flags: int = 0) -> abi.RtBatchScene:
+    """The RtBatchScene of one frame (its scene's own texture table, if any)."""
+    b = abi.RtBatchScene()
+    b.push = frame.gpu_scene.push_constants(frame.uniforms_buffer.data_ptr(), frame.tlas)
+    gs = frame.gpu_scene
+    if gs.texture_table is not None:
+        b.texture_table = gs.texture_table.data_ptr()
+        b.texture_count = gs.texture_count
+    d = b.desc
+    d.width, d.height = frame.width, frame.height
+    d.max_trace_depth = max_trace_depth
+    d.shadow_ray_count = shadow_ray_count
+    d.flags = flags
+    d.image_address = frame.image.data_ptr()
+    d.radiance_address = frame.radiance.data_ptr() if frame.radiance is not None else 0
+    return b
+
+
+def trace_batch(device: Device, scenes: list[abi.RtBatchScene], flags: int = 0,
+                sbt: abi.RtShaderBindingTable | None = None, stream=None) -> None:
+    """All frames in one rt_cmd_trace_rays_batched call."""
+    arr = (abi.RtBatchScene * max(len(scenes), 1))(*scenes)
+    sbt_p = C.byref(sbt) if sbt is not None else None
+    device.check(device.lib.rt_cmd_trace_rays_batched(device.ctx, arr, len(scenes), sbt_p, flags,
+                                                      Device.stream_handle(stream)))
 
 
 def render(device: Device, scene: Scene, radiance: bool = True, flags: int = 0, gpu_scene: GpuScene | None = None):

@@ -1,0 +1,144 @@
+"""rt_cmd_trace_rays_batched: several scenes in one set of persistent launches.
+
+Each scene keeps its own TLAS, uniforms, texture table, size, trace depth and
+shadow-ray count; every output must be identical, byte for byte, to what
+rt_cmd_trace_rays renders for that scene alone (same kernels, same arithmetic,
+only the ray lists are shared), and one scene is also checked against the
+oracle.  A CUDA graph capture of a batched call replays to the same images.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from rtgallery import abi, scenes
+
+pytestmark = pytest.mark.gpu
+
+
+def _host():
+    from rtgallery import host
+
+    return host
+
+
+def _frames(device, specs):
+    """specs: (scene, depth, shadows); returns [(frame, depth, shadows)]."""
+    host = _host()
+    out = []
+    for sc, depth, shadows in specs:
+        gs = host.GpuScene(device, sc, own_textures=True)
+        fr = host.PerFrameResources(device, gs, sc.width, sc.height, radiance=True)
+        fr.write_uniforms(sc.uniforms)
+        out.append((fr, depth, shadows))
+    return out
+
+
+def _specs():
+    return [
+        (scenes.scene_small(96, 64), 1, 1),
+        (scenes.scene_gallery(160, 100), 3, 2),
+        (scenes.scene_full(3, 200, 120), 2, 4),
+        (scenes.scene_small(33, 17), 2, 0),
+        (scenes.scene_gallery(64, 40), 2, 8),
+    ]
+
+
+def _alone(device, frames):
+    """Each frame rendered by its own rt_cmd_trace_rays call (its textures bound
+    into the context's table first)."""
+    import torch
+
+    host = _host()
+    imgs = []
+    for fr, depth, shadows in frames:
+        host.ImageManager(device).push_images(fr.gpu_scene.scene.textures)
+        fr.image.zero_()
+        fr.radiance.zero_()
+        fr.record(depth, shadows)
+        torch.cuda.synchronize()
+        imgs.append((fr.image.clone(), fr.radiance.clone()))
+    return imgs
+
+
+def test_batch_matches_individual_frames(device):
+    import torch
+
+    host = _host()
+    frames = _frames(device, _specs())
+    alone = _alone(device, frames)
+    device.read_stats(reset=True)
+    for fr, _, _ in frames:
+        fr.image.zero_()
+        fr.radiance.zero_()
+    host.trace_batch(device, [host.batch_scene(fr, d, s) for fr, d, s in frames], abi.RT_TRACE_FLAG_COLLECT_STATS)
+    torch.cuda.synchronize()
+    st = device.read_stats(reset=True)
+    assert st["status"] == 0
+    for k, ((fr, d, s), (img, rad)) in enumerate(zip(frames, alone)):
+        assert torch.equal(fr.image, img), f"scene {k}: image differs from its own launch"
+        assert torch.equal(fr.radiance, rad), f"scene {k}: radiance differs from its own launch"
+    # the traversal counts add up to the oracle's for every scene
+    want = 0
+    for (fr, d, s) in frames:
+        sc = fr.gpu_scene.scene
+        _, _, o_st = O.OracleScene(sc).render(max_trace_depth=d, shadow_ray_count=s)
+        want += o_st["traversals"]
+    assert st["traversals"] == want
+
+
+def test_batch_scene_matches_oracle(device):
+    import torch
+
+    host = _host()
+    sc = scenes.scene_gallery(120, 80)
+    other = scenes.scene_full(1, 64, 48)
+    frames = _frames(device, [(other, 2, 4), (sc, 3, 2), (other, 1, 1)])
+    host.trace_batch(device, [host.batch_scene(fr, d, s) for fr, d, s in frames])
+    torch.cuda.synchronize()
+    o_img, o_rad, _ = O.OracleScene(sc).render(max_trace_depth=3, shadow_ray_count=2)
+    rad = frames[1][0].radiance.cpu().numpy()
+    img = frames[1][0].image.cpu().numpy()
+    assert np.abs(rad - o_rad).max() <= 1e-3
+    assert np.abs(img.astype(int) - o_img.astype(int)).max() <= 1
+
+
+def test_batch_graph_replay(device):
+    import torch
+
+    host = _host()
+    frames = _frames(device, _specs()[:3])
+    batch = [host.batch_scene(fr, d, s) for fr, d, s in frames]
+    stream = torch.cuda.Stream()
+    with torch.cuda.stream(stream):
+        host.trace_batch(device, batch, stream=stream)  # sizes the stream's workspace outside the capture
+    stream.synchronize()
+    direct = [fr.image.clone() for fr, _, _ in frames]
+    for fr, _, _ in frames:
+        fr.image.zero_()
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=stream):
+        host.trace_batch(device, batch, stream=stream)
+    for _ in range(2):
+        for fr, _, _ in frames:
+            fr.image.zero_()
+        g.replay()
+        torch.cuda.synchronize()
+        for k, (fr, _, _) in enumerate(frames):
+            assert torch.equal(fr.image, direct[k]), f"scene {k} differs after graph replay"
+
+
+def test_batch_rejects_bad_scenes(device):
+    host = _host()
+    frames = _frames(device, _specs()[:2])
+    good = [host.batch_scene(fr, d, s) for fr, d, s in frames]
+    bad = host.batch_scene(frames[0][0], 1, 1)
+    bad.texture_count = abi.RT_MAX_BOUND_IMAGES + 1
+    with pytest.raises(abi.RtError) as e:
+        host.trace_batch(device, [good[0], bad])
+    assert e.value.status == abi.RT_ERR_INVALID
+    bad = host.batch_scene(frames[0][0], 0, 1)
+    with pytest.raises(abi.RtError):
+        host.trace_batch(device, [bad, good[1]])
+    host.trace_batch(device, [])  # an empty batch is a no-op
+    host.trace_batch(device, good)  # and a good batch still works after the rejected ones
