@@ -65,9 +65,10 @@ def parse_args():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--width", type=int, default=WIDTH)
     p.add_argument("--height", type=int, default=HEIGHT)
-    p.add_argument("--workload", default="frame", choices=["frame", "precision"],
+    p.add_argument("--workload", default="frame", choices=["frame", "precision", "batch"],
                    help="frame: the full 1080p frame (default); precision: 10,485,760-triangle icosphere, "
-                        "4M random rays, quantised vs FP32 nodes")
+                        "4M random rays, quantised vs FP32 nodes; batch: 64 scenes in one batched launch")
+    p.add_argument("--batch-scenes", type=int, default=64, help=argparse.SUPPRESS)
     p.add_argument("--precision-level", type=int, default=9, help=argparse.SUPPRESS)
     p.add_argument("--precision-rays", type=int, default=PRECISION_RAYS, help=argparse.SUPPRESS)
     return p.parse_args()
@@ -607,9 +608,259 @@ def bench_precision(args):
         dist.destroy_process_group()
 
 
+BATCH_WORKLOAD = ("batch: 64 independent scenes (procedural torus + displaced UV sphere + ground grid, unique "
+                  "triangles log-uniform in [10k, 2M], resolutions from {128^2, 256^2, 512^2, 1024^2, 1920x1080}), "
+                  "primary + 2 blue-noise soft shadows + 1 reflection bounce each, one batched launch sequence "
+                  "replayed from a CUDA graph")
+
+
+def batch_setup(dev, count):
+    from rtgallery import host
+
+    scs = scenes.batch_scenes(count)
+    frames = []
+    for sc in scs:
+        gs = host.GpuScene(dev, sc, own_textures=True)
+        fr = host.PerFrameResources(dev, gs, sc.width, sc.height)
+        fr.write_uniforms(sc.uniforms)
+        frames.append(fr)
+    return scs, frames
+
+
+def batch_cpu(scs, budget_s: float = 12.0) -> dict:
+    """The oracle (FP32, all host threads) rendering row bands of the batch's
+    scenes in turn until about `budget_s` seconds of CPU work."""
+    from oracle.oracle import OracleScene, default_threads
+
+    threads = default_threads()
+    rays, t_total, done = 0, 0.0, 0
+    for sc in scs:
+        o = OracleScene(sc)
+        band = max(4, sc.height // 16)
+        t = time.perf_counter()
+        _, _, st = o.render(rows=(0, band), threads=threads)
+        t_total += time.perf_counter() - t
+        rays += st["traversals"]
+        done += 1
+        if t_total >= budget_s:
+            break
+    return {"value": rays / t_total / 1e6, "unit": "Mrays/s", "cores": threads, "kind": "port",
+            "sample": f"first 1/16 of the rows of {done} of the {len(scs)} scenes ({rays} traversals, {t_total:.1f} s)"}
+
+
+def bench_batch_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    from oracle.oracle import OracleScene, default_threads
+
+    threads = default_threads()
+    scs = scenes.batch_scenes(args.batch_scenes)
+    times, rays = [], 0
+    for k in range(args.warmup + args.steps):
+        sc = scs[k % len(scs)]
+        o = OracleScene(sc)
+        band = max(4, sc.height // 32)
+        y0 = (k * band) % max(1, sc.height - band)
+        t = time.perf_counter()
+        _, _, st = o.render(rows=(y0, y0 + band), threads=threads)
+        dt = time.perf_counter() - t
+        if k >= args.warmup:
+            times.append(dt)
+            rays += st["traversals"]
+    total = sum(times)
+    value = rays / total / 1e6
+    print(json.dumps({
+        "impl": "reference", "metric": "Mrays/s", "value": value, "unit": "Mrays/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": BATCH_WORKLOAD, "sample": "a 1/32 row band of one scene per step"},
+        "cpu_baseline": {"value": value, "unit": "Mrays/s", "cores": threads, "kind": "port",
+                         "sample": f"1/32 row band of one scene per step, {args.steps} steps"},
+        "e2e": {"value": value, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+
+
+def bench_batch(args):
+    """64 scenes per step: per-scene launches vs one batched launch sequence,
+    direct and replayed from a CUDA graph."""
+    import torch
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    from rtgallery import host
+
+    dev = host.Device()
+    lib = dev.lib
+    t0 = time.perf_counter()
+    scs, frames = batch_setup(dev, args.batch_scenes)
+    torch.cuda.synchronize()
+    setup_s = time.perf_counter() - t0
+    stream = torch.cuda.Stream()
+    sh = host.Device.stream_handle(stream)
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    items = [host.batch_scene(fr, sc.max_trace_depth, sc.shadow_ray_count) for fr, sc in zip(frames, scs)]
+    arr = (abi.RtBatchScene * len(items))(*items)
+    singles = [(abi.RtBatchScene * 1)(it) for it in items]
+
+    def batched(flags=0):
+        dev.check(lib.rt_cmd_trace_rays_batched(dev.ctx, arr, len(items), None, flags, sh))
+
+    def per_scene():
+        for one in singles:
+            dev.check(lib.rt_cmd_trace_rays_batched(dev.ctx, one, 1, None, 0, sh))
+
+    def timed(fn, steps):
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        with torch.cuda.stream(stream):
+            for i in range(steps):
+                flush.fill_(i & 0xFF)
+                ev[i][0].record(stream)
+                fn()
+                ev[i][1].record(stream)
+        torch.cuda.synchronize()
+        return sum(a.elapsed_time(b) for a, b in ev)
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            per_scene()
+            batched()
+    torch.cuda.synchronize()
+    dev.read_stats(reset=True)
+    with torch.cuda.stream(stream):
+        batched()
+    torch.cuda.synchronize()
+    rays_per_step = dev.read_stats(reset=True)["traversals"]
+
+    # untuned: per-scene launches and one batched launch, the default traversal configuration
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    ms_single = timed(per_scene, args.steps)
+    ms_batch = timed(batched, args.steps)
+
+    # the autotuner picks the traversal launch shape on this batch, then the graph is captured with it
+    report = abi.RtAutotuneReport()
+    t_tune = time.perf_counter()
+    dev.check(lib.rt_ctx_autotune(dev.ctx, arr, len(items), None, 3, sh, C.byref(report)))
+    tune_s = time.perf_counter() - t_tune
+    tuned = report.configs[report.best]
+    default_ms = [report.median_ms[i] for i in range(report.count)
+                  if report.configs[i].as_tuple() == (128, 0, 20)][0]
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph, stream=stream):
+        batched()
+    for _ in range(args.warmup):
+        graph.replay()
+    torch.cuda.synchronize()
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    l0 = lib.rt_kernel_launch_count()
+    batched()
+    launches_per_step = lib.rt_kernel_launch_count() - l0
+    ms_graph = timed(graph.replay, args.steps)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clk = clocks.stop()
+    if dist:
+        t = torch.tensor([ms_graph], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_graph = float(t.item())
+    value = rays_per_step * world * args.steps / (ms_graph / 1e3) / 1e6
+
+    # kernel split and roofline of the traversal (a direct call with per-kernel events)
+    with torch.cuda.stream(stream):
+        batched(abi.RT_TRACE_FLAG_KERNEL_TIMINGS)
+    tt = abi.RtTraceTimings()
+    dev.check(lib.rt_ctx_read_trace_timings(dev.ctx, C.byref(tt)))
+    kt = tt.as_dict()
+    torch.cuda.synchronize()
+    dev.read_stats(reset=True)
+    with torch.cuda.stream(stream):
+        batched(abi.RT_TRACE_FLAG_COLLECT_STATS)
+    torch.cuda.synchronize()
+    s = dev.read_stats(reset=True)
+    bytes_step = (s["traversals"] * (RAY_BYTES + HIT_BYTES) + s["nodes_visited"] * NODE_BYTES +
+                  s["triangles_tested"] * TRI_BYTES + s["instances_visited"] * INST_BYTES)
+    achieved = bytes_step / (kt["trace_ms"] / 1e3) / 1e9
+    peak, peak_kind = measured_peaks()
+
+    # end to end: uniforms in from pinned host memory, every image out, graph replay
+    uni_host = torch.from_numpy(np.concatenate([np.frombuffer(bytes(sc.uniforms), np.uint8) for sc in scs])).pin_memory()
+    img_host = [torch.empty_like(fr.image, device="cpu").pin_memory() for fr in frames]
+    usz = C.sizeof(abi.RtUniforms)
+    e2e_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with torch.cuda.stream(stream):
+        for i in range(args.steps):
+            flush.fill_(i & 0xFF)
+            e2e_ev[i][0].record(stream)
+            for k, fr in enumerate(frames):
+                fr.uniforms_buffer.copy_(uni_host[k * usz:(k + 1) * usz], non_blocking=True)
+            graph.replay()
+            for k, fr in enumerate(frames):
+                img_host[k].copy_(fr.image, non_blocking=True)
+            e2e_ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = sum(a.elapsed_time(b) for a, b in e2e_ev)
+    e2e_value = rays_per_step * world * args.steps / (e2e_ms / 1e3) / 1e6
+    cpu = batch_cpu(scs) if rank == 0 and not args.no_cpu_baseline else None
+    if rank == 0:
+        pixels = sum(sc.width * sc.height for sc in scs)
+        print(json.dumps({
+            "metric": "Mrays/s", "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_graph / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (procedural scenes from seeds)",
+            "config": {"workload": BATCH_WORKLOAD, "scenes": len(scs), "pixels_per_step": pixels,
+                       "unique_triangles": int(sum(m.triangle_count for sc in scs for m in sc.models)),
+                       "traversals_per_step": rays_per_step, "parallelism": f"replicas x{world}",
+                       "l2": "flushed between steps (256 MiB write outside the timed events)",
+                       "per_scene_launches_mrays_s": rays_per_step * args.steps / (ms_single / 1e3) / 1e6,
+                       "batched_direct_mrays_s": rays_per_step * args.steps / (ms_batch / 1e3) / 1e6,
+                       "batched_graph_mrays_s": value,
+                       "autotuned_config": {"block_size": tuned.block_size,
+                                            "shared_stack_depth": tuned.shared_stack_depth,
+                                            "leaf_wait": tuned.leaf_wait},
+                       "autotune_configs": int(report.count), "autotune_s": tune_s,
+                       "autotune_best_ms": report.median_ms[report.best], "autotune_default_config_ms": default_ms,
+                       "speedup_graph_batch_over_per_scene": ms_single / ms_graph,
+                       "kernel_launches_per_step": launches_per_step, "scene_setup_s": setup_s,
+                       "trace_ms_per_step": kt["trace_ms"], "shade_ms_per_step": kt["shade_ms"],
+                       "pipeline_ms_per_step": kt["total_ms"]},
+            "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": usz * len(scs),
+                    "d2h_bytes_per_step": pixels * 4},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": None, "kernel": "k_trace (all traversal launches of the batch)",
+                         "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
+                         else "fallback 6.8 TB/s",
+                         "algorithmic_bytes_per_step": bytes_step,
+                         "bytes_per_ray": bytes_step / max(1, s["traversals"]),
+                         "nodes_per_ray": s["nodes_visited"] / max(1, s["traversals"])},
+            "cpu_baseline": cpu,
+            "clocks": clk,
+            "gpu_launches": int(launches_per_step) * args.steps,
+        }))
+    dev.close()
+    if dist:
+        dist.destroy_process_group()
+
+
 def main():
     args = parse_args()
-    if args.workload == "precision":
+    if args.workload == "batch":
+        if args.impl == "reference":
+            bench_batch_reference(args)
+        else:
+            bench_batch(args)
+    elif args.workload == "precision":
         if args.impl == "reference":
             bench_precision_reference(args)
         else:

@@ -417,6 +417,42 @@ typedef struct RtBatchScene {
  * 2^31 shadow rays per batch. */
 RTCORE_API int32_t rt_cmd_trace_rays_batched(rt_ctx* ctx, const RtBatchScene* scenes, uint32_t scene_count,
                                              const RtShaderBindingTable* sbt, uint32_t flags, void* stream);
+
+/* Launch shape of the wavefront traversal kernels (rt_cmd_trace_rays and
+ * rt_cmd_trace_rays_batched).  Every configuration gives identical results;
+ * they differ only in speed.  No counterpart in the reference (the driver
+ * schedules its own traversal).
+ *   block_size          threads per block: 64, 128 or 256 (24 warps per SM each)
+ *   shared_stack_depth  traversal-stack entries kept in shared memory: 0, 16,
+ *                       24 or 32 (the rest of the 64 live in local memory)
+ *   leaf_wait           0..32: a warp runs leaf steps once leaf_wait/32 of its
+ *                       lanes wait on one, else node steps
+ * Default {128, 0, 20}. */
+typedef struct RtTraversalConfig {
+    uint32_t block_size;
+    uint32_t shared_stack_depth;
+    uint32_t leaf_wait;
+    uint32_t _padding;
+} RtTraversalConfig;
+RTCORE_API int32_t rt_ctx_set_traversal_config(rt_ctx* ctx, const RtTraversalConfig* config);
+RTCORE_API int32_t rt_ctx_get_traversal_config(rt_ctx* ctx, RtTraversalConfig* out);
+
+#define RT_AUTOTUNE_MAX_CONFIGS 64u
+typedef struct RtAutotuneReport {
+    uint32_t count;                                  /* configurations timed */
+    uint32_t best;                                   /* index of the fastest */
+    RtTraversalConfig configs[RT_AUTOTUNE_MAX_CONFIGS];
+    float median_ms[RT_AUTOTUNE_MAX_CONFIGS];        /* of `reps` batched launches each */
+} RtAutotuneReport;
+/* Times rt_cmd_trace_rays_batched(scenes) under every traversal
+ * configuration (block size x shared stack depth x leaf_wait in {16, 20,
+ * 24}), `reps` timed launches each after one warm-up, and makes the fastest
+ * the context's configuration.  Synchronises `stream`; not allowed while it
+ * is being captured.  The scenes' output buffers are overwritten.  `report`
+ * may be NULL. */
+RTCORE_API int32_t rt_ctx_autotune(rt_ctx* ctx, const RtBatchScene* scenes, uint32_t scene_count,
+                                   const RtShaderBindingTable* sbt, uint32_t reps, void* stream,
+                                   RtAutotuneReport* report);
 /* Traversal only: one traceRay per RtRay against `tlas`, writing RtHit.
  * `push` may be NULL (then any-hit programs cannot run and candidates are
  * accepted as if opaque). */

@@ -212,6 +212,23 @@ class RtBatchScene(C.Structure):
 RT_MAX_BATCH_SCENES = 65536
 
 
+class RtTraversalConfig(C.Structure):
+    _fields_ = [("block_size", C.c_uint32), ("shared_stack_depth", C.c_uint32), ("leaf_wait", C.c_uint32),
+                ("_padding", C.c_uint32)]
+
+    def as_tuple(self) -> tuple:
+        return (self.block_size, self.shared_stack_depth, self.leaf_wait)
+
+
+RT_AUTOTUNE_MAX_CONFIGS = 64
+
+
+class RtAutotuneReport(C.Structure):
+    _fields_ = [("count", C.c_uint32), ("best", C.c_uint32),
+                ("configs", RtTraversalConfig * RT_AUTOTUNE_MAX_CONFIGS),
+                ("median_ms", C.c_float * RT_AUTOTUNE_MAX_CONFIGS)]
+
+
 class RtRay(C.Structure):
     _fields_ = [("origin", C.c_float * 3), ("tmin", C.c_float), ("direction", C.c_float * 3), ("tmax", C.c_float)]
 
@@ -303,6 +320,10 @@ EXPORTED_FUNCTIONS = {
                                        C.POINTER(RtShaderBindingTable), C.POINTER(RtTraceRaysDesc), C.c_void_p]),
     "rt_cmd_trace_rays_batched": (C.c_int32, [C.c_void_p, C.POINTER(RtBatchScene), C.c_uint32,
                                                C.POINTER(RtShaderBindingTable), C.c_uint32, C.c_void_p]),
+    "rt_ctx_set_traversal_config": (C.c_int32, [C.c_void_p, C.POINTER(RtTraversalConfig)]),
+    "rt_ctx_get_traversal_config": (C.c_int32, [C.c_void_p, C.POINTER(RtTraversalConfig)]),
+    "rt_ctx_autotune": (C.c_int32, [C.c_void_p, C.POINTER(RtBatchScene), C.c_uint32, C.POINTER(RtShaderBindingTable),
+                                     C.c_uint32, C.c_void_p, C.POINTER(RtAutotuneReport)]),
     "rt_cmd_trace_ray_buffer": (C.c_int32, [C.c_void_p, C.c_uint64, C.POINTER(RtPushConstantBufferAddresses),
                                              C.POINTER(RtShaderBindingTable), C.c_uint32, C.c_uint32, C.c_uint32,
                                              C.c_uint64, C.c_uint32, C.c_uint64, C.c_void_p]),
@@ -388,3 +409,5 @@ def check_layouts() -> None:
     assert C.sizeof(RtTraceRaysDesc) == 40
     assert C.sizeof(RtTraceTimings) == 32
     assert C.sizeof(RtBatchScene) == 80 and RtBatchScene.desc.offset == 40
+    assert C.sizeof(RtTraversalConfig) == 16
+    assert C.sizeof(RtAutotuneReport) == 8 + 64 * 16 + 64 * 4

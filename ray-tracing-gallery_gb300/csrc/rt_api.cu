@@ -5,6 +5,7 @@
 // with a message in rt_last_error_string() and launches nothing.  Errors the
 // device finds (a stack overflow, an out-of-range vertex index) are recorded
 // in the AS header's status word or the context's statistics block.
+#include <algorithm>
 #include <atomic>
 #include <cstdarg>
 #include <cstdio>
@@ -95,6 +96,7 @@ struct rt_ctx {
     std::mutex mu;
     std::vector<Workspace> workspaces;
     KernelTimer timer;
+    RtTraversalConfig traversal{128, 0, 20, 0};
 };
 
 namespace {
@@ -559,6 +561,7 @@ int32_t trace_scenes(rt_ctx* ctx, const std::vector<TraceScene>& scenes, const R
     b.stats_dev = &ctx->dev->stats;
     b.status = &ctx->dev->stats.status;
     b.kinds_built = blas_kinds_built();
+    b.config = ctx->traversal;
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     uint8_t* ws = nullptr;
     cudaError_t e = ctx_workspace(ctx, s, trace_workspace_bytes(b.scenes, b.count), &ws);
@@ -622,6 +625,84 @@ RTCORE_API int32_t rt_cmd_trace_rays_batched(rt_ctx* ctx, const RtBatchScene* sc
         v[i]._pad = 0;
     }
     return trace_scenes(ctx, v, sbt, flags, stream, "rt_cmd_trace_rays_batched");
+}
+
+RTCORE_API int32_t rt_ctx_set_traversal_config(rt_ctx* ctx, const RtTraversalConfig* config) {
+    if (!ctx || !config) return fail(RT_ERR_INVALID, "ctx or config is NULL");
+    if (!traversal_config_supported(*config))
+        return fail(RT_ERR_UNSUPPORTED, "traversal config {%u, %u, %u} is not built (block 64/128/256, shared stack "
+                    "depth 0/16/24/32, leaf_wait <= 32)", config->block_size, config->shared_stack_depth,
+                    config->leaf_wait);
+    MaybeLock l(ctx);
+    ctx->traversal = *config;
+    ctx->traversal._padding = 0;
+    return RT_OK;
+}
+
+RTCORE_API int32_t rt_ctx_get_traversal_config(rt_ctx* ctx, RtTraversalConfig* out) {
+    if (!ctx || !out) return fail(RT_ERR_INVALID, "ctx or out is NULL");
+    MaybeLock l(ctx);
+    *out = ctx->traversal;
+    return RT_OK;
+}
+
+RTCORE_API int32_t rt_ctx_autotune(rt_ctx* ctx, const RtBatchScene* scenes, uint32_t scene_count,
+                                   const RtShaderBindingTable* sbt, uint32_t reps, void* stream,
+                                   RtAutotuneReport* report) {
+    if (!ctx || !scenes || scene_count == 0) return fail(RT_ERR_INVALID, "ctx or scenes is NULL / empty");
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    if (stream_capturing(s)) return fail(RT_ERR_INVALID, "rt_ctx_autotune cannot run inside a stream capture");
+    reps = std::max(1u, std::min(reps, 64u));
+    static const uint32_t kBlocks[] = {64, 128, 256}, kDepths[] = {0, 16, 24, 32}, kWaits[] = {16, 20, 24};
+    std::vector<RtTraversalConfig> cands;
+    for (uint32_t b : kBlocks)
+        for (uint32_t d : kDepths)
+            for (uint32_t w : kWaits) cands.push_back(RtTraversalConfig{b, d, w, 0});
+    const RtTraversalConfig saved = ctx->traversal;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaError_t ce = cudaEventCreate(&e0);
+    if (ce == cudaSuccess) ce = cudaEventCreate(&e1);
+    if (ce != cudaSuccess) return cuda_fail(ce, "rt_ctx_autotune (events)");
+    std::vector<float> med(cands.size(), 0.0f);
+    int32_t r = RT_OK;
+    for (size_t i = 0; i < cands.size() && r == RT_OK; i++) {
+        ctx->traversal = cands[i];
+        std::vector<float> t;
+        for (uint32_t k = 0; k <= reps && r == RT_OK; k++) {
+            ce = cudaEventRecord(e0, s);
+            if (ce == cudaSuccess) r = rt_cmd_trace_rays_batched(ctx, scenes, scene_count, sbt, 0, stream);
+            if (r == RT_OK && ce == cudaSuccess) ce = cudaEventRecord(e1, s);
+            if (r == RT_OK && ce == cudaSuccess) ce = cudaEventSynchronize(e1);
+            float ms = 0.0f;
+            if (r == RT_OK && ce == cudaSuccess) ce = cudaEventElapsedTime(&ms, e0, e1);
+            if (ce != cudaSuccess) r = cuda_fail(ce, "rt_ctx_autotune");
+            if (k > 0) t.push_back(ms);  // the first run is the warm-up
+        }
+        if (r == RT_OK) {
+            std::sort(t.begin(), t.end());
+            med[i] = t[t.size() / 2];
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (r != RT_OK) {
+        ctx->traversal = saved;
+        return r;
+    }
+    size_t best = 0;
+    for (size_t i = 1; i < cands.size(); i++)
+        if (med[i] < med[best]) best = i;
+    ctx->traversal = cands[best];
+    if (report) {
+        memset(report, 0, sizeof *report);
+        report->count = (uint32_t)std::min<size_t>(cands.size(), RT_AUTOTUNE_MAX_CONFIGS);
+        report->best = (uint32_t)best;
+        for (uint32_t i = 0; i < report->count; i++) {
+            report->configs[i] = cands[i];
+            report->median_ms[i] = med[i];
+        }
+    }
+    return RT_OK;
 }
 
 RTCORE_API int32_t rt_cmd_trace_ray_buffer(rt_ctx* ctx, uint64_t tlas, const RtPushConstantBufferAddresses* push,

@@ -82,7 +82,10 @@ struct TraceBatch {
     RtStats* stats_dev;             // device
     uint32_t* status;               // device (same block)
     uint32_t kinds_built;           // blas_kinds_built() when the launch was recorded
+    RtTraversalConfig config;       // launch shape of the traversal kernels
 };
+// Whether the traversal kernels are built for `c` (block size, shared stack depth, leaf_wait <= 32).
+bool traversal_config_supported(const RtTraversalConfig& c);
 // Bytes of the wavefront workspace a batch needs.
 uint64_t trace_workspace_bytes(const TraceScene* scenes, uint32_t count);
 

@@ -61,16 +61,18 @@ constexpr int kMaxDepth = 64;
 // node steps (lanes whose next entry is an internal node) or the other steps
 // (leaves, instance entries, TLAS returns), so a warp never pays for both
 // branch bodies in one iteration.  Lanes wait for their phase: the warp
-// switches to the leaf phase once RT_TRACE_LEAF_WAIT/32 of its active lanes
-// wait on one (or no lane has a node).  -1 = no phases: every lane takes its
-// own step each iteration.
+// switches to the leaf phase once leaf_wait/32 of its active lanes wait on
+// one (or no lane has a node).  The default; the wavefront launches take it
+// from the context's traversal configuration.
 #ifndef RT_TRACE_LEAF_WAIT
 #define RT_TRACE_LEAF_WAIT 20
 #endif
+// Resident warps per SM every trace kernel variant is compiled for (at most
+// 80 registers a thread); block size x blocks per SM = 24 warps.
+constexpr int kTraceWarpsPerSM = 24;
 
 constexpr int kModeBounce = 0;   // closest hit of a bounce list -> hit records
 constexpr int kModeShadow = 1;   // any hit of generated shadow rays -> lit counters
-constexpr int kModeRayBuf = 2;   // the API's RtRay -> RtHit query
 
 // Work counters of one lane (RT_TRACE_FLAG_COLLECT_STATS launches only).
 struct Counters {
@@ -194,10 +196,27 @@ __device__ __forceinline__ void trav_begin(Trav& s, const Env& e, V3 o, V3 d, fl
     s.entry = (e.tnode_count == 0 || !(tmin <= tmax)) ? kNoEntry : 0u;  // 0 = TLAS root
 }
 
-__device__ __forceinline__ void trav_pop(Trav& s, const uint2* stack) {
+// The traversal stack of one lane: kStackSize entries (node/leaf entry,
+// tnear bits).  The first SD live in shared memory (a column per thread,
+// stride BLOCK, so a warp's accesses are conflict-free), the rest in local
+// memory; SD = 0 keeps all of it local.  The split only moves entries, so
+// every depth gives the same hits; the autotuner picks SD by speed.
+template <int SD, int BLOCK>
+struct TravStack {
+    uint2* sh;                                  // this thread's column in dynamic shared memory
+    uint2 lo[kStackSize - SD];
+    __device__ __forceinline__ void put(int i, uint2 v) {
+        if (SD > 0 && i < SD) sh[i * BLOCK] = v;
+        else lo[i - SD] = v;
+    }
+    __device__ __forceinline__ uint2 get(int i) const { return (SD > 0 && i < SD) ? sh[i * BLOCK] : lo[i - SD]; }
+};
+
+template <class STK>
+__device__ __forceinline__ void trav_pop(Trav& s, const STK& stack) {
     const float cull = s.t * kBoxFarScale;
     while (s.sp > 0) {
-        uint2 en = stack[--s.sp];
+        uint2 en = stack.get(--s.sp);
         if (en.x != kMarker && __uint_as_float(en.y) > cull) continue;
         s.entry = en.x;
         return;
@@ -361,13 +380,14 @@ __device__ __forceinline__ bool is_node_entry(uint32_t entry) {
     return entry != kMarker && (entry & kLeafEntry) == 0u;  // kNoEntry has the leaf bit
 }
 
-// The phase of this iteration for the calling (converged) lanes.
-__device__ __forceinline__ bool node_phase(uint32_t entry) {
+// The phase of this iteration for the calling (converged) lanes: leaves once
+// leaf_wait/32 of them wait on a non-node step (or none has a node).
+__device__ __forceinline__ bool node_phase(uint32_t entry, uint32_t leaf_wait) {
     const unsigned act = __activemask();
     const unsigned nm = __ballot_sync(act, is_node_entry(entry));
     if (nm == 0u) return false;
     if (nm == act) return true;
-    return (uint32_t)__popc(act & ~nm) * 32u < (uint32_t)RT_TRACE_LEAF_WAIT * (uint32_t)__popc(act);
+    return (uint32_t)__popc(act & ~nm) * 32u < leaf_wait * (uint32_t)__popc(act);
 }
 
 // `phase`: 1 = node steps only, 0 = non-node steps only, -1 = any step.
@@ -397,8 +417,8 @@ struct SceneTable {
 // SV maps the ray's scene index to its Env: OneScene (the ray-buffer query,
 // registers) or SceneTable (the wavefront pipeline, one device record per
 // scene; loaded only on instance entry / exit and in leaves).
-template <bool STATS, uint32_t KINDS, class SV>
-__device__ __forceinline__ bool trav_step(Trav& s, uint2* stack, const SV& sv, const RtShaderBindingTable* sbt,
+template <bool STATS, uint32_t KINDS, class SV, class STK>
+__device__ __forceinline__ bool trav_step(Trav& s, STK& stack, const SV& sv, const RtShaderBindingTable* sbt,
                                           uint32_t* status, uint32_t ray_flags, uint32_t cull_mask,
                                           uint32_t ray_sbt_offset, Counters& cnt, int phase) {
     const uint32_t entry = s.entry;
@@ -430,7 +450,7 @@ __device__ __forceinline__ bool trav_step(Trav& s, uint2* stack, const SV& sv, c
                 for (int q = 7; q >= 1; q--) {
                     uint32_t key = keys[q];
                     if (key == 0xFFFFFFFFu) continue;
-                    if (s.sp < (int)kStackSize) stack[s.sp++] = make_uint2(pick8(refs, key & 7u), key & ~7u);
+                    if (s.sp < (int)kStackSize) stack.put(s.sp++, make_uint2(pick8(refs, key & 7u), key & ~7u));
                     else atomicOr(status, 1u << RT_ERR_STACK_OVERFLOW);
                 }
                 s.entry = pick8(refs, keys[0] & 7u);
@@ -473,7 +493,7 @@ __device__ __forceinline__ bool trav_step(Trav& s, uint2* stack, const SV& sv, c
                 s.c_sbt_flags = q1.x;
                 s.in_blas = true;
                 if (s.sp < (int)kStackSize) {
-                    stack[s.sp++] = make_uint2(kMarker, 0u);
+                    stack.put(s.sp++, make_uint2(kMarker, 0u));
                     s.entry = 0;  // BLAS root
                     return false;
                 }
@@ -600,6 +620,7 @@ struct WfParams {
     uint32_t total_pixels;
     uint32_t bounce;
     uint32_t kinds_built;
+    uint32_t leaf_wait;        // phase threshold (node_phase)
 };
 
 // Scene of batch tile / pixel v: the last scene whose first tile / pixel is <= v.
@@ -709,7 +730,7 @@ __global__ void k_raygen(const __grid_constant__ WfParams P) {
 }
 
 // Persistent trace loop with per-lane ray replacement.
-template <int MODE, bool STATS, uint32_t KINDS>
+template <int MODE, bool STATS, uint32_t KINDS, int SD, int BLOCK>
 __device__ __forceinline__ void trace_wavefront(const WfParams& P) {
     const SceneTable sv{P.B.scenes};
     const uint32_t b = P.bounce;
@@ -728,7 +749,11 @@ __device__ __forceinline__ void trace_wavefront(const WfParams& P) {
     const uint32_t sbt_offset = MODE == kModeShadow ? 1u : 0u;
 
     Counters cnt = {0, 0, 0};
-    uint2 stack[kStackSize];
+    TravStack<SD, BLOCK> stack;
+    if (SD > 0) {
+        extern __shared__ uint2 stack_smem[];
+        stack.sh = stack_smem + threadIdx.x;
+    }
     Trav s;
     uint32_t item = kNoItem;
     bool heat = false;
@@ -754,11 +779,7 @@ __device__ __forceinline__ void trace_wavefront(const WfParams& P) {
             heat = pix != kNoPixel && P.B.scenes[sc].uniforms->show_heatmap != 0;
             if (heat) t0 = (uint32_t)clock();
         }
-#if RT_TRACE_LEAF_WAIT < 0
-        const int phase = -1;
-#else
-        const int phase = node_phase(s.entry) ? 1 : 0;
-#endif
+        const int phase = node_phase(s.entry, P.leaf_wait) ? 1 : 0;
         if (!trav_step<STATS, KINDS>(s, stack, sv, &P.sbt, P.status, ray_flags, 0xFFu, sbt_offset, cnt, phase))
             continue;
         // the ray is finished
@@ -788,9 +809,9 @@ __device__ __forceinline__ bool kinds_selected(uint32_t kinds_built, uint32_t tl
     return (tlas_kinds ? tlas_kinds : kBlasKindF32) == kinds;
 }
 
-template <int MODE, bool STATS, uint32_t KINDS>
-__global__ void __launch_bounds__(kTraceThreads, RT_TRACE_MIN_BLOCKS) k_trace(const __grid_constant__ WfParams P) {
-    if (kinds_selected(P.kinds_built, P.B.ctr->kinds, KINDS)) trace_wavefront<MODE, STATS, KINDS>(P);
+template <int MODE, bool STATS, uint32_t KINDS, int SD, int BLOCK>
+__global__ void __launch_bounds__(BLOCK, kTraceWarpsPerSM * 32 / BLOCK) k_trace(const __grid_constant__ WfParams P) {
+    if (kinds_selected(P.kinds_built, P.B.ctr->kinds, KINDS)) trace_wavefront<MODE, STATS, KINDS, SD, BLOCK>(P);
 }
 
 // The closest-hit and miss programs for every ray of bounce b.  Every lane
@@ -949,7 +970,7 @@ __device__ __forceinline__ void trace_ray_buffer(const RayBufferParams& P, const
     const RayBufferLaunch& L = P.L;
     const OneScene sv{e};
     Counters cnt = {0, 0, 0};
-    uint2 stack[kStackSize];
+    TravStack<0, kTraceThreads> stack;
     Trav s;
     uint32_t item = kNoItem;
     if (blockIdx.x == 0 && threadIdx.x == 0 && L.count) {
@@ -966,11 +987,7 @@ __device__ __forceinline__ void trace_ray_buffer(const RayBufferParams& P, const
             trav_begin(s, e, mk3(a.x, a.y, a.z), mk3(c.x, c.y, c.z), a.w, c.w);
             s.scene = 0;
         }
-#if RT_TRACE_LEAF_WAIT < 0
-        const int phase = -1;
-#else
-        const int phase = node_phase(s.entry) ? 1 : 0;
-#endif
+        const int phase = node_phase(s.entry, RT_TRACE_LEAF_WAIT) ? 1 : 0;
         if (!trav_step<STATS, KINDS>(s, stack, sv, &L.sbt, L.status, L.ray_flags, L.cull_mask, L.sbt_offset, cnt,
                                      phase))
             continue;
@@ -1062,9 +1079,9 @@ __global__ void k_debug_eval(uint32_t fn, const float* in, float* out, uint32_t 
 }
 
 template <class K>
-int persistent_blocks(K kernel, int threads, int num_sms) {
+int persistent_blocks(K kernel, int threads, int num_sms, size_t smem = 0) {
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, 0) != cudaSuccess || per_sm < 1)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem) != cudaSuccess || per_sm < 1)
         per_sm = 1;
     return per_sm * num_sms;
 }
@@ -1087,19 +1104,46 @@ void for_each_variant(uint32_t kinds_built, F&& f) {
     }
 }
 
-template <int MODE, bool STATS, uint32_t KINDS>
+template <int MODE, bool STATS, uint32_t KINDS, int SD, int BLOCK>
 void launch_trace_kernel(const WfParams& P, int num_sms, cudaStream_t stream) {
+    const auto kern = k_trace<MODE, STATS, KINDS, SD, BLOCK>;
+    constexpr size_t smem = (size_t)SD * BLOCK * sizeof(uint2);
     static int blocks = 0;
-    if (!blocks) blocks = persistent_blocks(k_trace<MODE, STATS, KINDS>, kTraceThreads, num_sms);
-    note_launch(), k_trace<MODE, STATS, KINDS><<<blocks, kTraceThreads, 0, stream>>>(P);
+    if (!blocks) {
+        if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        blocks = persistent_blocks(kern, BLOCK, num_sms, smem);
+    }
+    note_launch(), kern<<<blocks, BLOCK, smem, stream>>>(P);
+}
+
+// The traversal variants the autotuner chooses among: block size x depth of
+// the shared-memory part of the stack (kTraversalConfigs in the same order).
+#define RT_FOR_EACH_TRAVERSAL_VARIANT(X) \
+    X(64, 0) X(64, 16) X(64, 24) X(64, 32) X(128, 0) X(128, 16) X(128, 24) X(128, 32) \
+    X(256, 0) X(256, 16) X(256, 24) X(256, 32)
+
+template <int MODE, uint32_t K>
+void launch_trace_config(const WfParams& P, const RtTraversalConfig& c, bool stats, int num_sms,
+                         cudaStream_t stream) {
+    if (stats) {  // statistics runs use the default variant
+        launch_trace_kernel<MODE, true, K, 0, kTraceThreads>(P, num_sms, stream);
+        return;
+    }
+#define RT_TRACE_CASE(B, D)                                                  \
+    if (c.block_size == B && c.shared_stack_depth == D) {                   \
+        launch_trace_kernel<MODE, false, K, D, B>(P, num_sms, stream);     \
+        return;                                                             \
+    }
+    RT_FOR_EACH_TRAVERSAL_VARIANT(RT_TRACE_CASE)
+#undef RT_TRACE_CASE
+    launch_trace_kernel<MODE, false, K, 0, kTraceThreads>(P, num_sms, stream);
 }
 
 template <int MODE>
-void launch_trace_mode(const WfParams& P, bool stats, int num_sms, cudaStream_t stream) {
+void launch_trace_mode(const WfParams& P, const RtTraversalConfig& c, bool stats, int num_sms, cudaStream_t stream) {
     for_each_variant(P.kinds_built, [&](auto k) {
         constexpr uint32_t K = decltype(k)::value;
-        if (stats) launch_trace_kernel<MODE, true, K>(P, num_sms, stream);
-        else launch_trace_kernel<MODE, false, K>(P, num_sms, stream);
+        launch_trace_config<MODE, K>(P, c, stats, num_sms, stream);
     });
 }
 
@@ -1166,6 +1210,15 @@ struct BatchLayout {
 
 }  // namespace
 
+bool traversal_config_supported(const RtTraversalConfig& c) {
+    if (c.leaf_wait > 32) return false;
+#define RT_TRACE_SUPPORTED(B, D) \
+    if (c.block_size == B && c.shared_stack_depth == D) return true;
+    RT_FOR_EACH_TRAVERSAL_VARIANT(RT_TRACE_SUPPORTED)
+#undef RT_TRACE_SUPPORTED
+    return false;
+}
+
 uint64_t trace_workspace_bytes(const TraceScene* scenes, uint32_t count) {
     return BatchLayout(scenes, count).total;
 }
@@ -1208,6 +1261,7 @@ cudaError_t launch_trace_batch(const TraceBatch& tb, uint8_t* ws, int num_sms, c
     P.total_pixels = (uint32_t)L.pixels;
     P.bounce = 0;
     P.kinds_built = tb.kinds_built;
+    P.leaf_wait = tb.config.leaf_wait;
     cudaError_t err = cudaMemsetAsync(P.B.ctr, 0, sizeof(WfCounters), stream);
     if (err == cudaSuccess) err = cudaMemsetAsync(P.B.lit, 0, L.pixels * 4, stream);
     if (err == cudaSuccess) err = cudaMemsetAsync(P.B.heat, 0, L.pixels * 8, stream);
@@ -1237,13 +1291,13 @@ cudaError_t launch_trace_batch(const TraceBatch& tb, uint8_t* ws, int num_sms, c
     mark(kKernOther);
     for (uint32_t b = 0; b < L.max_depth; b++) {
         P.bounce = b;
-        launch_trace_mode<kModeBounce>(P, stats, num_sms, stream);
+        launch_trace_mode<kModeBounce>(P, tb.config, stats, num_sms, stream);
         mark(kKernClosest);
         note_launch(), k_shade<<<(uint32_t)((L.slots + 127) / 128), 128, 0, stream>>>(P);
         mark(kKernShade);
     }
     if (L.any_shadow) {
-        launch_trace_mode<kModeShadow>(P, stats, num_sms, stream);
+        launch_trace_mode<kModeShadow>(P, tb.config, stats, num_sms, stream);
         mark(kKernShadow);
         note_launch(), k_resolve<<<(uint32_t)((L.pixels + 255) / 256), 256, 0, stream>>>(P);
         mark(kKernOther);

@@ -601,3 +601,56 @@ def single_mesh_scene(model: Model, width: int = 64, height: int = 64) -> Scene:
                       perspective_reversed_infinite_z_vk_inverse(math.radians(60), 1.0, 0.1),
                       -np.asarray(SUN_DIR_CONFIG), 0.0, TEX_BLUE_NOISE, TEX_GGX_LUT)
     return Scene([model], _base_textures(1), inst, u, width, height, name=model.name)
+
+
+BATCH_RESOLUTIONS = ((128, 128), (256, 256), (512, 512), (1024, 1024), (1920, 1080))
+BATCH_TRIS = (10_000, 2_000_000)
+
+
+def scene_batch_member(index: int, seed: int = 23) -> Scene:
+    """One scene of the batched workload: a procedural torus, a displaced UV
+    sphere and a ground grid whose unique triangles total a log-uniform count
+    in [10k, 2M] (split 1/2, 1/3, 1/6), instanced six, four and one times
+    (one torus a mirror); resolution drawn from {128^2, 256^2, 512^2,
+    1024^2, 1920x1080}; primary rays, 2 blue-noise soft shadows (2 deg) and
+    1 reflection bounce.  Everything follows from (seed, index)."""
+    rng = Pcg32(seed * 7919 + index, 0xB7 + index)
+    lo, hi = math.log(BATCH_TRIS[0]), math.log(BATCH_TRIS[1])
+    target = math.exp(lo + (hi - lo) * rng.uniform())
+    width, height = BATCH_RESOLUTIONS[int(rng.next_u32() % len(BATCH_RESOLUTIONS))]
+
+    def grid_dims(tris, aspect):
+        nv = max(3, int(round(math.sqrt(tris / (2.0 * aspect)))))
+        return max(3, int(round(tris / (2.0 * nv)))), nv
+
+    tu, tv = grid_dims(target / 2, 2.0)
+    su, sv = grid_dims(target / 3, 2.0)
+    gx = max(1, int(round(math.sqrt(target / 12))))
+    tor = _model(torus(1.0, 0.35, tu, tv), f"torus{tu}x{tv}",
+                 lambda idx: [Geometry(idx, True, TEX_DIFFUSE_A, TEX_MR_SHINY)])
+    sph = _model(uv_sphere(su, sv, 1.0, 0.05, seed + index), f"sphere{su}x{sv}",
+                 lambda idx: [Geometry(idx, True, TEX_DIFFUSE_B, TEX_MR_DEFAULT)])
+    gp, gn, guv, gi = quad_grid(gx, gx, 40.0, 40.0, 8.0, 8.0)
+    rot = np.array([[1.0, 0.0, 0.0], [0.0, 0.0, -1.0], [0.0, 1.0, 0.0]], np.float32)  # XY grid -> y = 0, normal +y
+    gp = (gp @ rot.T).astype(np.float32)
+    gn = (gn @ rot.T).astype(np.float32)
+    grd = _model((gp, gn, guv, gi), f"ground{gx}x{gx}", lambda idx: [Geometry(idx, True, TEX_DIFFUSE_B, TEX_MR_DEFAULT)])
+    xf, mdl, sbt = [affine(np.eye(3), [0.0, -1.2, -20.0])], [2], [abi.HIT_SHADER_TEXTURED]
+    for k in range(10):
+        t = [rng.uniform_range(-6, 6), rng.uniform_range(-0.5, 2.5), rng.uniform_range(-6, 6)]
+        m = 0 if k < 6 else 1
+        xf.append(affine(random_rotation(rng), t, rng.uniform_range(0.6, 1.6)))
+        mdl.append(m)
+        sbt.append(abi.HIT_SHADER_MIRROR if k == 0 else abi.HIT_SHADER_TEXTURED)
+    inst = instance_records(np.array(xf), np.array(mdl), np.array(mdl), np.array(sbt))
+    a = rng.uniform_range(0.0, 2.0 * math.pi)
+    eye = (12.0 * math.cos(a), rng.uniform_range(4.0, 9.0), 12.0 * math.sin(a))
+    u = make_uniforms(look_at_view_inverse(eye, (0.0, 0.5, 0.0)),
+                      perspective_reversed_infinite_z_vk_inverse(math.radians(60), width / height, 0.1),
+                      -np.asarray(SUN_DIR_CONFIG), math.tan(math.radians(2.0)), TEX_BLUE_NOISE, TEX_GGX_LUT, index)
+    return Scene([tor, sph, grd], _base_textures(seed + index), inst, u, width, height, max_trace_depth=2,
+                 shadow_ray_count=2, name=f"batch-{index}")
+
+
+def batch_scenes(count: int = 64, seed: int = 23) -> list[Scene]:
+    return [scene_batch_member(i, seed) for i in range(count)]

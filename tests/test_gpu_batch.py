@@ -142,3 +142,75 @@ def test_batch_rejects_bad_scenes(device):
         host.trace_batch(device, [bad, good[1]])
     host.trace_batch(device, [])  # an empty batch is a no-op
     host.trace_batch(device, good)  # and a good batch still works after the rejected ones
+
+
+def _images(frames):
+    return [fr.image.clone() for fr, _, _ in frames]
+
+
+def test_every_traversal_config_gives_identical_images(device):
+    import ctypes as C
+
+    import torch
+
+    host = _host()
+    frames = _frames(device, _specs()[:3])
+    batch = [host.batch_scene(fr, d, s) for fr, d, s in frames]
+    host.trace_batch(device, batch)
+    torch.cuda.synchronize()
+    ref = _images(frames)
+    default = abi.RtTraversalConfig()
+    device.check(device.lib.rt_ctx_get_traversal_config(device.ctx, C.byref(default)))
+    assert default.as_tuple() == (128, 0, 20)
+    try:
+        for block in (64, 128, 256):
+            for depth in (0, 16, 24, 32):
+                for wait in (0, 20, 32):
+                    c = abi.RtTraversalConfig(block, depth, wait, 0)
+                    device.check(device.lib.rt_ctx_set_traversal_config(device.ctx, C.byref(c)))
+                    for fr, _, _ in frames:
+                        fr.image.zero_()
+                    host.trace_batch(device, batch)
+                    torch.cuda.synchronize()
+                    for k, (fr, _, _) in enumerate(frames):
+                        assert torch.equal(fr.image, ref[k]), (block, depth, wait, k)
+    finally:
+        device.check(device.lib.rt_ctx_set_traversal_config(device.ctx, C.byref(default)))
+    for bad in ((96, 0, 20), (128, 8, 20), (128, 0, 33)):
+        with pytest.raises(abi.RtError) as e:
+            device.check(device.lib.rt_ctx_set_traversal_config(device.ctx, C.byref(abi.RtTraversalConfig(*bad, 0))))
+        assert e.value.status == abi.RT_ERR_UNSUPPORTED
+
+
+def test_autotune_picks_a_built_config(device):
+    import ctypes as C
+
+    import torch
+
+    host = _host()
+    frames = _frames(device, _specs()[:2])
+    batch = [host.batch_scene(fr, d, s) for fr, d, s in frames]
+    arr = (abi.RtBatchScene * len(batch))(*batch)
+    host.trace_batch(device, batch)
+    torch.cuda.synchronize()
+    ref = _images(frames)
+    default = abi.RtTraversalConfig()
+    device.check(device.lib.rt_ctx_get_traversal_config(device.ctx, C.byref(default)))
+    rep = abi.RtAutotuneReport()
+    try:
+        device.check(device.lib.rt_ctx_autotune(device.ctx, arr, len(batch), None, 1, host.Device.stream_handle(),
+                                                C.byref(rep)))
+        assert rep.count == 36 and rep.best < rep.count
+        ms = [rep.median_ms[i] for i in range(rep.count)]
+        assert all(m > 0 for m in ms) and ms[rep.best] == min(ms)
+        chosen = abi.RtTraversalConfig()
+        device.check(device.lib.rt_ctx_get_traversal_config(device.ctx, C.byref(chosen)))
+        assert chosen.as_tuple() == rep.configs[rep.best].as_tuple()
+        for fr, _, _ in frames:
+            fr.image.zero_()
+        host.trace_batch(device, batch)
+        torch.cuda.synchronize()
+        for k, (fr, _, _) in enumerate(frames):
+            assert torch.equal(fr.image, ref[k])
+    finally:
+        device.check(device.lib.rt_ctx_set_traversal_config(device.ctx, C.byref(default)))
