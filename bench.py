@@ -24,6 +24,7 @@ from __future__ import annotations
 import argparse
 import ctypes as C
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -65,10 +66,15 @@ def parse_args():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--width", type=int, default=WIDTH)
     p.add_argument("--height", type=int, default=HEIGHT)
-    p.add_argument("--workload", default="frame", choices=["frame", "precision", "batch"],
+    p.add_argument("--workload", default="frame", choices=["frame", "precision", "batch", "serve"],
                    help="frame: the full 1080p frame (default); precision: 10,485,760-triangle icosphere, "
-                        "4M random rays, quantised vs FP32 nodes; batch: 64 scenes in one batched launch")
+                        "4M random rays, quantised vs FP32 nodes; batch: 64 scenes in one batched launch; "
+                        "serve: Poisson request stream over 32 resident scenes")
     p.add_argument("--batch-scenes", type=int, default=64, help=argparse.SUPPRESS)
+    p.add_argument("--serve-seconds", type=float, default=120.0, help="serve: length of the request stream")
+    p.add_argument("--serve-rate", type=float, default=400.0, help=argparse.SUPPRESS)
+    p.add_argument("--serve-scenes", type=int, default=32, help=argparse.SUPPRESS)
+    p.add_argument("--serve-budget-gb", type=float, default=150.0, help=argparse.SUPPRESS)
     p.add_argument("--precision-level", type=int, default=9, help=argparse.SUPPRESS)
     p.add_argument("--precision-rays", type=int, default=PRECISION_RAYS, help=argparse.SUPPRESS)
     return p.parse_args()
@@ -853,8 +859,199 @@ def bench_batch(args):
         dist.destroy_process_group()
 
 
+SERVE_WORKLOAD = ("serve: Poisson request stream (seeded) over 32 device-resident scenes (procedural, unique "
+                  "triangles log-uniform in [50k, 4M], RGBA8 textures), each request a random scene, camera and "
+                  "light, resolution from {256^2, 512^2, 1024^2, 1280x720, 1920x1080}, 1-8 soft-shadow rays and "
+                  "1 reflection bounce; admission by an HBM budget for BVHs + textures + frame buffers; "
+                  "continuous batching vs the plain one-request-per-launch path on the same stream")
+
+
+def serve_requests(args, n_scenes):
+    """The seeded request stream: (arrival s, scene, w, h, shadows, uniforms)."""
+    rng = scenes.Pcg32(4242, 0x77)
+    t, out = 0.0, []
+    while True:
+        t += -math.log(1.0 - rng.uniform()) / args.serve_rate
+        if t >= args.serve_seconds:
+            break
+        sc = int(rng.next_u32() % n_scenes)
+        w, h = scenes.SERVE_RESOLUTIONS[int(rng.next_u32() % len(scenes.SERVE_RESOLUTIONS))]
+        shadows = 1 + int(rng.next_u32() % 8)
+        out.append((t, sc, w, h, shadows, scenes.random_view_uniforms(rng, w, h, frame=len(out))))
+    return out
+
+
+def run_stream(dev, gscenes, reqs, budget, max_batch, in_flight, ring):
+    """Replays `reqs` at their arrival times against a fresh server; returns
+    (latencies ms, queue ms, batch sizes, wall s, traversals, server stats)."""
+    import torch
+
+    from rtgallery import host
+
+    srv = host.Server(dev, budget, max_batch_requests=max_batch, max_in_flight=in_flight)
+    ids = [srv.add_scene(g) for g in gscenes]
+    tickets = [None] * len(reqs)
+    results = [None] * len(reqs)
+    slot_owner = [None] * len(ring)
+    torch.cuda.synchronize()
+    dev.read_stats(reset=True)
+
+    def waiter():
+        for i in range(len(reqs)):
+            while tickets[i] is None:
+                time.sleep(0.0002)
+            results[i] = srv.wait(tickets[i], 600000)
+
+    th = threading.Thread(target=waiter)
+    th.start()
+    t0 = time.perf_counter()
+    for i, (t, sc, w, h, shadows, u) in enumerate(reqs):
+        k = i % len(ring)
+        while slot_owner[k] is not None and results[slot_owner[k]] is None:
+            time.sleep(0.0002)  # the pinned slot is still being written by an earlier request
+        slot_owner[k] = i
+        delay = t0 + t - time.perf_counter()
+        if delay > 0:
+            time.sleep(delay)
+        tickets[i] = srv.submit(ids[sc], u, w, h, 2, shadows, image_host=ring[k].data_ptr())
+    th.join()
+    wall = time.perf_counter() - t0
+    st = srv.stats()
+    srv.close()
+    torch.cuda.synchronize()
+    rays = dev.read_stats(reset=True)["traversals"]
+    lat = np.array([r.latency_ms for r in results])
+    qms = np.array([r.queue_ms for r in results])
+    bs = np.array([r.batch_requests for r in results])
+    return lat, qms, bs, wall, rays, st
+
+
+def bench_serve_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    from oracle.oracle import OracleScene, default_threads
+
+    threads = default_threads()
+    scs = [scenes.scene_serve_member(i) for i in range(min(args.serve_scenes, 4))]
+    reqs = serve_requests(args, len(scs))
+    times, rays = [], 0
+    for k in range(args.warmup + args.steps):
+        t, sc, w, h, shadows, u = reqs[k % len(reqs)]
+        o = OracleScene(scs[sc])
+        band = max(2, h // 64)
+        y0 = (k * band) % max(1, h - band)
+        t1 = time.perf_counter()
+        _, _, st = o.render(uniforms=u, width=w, height=h, max_trace_depth=2, shadow_ray_count=shadows,
+                            rows=(y0, y0 + band), threads=threads)
+        dt = time.perf_counter() - t1
+        if k >= args.warmup:
+            times.append(dt)
+            rays += st["traversals"]
+    total = sum(times)
+    value = rays / total / 1e6
+    print(json.dumps({
+        "impl": "reference", "metric": "Mrays/s", "value": value, "unit": "Mrays/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": SERVE_WORKLOAD, "sample": "a 1/64 row band of one request per step (4 scenes)"},
+        "cpu_baseline": {"value": value, "unit": "Mrays/s", "cores": threads, "kind": "port",
+                         "sample": f"1/64 row band of one request per step, {args.steps} steps"},
+        "e2e": {"value": value, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+
+
+def bench_serve(args):
+    import torch
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    from rtgallery import host
+
+    dev = host.Device(threadsafe=True)
+    t0 = time.perf_counter()
+    scs = [scenes.scene_serve_member(i) for i in range(args.serve_scenes)]
+    gscenes = [host.GpuScene(dev, sc, own_textures=True) for sc in scs]
+    torch.cuda.synchronize()
+    setup_s = time.perf_counter() - t0
+    reqs = serve_requests(args, len(scs))
+    budget = int(args.serve_budget_gb * (1 << 30))
+    max_px = max(w * h for w, h in scenes.SERVE_RESOLUTIONS)
+    ring = [torch.empty(max_px * 4, dtype=torch.uint8).pin_memory() for _ in range(256)]
+    # warm-up: a short stream so kernels, pools and the workspace exist
+    warm = [(0.0005 * i, *r[1:]) for i, r in enumerate(reqs[:64])]
+    run_stream(dev, gscenes, warm, budget, 32, 2, ring)
+    clocks = ClockSampler(local)
+    clocks.start()
+    lat, qms, bs, wall, rays, st = run_stream(dev, gscenes, reqs, budget, 32, 2, ring)
+    clk = clocks.stop()
+    p_lat, p_q, p_bs, p_wall, p_rays, p_st = run_stream(dev, gscenes, reqs, budget, 1, 1, ring)
+    # capacity: the first 2000 requests all arriving at once, batched and plain
+    burst = [(0.0, *r[1:]) for r in reqs[:2000]]
+    _, _, c_bs, c_wall, c_rays, _ = run_stream(dev, gscenes, burst, budget, 32, 2, ring)
+    _, _, _, cp_wall, cp_rays, _ = run_stream(dev, gscenes, burst, budget, 1, 1, ring)
+
+    def pct(a, q):
+        return float(np.percentile(a, q))
+
+    value = rays / wall / 1e6
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        from oracle.oracle import OracleScene, default_threads
+
+        threads = default_threads()
+        t_cpu, r_cpu, k = 0.0, 0, 0
+        while t_cpu < 10.0 and k < len(reqs):
+            t, sc, w, h, shadows, u = reqs[k]
+            o = OracleScene(scs[sc])
+            band = max(2, h // 64)
+            t1 = time.perf_counter()
+            _, _, s2 = o.render(uniforms=u, width=w, height=h, max_trace_depth=2, shadow_ray_count=shadows,
+                                rows=(0, band), threads=threads)
+            t_cpu += time.perf_counter() - t1
+            r_cpu += s2["traversals"]
+            k += 1
+        cpu = {"value": r_cpu / t_cpu / 1e6, "unit": "Mrays/s", "cores": threads, "kind": "port",
+               "sample": f"1/64 row bands of the first {k} requests ({r_cpu} traversals, {t_cpu:.1f} s)"}
+    if rank == 0:
+        print(json.dumps({
+            "metric": "Mrays/s", "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": len(reqs),
+            "warmup": 64, "ms_per_step": 1e3 * wall / len(reqs), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (procedural scenes and request stream from seeds)",
+            "config": {"workload": SERVE_WORKLOAD, "requests": len(reqs), "rate_per_s": args.serve_rate,
+                       "stream_s": args.serve_seconds, "scenes": len(scs),
+                       "unique_triangles": int(sum(m.triangle_count for sc in scs for m in sc.models)),
+                       "hbm_budget_bytes": budget, "peak_bytes": st["peak_bytes"], "resident_bytes": st["resident_bytes"],
+                       "scene_setup_s": setup_s,
+                       "batched": {"p50_ms": pct(lat, 50), "p99_ms": pct(lat, 99), "p999_ms": pct(lat, 99.9),
+                                   "queue_p50_ms": pct(qms, 50), "mean_batch": float(bs.mean()),
+                                   "batches": st["batches"], "mrays_s": value, "wall_s": wall,
+                                   "rejected": st["rejected"]},
+                       "plain_per_request": {"p50_ms": pct(p_lat, 50), "p99_ms": pct(p_lat, 99),
+                                             "p999_ms": pct(p_lat, 99.9), "mrays_s": p_rays / p_wall / 1e6,
+                                             "wall_s": p_wall, "rejected": p_st["rejected"]},
+                       "capacity_burst_2000": {"batched_mrays_s": c_rays / c_wall / 1e6,
+                                               "plain_mrays_s": cp_rays / cp_wall / 1e6,
+                                               "batched_req_s": len(burst) / c_wall, "plain_req_s": len(burst) / cp_wall,
+                                               "mean_batch": float(c_bs.mean())},
+                       "max_batch_requests": 32, "max_in_flight": 2},
+            "e2e": {"value": value, "unit": "Mrays/s", "h2d_bytes_per_step": C.sizeof(abi.RtUniforms),
+                    "d2h_bytes_per_step": float(np.mean([w * h * 4 for _, _, w, h, _, _ in reqs]))},
+            "roofline": None,
+            "cpu_baseline": cpu,
+            "clocks": clk,
+            "gpu_launches": int(st["batches"]) * 9,
+        }))
+    dev.close()
+
+
 def main():
     args = parse_args()
+    if args.workload == "serve":
+        if args.impl == "reference":
+            bench_serve_reference(args)
+        else:
+            bench_serve(args)
+        return
     if args.workload == "batch":
         if args.impl == "reference":
             bench_batch_reference(args)

@@ -453,6 +453,71 @@ typedef struct RtAutotuneReport {
 RTCORE_API int32_t rt_ctx_autotune(rt_ctx* ctx, const RtBatchScene* scenes, uint32_t scene_count,
                                    const RtShaderBindingTable* sbt, uint32_t reps, void* stream,
                                    RtAutotuneReport* report);
+/* ---- serving: a request loop over device-resident scenes ----
+ * No counterpart in the reference (a single-window renderer).  A server owns
+ * one stream and a worker thread.  Scenes stay resident (their BVHs, buffers
+ * and textures are the caller's, registered with their byte size); requests
+ * (scene, camera/light uniforms, size, depth, shadow rays) are admitted in
+ * arrival order while resident scenes + frame buffers + the batch workspace
+ * fit the HBM budget, and the admitted ones are rendered together by
+ * rt_cmd_trace_rays_batched as soon as one of `max_in_flight` batch slots is
+ * free (continuous batching: requests that arrive while a batch runs join the
+ * next one).  A request's image is identical to rendering it alone. */
+typedef struct rt_server rt_server;
+typedef struct RtServerConfig {
+    uint64_t hbm_budget_bytes;    /* resident scenes + frame buffers + workspace */
+    uint32_t max_batch_requests;  /* 1 = the plain per-request path */
+    uint32_t max_batch_pixels;    /* 0 = no limit */
+    uint32_t max_in_flight;       /* batches queued on the GPU at once, >= 1 */
+    uint32_t _padding;
+} RtServerConfig;
+typedef struct RtServeScene {
+    uint64_t acceleration_structure;  /* TLAS device address */
+    uint64_t model_info;              /* device RtModelInfo[] */
+    uint64_t texture_table;           /* device RtTextureDesc[texture_count] */
+    uint32_t texture_count;
+    uint32_t _padding;
+    uint64_t resident_bytes;          /* device bytes the scene keeps resident */
+} RtServeScene;
+typedef struct RtServeRequest {
+    RtUniforms uniforms;              /* copied at submit */
+    uint32_t scene;                   /* rt_server_add_scene id */
+    uint32_t width, height;
+    uint32_t max_trace_depth;
+    uint32_t shadow_ray_count;
+    uint32_t flags;                   /* RT_TRACE_FLAG_LAMBERT_DIFFUSE */
+    uint64_t image_device;            /* 0 = a server frame buffer (counted in the budget) */
+    uint64_t image_host;              /* optional: RGBA8 copied here (pinned memory recommended) */
+    uint32_t _padding[2];
+} RtServeRequest;
+#define RT_SERVE_PENDING 0u
+#define RT_SERVE_DONE 1u
+#define RT_SERVE_REJECTED 2u
+typedef struct RtServeResult {
+    uint32_t state;                   /* RT_SERVE_* */
+    uint32_t status;                  /* RT_OK or why it failed / was rejected */
+    uint32_t batch;                   /* sequence number of its batch */
+    uint32_t batch_requests;          /* requests in that batch */
+    double queue_ms;                  /* submit -> its batch was launched */
+    double latency_ms;                /* submit -> image complete (and copied to image_host) */
+} RtServeResult;
+typedef struct RtServeStats {
+    uint64_t submitted, completed, rejected, batches;
+    uint64_t resident_bytes, peak_bytes, budget_bytes;
+    uint64_t pixels;                  /* rendered */
+} RtServeStats;
+RTCORE_API int32_t rt_server_create(rt_ctx* ctx, const RtServerConfig* config, rt_server** out);
+/* Finishes every admitted request, then releases the server's memory. */
+RTCORE_API int32_t rt_server_destroy(rt_server* server);
+/* RT_ERR_OOM if the scene would exceed the budget. */
+RTCORE_API int32_t rt_server_add_scene(rt_server* server, const RtServeScene* scene, uint32_t* id);
+/* Queues a request; RT_ERR_TOO_LARGE if it cannot fit the budget even alone. */
+RTCORE_API int32_t rt_server_submit(rt_server* server, const RtServeRequest* request, uint64_t* ticket);
+/* Waits up to timeout_ms for `ticket` (RT_ERR_TIMEOUT if still pending); a
+ * finished result is returned once and then forgotten. */
+RTCORE_API int32_t rt_server_wait(rt_server* server, uint64_t ticket, uint32_t timeout_ms, RtServeResult* out);
+RTCORE_API int32_t rt_server_stats(rt_server* server, RtServeStats* out);
+
 /* Traversal only: one traceRay per RtRay against `tlas`, writing RtHit.
  * `push` may be NULL (then any-hit programs cannot run and candidates are
  * accepted as if opaque). */
@@ -504,6 +569,12 @@ RT_STATIC_ASSERT(sizeof(RtShaderBindingTable) == 72, "sbt is 72 bytes");
 RT_STATIC_ASSERT(sizeof(RtTraceRaysDesc) == 40, "trace desc is 40 bytes");
 RT_STATIC_ASSERT(sizeof(RtBatchScene) == 80, "batch scene is 80 bytes");
 RT_STATIC_ASSERT(offsetof(RtBatchScene, desc) == 40, "RtBatchScene.desc @40");
+RT_STATIC_ASSERT(sizeof(RtServerConfig) == 24, "server config is 24 bytes");
+RT_STATIC_ASSERT(sizeof(RtServeScene) == 40, "serve scene is 40 bytes");
+RT_STATIC_ASSERT(sizeof(RtServeRequest) == 224, "serve request is 224 bytes");
+RT_STATIC_ASSERT(offsetof(RtServeRequest, image_device) == 200, "RtServeRequest.image_device @200");
+RT_STATIC_ASSERT(sizeof(RtServeResult) == 32, "serve result is 32 bytes");
+RT_STATIC_ASSERT(sizeof(RtServeStats) == 64, "serve stats are 64 bytes");
 RT_STATIC_ASSERT(sizeof(RtTraceTimings) == 32, "timings are 32 bytes");
 
 #endif /* RTCORE_H */

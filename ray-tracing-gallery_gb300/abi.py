@@ -229,6 +229,39 @@ class RtAutotuneReport(C.Structure):
                 ("median_ms", C.c_float * RT_AUTOTUNE_MAX_CONFIGS)]
 
 
+class RtServerConfig(C.Structure):
+    _fields_ = [("hbm_budget_bytes", C.c_uint64), ("max_batch_requests", C.c_uint32),
+                ("max_batch_pixels", C.c_uint32), ("max_in_flight", C.c_uint32), ("_padding", C.c_uint32)]
+
+
+class RtServeScene(C.Structure):
+    _fields_ = [("acceleration_structure", C.c_uint64), ("model_info", C.c_uint64), ("texture_table", C.c_uint64),
+                ("texture_count", C.c_uint32), ("_padding", C.c_uint32), ("resident_bytes", C.c_uint64)]
+
+
+class RtServeRequest(C.Structure):
+    _fields_ = [("uniforms", RtUniforms), ("scene", C.c_uint32), ("width", C.c_uint32), ("height", C.c_uint32),
+                ("max_trace_depth", C.c_uint32), ("shadow_ray_count", C.c_uint32), ("flags", C.c_uint32),
+                ("image_device", C.c_uint64), ("image_host", C.c_uint64), ("_padding", C.c_uint32 * 2)]
+
+
+RT_SERVE_PENDING, RT_SERVE_DONE, RT_SERVE_REJECTED = 0, 1, 2
+
+
+class RtServeResult(C.Structure):
+    _fields_ = [("state", C.c_uint32), ("status", C.c_uint32), ("batch", C.c_uint32), ("batch_requests", C.c_uint32),
+                ("queue_ms", C.c_double), ("latency_ms", C.c_double)]
+
+
+class RtServeStats(C.Structure):
+    _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("rejected", C.c_uint64),
+                ("batches", C.c_uint64), ("resident_bytes", C.c_uint64), ("peak_bytes", C.c_uint64),
+                ("budget_bytes", C.c_uint64), ("pixels", C.c_uint64)]
+
+    def as_dict(self) -> dict:
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
 class RtRay(C.Structure):
     _fields_ = [("origin", C.c_float * 3), ("tmin", C.c_float), ("direction", C.c_float * 3), ("tmax", C.c_float)]
 
@@ -322,6 +355,12 @@ EXPORTED_FUNCTIONS = {
                                                C.POINTER(RtShaderBindingTable), C.c_uint32, C.c_void_p]),
     "rt_ctx_set_traversal_config": (C.c_int32, [C.c_void_p, C.POINTER(RtTraversalConfig)]),
     "rt_ctx_get_traversal_config": (C.c_int32, [C.c_void_p, C.POINTER(RtTraversalConfig)]),
+    "rt_server_create": (C.c_int32, [C.c_void_p, C.POINTER(RtServerConfig), C.POINTER(C.c_void_p)]),
+    "rt_server_destroy": (C.c_int32, [C.c_void_p]),
+    "rt_server_add_scene": (C.c_int32, [C.c_void_p, C.POINTER(RtServeScene), C.POINTER(C.c_uint32)]),
+    "rt_server_submit": (C.c_int32, [C.c_void_p, C.POINTER(RtServeRequest), C.POINTER(C.c_uint64)]),
+    "rt_server_wait": (C.c_int32, [C.c_void_p, C.c_uint64, C.c_uint32, C.POINTER(RtServeResult)]),
+    "rt_server_stats": (C.c_int32, [C.c_void_p, C.POINTER(RtServeStats)]),
     "rt_ctx_autotune": (C.c_int32, [C.c_void_p, C.POINTER(RtBatchScene), C.c_uint32, C.POINTER(RtShaderBindingTable),
                                      C.c_uint32, C.c_void_p, C.POINTER(RtAutotuneReport)]),
     "rt_cmd_trace_ray_buffer": (C.c_int32, [C.c_void_p, C.c_uint64, C.POINTER(RtPushConstantBufferAddresses),
@@ -411,3 +450,6 @@ def check_layouts() -> None:
     assert C.sizeof(RtBatchScene) == 80 and RtBatchScene.desc.offset == 40
     assert C.sizeof(RtTraversalConfig) == 16
     assert C.sizeof(RtAutotuneReport) == 8 + 64 * 16 + 64 * 4
+    assert C.sizeof(RtServerConfig) == 24 and C.sizeof(RtServeScene) == 40
+    assert C.sizeof(RtServeRequest) == 224 and RtServeRequest.image_device.offset == 200
+    assert C.sizeof(RtServeResult) == 32 and C.sizeof(RtServeStats) == 64

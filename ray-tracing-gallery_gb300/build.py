@@ -19,7 +19,7 @@ CSRC = PKG_DIR / "csrc"
 BUILD_DIR = PKG_DIR / "_build"
 INCLUDE_DIR = PKG_DIR.parent / "include"
 LIB_NAME = "librtcore.so"
-SOURCES = ["rt_api.cu", "rt_build.cu", "rt_trace.cu"]
+SOURCES = ["rt_api.cu", "rt_build.cu", "rt_trace.cu", "rt_serve.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = [
     "-O3",

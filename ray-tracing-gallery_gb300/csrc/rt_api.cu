@@ -99,6 +99,8 @@ struct rt_ctx {
     RtTraversalConfig traversal{128, 0, 20, 0};
 };
 
+bool rt::ctx_is_threadsafe(const rt_ctx* c) { return c && (c->flags & RT_CTX_THREADSAFE) != 0; }
+
 namespace {
 bool stream_capturing(cudaStream_t s) {
     cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;

@@ -17,6 +17,9 @@ void note_launch();
 void note_blas_kind(uint32_t kind);
 uint32_t blas_kinds_built();
 
+// Whether the context was created with RT_CTX_THREADSAFE.
+bool ctx_is_threadsafe(const rt_ctx* ctx);
+
 // One BLAS geometry as the build kernels see it.
 struct BuildGeom {
     const float* pos;

@@ -398,3 +398,76 @@ def trace_ray_buffer(device: Device, gpu_scene: GpuScene, rays: np.ndarray, ray_
                                                     Device.stream_handle()))
     torch.cuda.synchronize()
     return hb.cpu().numpy().view(abi.HIT_DTYPE)
+
+
+def resident_bytes(gpu_scene: GpuScene) -> int:
+    """Device bytes a scene keeps resident: BLASes, TLAS, instance and model
+    buffers, and its textures."""
+    n = gpu_scene.tlas.size + gpu_scene.instances_buffer.numel() + gpu_scene.model_info_buffer.numel()
+    for m in gpu_scene.models:
+        n += m.blas.size + m.position_buffer.numel() + m.normal_buffer.numel() + m.uv_buffer.numel()
+        n += m.geometry_info_buffer.numel() + sum(ib.numel() for ib in m.index_buffers)
+    n += sum(t.numel() for t in gpu_scene._texture_refs)
+    if gpu_scene.texture_table is not None:
+        n += gpu_scene.texture_table.numel()
+    return int(n)
+
+
+class Server:
+    """The serving loop of librtcore (rt_server_*): resident scenes, requests
+    admitted by an HBM budget and rendered in continuous batches.  The device
+    context must be thread-safe (Device(threadsafe=True))."""
+
+    def __init__(self, device: Device, budget_bytes: int, max_batch_requests: int = 32, max_batch_pixels: int = 0,
+                 max_in_flight: int = 2):
+        self.device = device
+        cfg = abi.RtServerConfig(int(budget_bytes), max_batch_requests, max_batch_pixels, max_in_flight, 0)
+        self.handle = C.c_void_p()
+        device.check(device.lib.rt_server_create(device.ctx, C.byref(cfg), C.byref(self.handle)))
+        self.scenes = []
+
+    def add_scene(self, gpu_scene: GpuScene) -> int:
+        if gpu_scene.texture_table is None:
+            raise ValueError("a served scene needs its own texture table (GpuScene(own_textures=True))")
+        s = abi.RtServeScene()
+        s.acceleration_structure = gpu_scene.tlas.device_address()
+        s.model_info = gpu_scene.model_info_buffer.data_ptr()
+        s.texture_table = gpu_scene.texture_table.data_ptr()
+        s.texture_count = gpu_scene.texture_count
+        s.resident_bytes = resident_bytes(gpu_scene)
+        sid = C.c_uint32()
+        self.device.check(self.device.lib.rt_server_add_scene(self.handle, C.byref(s), C.byref(sid)))
+        self.scenes.append(gpu_scene)
+        return sid.value
+
+    def submit(self, scene: int, uniforms: abi.RtUniforms, width: int, height: int, max_trace_depth: int = 2,
+               shadow_ray_count: int = 2, image_device: int = 0, image_host: int = 0, flags: int = 0) -> int:
+        r = abi.RtServeRequest()
+        r.uniforms = uniforms
+        r.scene, r.width, r.height = scene, width, height
+        r.max_trace_depth, r.shadow_ray_count, r.flags = max_trace_depth, shadow_ray_count, flags
+        r.image_device, r.image_host = image_device, image_host
+        t = C.c_uint64()
+        self.device.check(self.device.lib.rt_server_submit(self.handle, C.byref(r), C.byref(t)))
+        return t.value
+
+    def wait(self, ticket: int, timeout_ms: int = 60000) -> abi.RtServeResult:
+        out = abi.RtServeResult()
+        self.device.check(self.device.lib.rt_server_wait(self.handle, ticket, timeout_ms, C.byref(out)))
+        return out
+
+    def stats(self) -> dict:
+        s = abi.RtServeStats()
+        self.device.check(self.device.lib.rt_server_stats(self.handle, C.byref(s)))
+        return s.as_dict()
+
+    def close(self) -> None:
+        if self.handle:
+            self.device.check(self.device.lib.rt_server_destroy(self.handle))
+            self.handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

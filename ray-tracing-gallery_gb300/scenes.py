@@ -607,17 +607,10 @@ BATCH_RESOLUTIONS = ((128, 128), (256, 256), (512, 512), (1024, 1024), (1920, 10
 BATCH_TRIS = (10_000, 2_000_000)
 
 
-def scene_batch_member(index: int, seed: int = 23) -> Scene:
-    """One scene of the batched workload: a procedural torus, a displaced UV
-    sphere and a ground grid whose unique triangles total a log-uniform count
-    in [10k, 2M] (split 1/2, 1/3, 1/6), instanced six, four and one times
-    (one torus a mirror); resolution drawn from {128^2, 256^2, 512^2,
-    1024^2, 1920x1080}; primary rays, 2 blue-noise soft shadows (2 deg) and
-    1 reflection bounce.  Everything follows from (seed, index)."""
-    rng = Pcg32(seed * 7919 + index, 0xB7 + index)
-    lo, hi = math.log(BATCH_TRIS[0]), math.log(BATCH_TRIS[1])
-    target = math.exp(lo + (hi - lo) * rng.uniform())
-    width, height = BATCH_RESOLUTIONS[int(rng.next_u32() % len(BATCH_RESOLUTIONS))]
+def _procedural_scene(rng: Pcg32, target: float, width: int, height: int, seed: int, name: str) -> Scene:
+    """A procedural torus, a displaced UV sphere and a ground grid whose
+    unique triangles total about `target` (split 1/2, 1/3, 1/6), instanced
+    six, four and one times (one torus a mirror), seen from a random bearing."""
 
     def grid_dims(tris, aspect):
         nv = max(3, int(round(math.sqrt(tris / (2.0 * aspect)))))
@@ -628,7 +621,7 @@ def scene_batch_member(index: int, seed: int = 23) -> Scene:
     gx = max(1, int(round(math.sqrt(target / 12))))
     tor = _model(torus(1.0, 0.35, tu, tv), f"torus{tu}x{tv}",
                  lambda idx: [Geometry(idx, True, TEX_DIFFUSE_A, TEX_MR_SHINY)])
-    sph = _model(uv_sphere(su, sv, 1.0, 0.05, seed + index), f"sphere{su}x{sv}",
+    sph = _model(uv_sphere(su, sv, 1.0, 0.05, seed), f"sphere{su}x{sv}",
                  lambda idx: [Geometry(idx, True, TEX_DIFFUSE_B, TEX_MR_DEFAULT)])
     gp, gn, guv, gi = quad_grid(gx, gx, 40.0, 40.0, 8.0, 8.0)
     rot = np.array([[1.0, 0.0, 0.0], [0.0, 0.0, -1.0], [0.0, 1.0, 0.0]], np.float32)  # XY grid -> y = 0, normal +y
@@ -647,10 +640,57 @@ def scene_batch_member(index: int, seed: int = 23) -> Scene:
     eye = (12.0 * math.cos(a), rng.uniform_range(4.0, 9.0), 12.0 * math.sin(a))
     u = make_uniforms(look_at_view_inverse(eye, (0.0, 0.5, 0.0)),
                       perspective_reversed_infinite_z_vk_inverse(math.radians(60), width / height, 0.1),
-                      -np.asarray(SUN_DIR_CONFIG), math.tan(math.radians(2.0)), TEX_BLUE_NOISE, TEX_GGX_LUT, index)
-    return Scene([tor, sph, grd], _base_textures(seed + index), inst, u, width, height, max_trace_depth=2,
-                 shadow_ray_count=2, name=f"batch-{index}")
+                      -np.asarray(SUN_DIR_CONFIG), math.tan(math.radians(2.0)), TEX_BLUE_NOISE, TEX_GGX_LUT, 0)
+    return Scene([tor, sph, grd], _base_textures(seed), inst, u, width, height, max_trace_depth=2,
+                 shadow_ray_count=2, name=name)
+
+
+def scene_batch_member(index: int, seed: int = 23) -> Scene:
+    """One scene of the batched workload: a procedural torus, a displaced UV
+    sphere and a ground grid whose unique triangles total a log-uniform count
+    in [10k, 2M] (split 1/2, 1/3, 1/6), instanced six, four and one times
+    (one torus a mirror); resolution drawn from {128^2, 256^2, 512^2,
+    1024^2, 1920x1080}; primary rays, 2 blue-noise soft shadows (2 deg) and
+    1 reflection bounce.  Everything follows from (seed, index)."""
+    rng = Pcg32(seed * 7919 + index, 0xB7 + index)
+    lo, hi = math.log(BATCH_TRIS[0]), math.log(BATCH_TRIS[1])
+    target = math.exp(lo + (hi - lo) * rng.uniform())
+    width, height = BATCH_RESOLUTIONS[int(rng.next_u32() % len(BATCH_RESOLUTIONS))]
+    sc = _procedural_scene(rng, target, width, height, seed + index, f"batch-{index}")
+    sc.uniforms.frame_index = index
+    return sc
 
 
 def batch_scenes(count: int = 64, seed: int = 23) -> list[Scene]:
     return [scene_batch_member(i, seed) for i in range(count)]
+
+
+def random_view_uniforms(rng: Pcg32, width: int, height: int, frame: int = 0, distance=(8.0, 16.0),
+                         height_range=(2.0, 9.0), target=(0.0, 0.5, 0.0)) -> abi.RtUniforms:
+    """A request's camera and light: eye on a random bearing around `target`,
+    sun direction random above the horizon, 2 degree soft-shadow cone."""
+    a = rng.uniform_range(0.0, 2.0 * math.pi)
+    r = rng.uniform_range(*distance)
+    eye = (target[0] + r * math.cos(a), rng.uniform_range(*height_range), target[2] + r * math.sin(a))
+    sa = rng.uniform_range(0.0, 2.0 * math.pi)
+    el = rng.uniform_range(0.3, 1.3)
+    to_sun = np.array([math.cos(el) * math.cos(sa), math.sin(el), math.cos(el) * math.sin(sa)])
+    return make_uniforms(look_at_view_inverse(eye, target),
+                         perspective_reversed_infinite_z_vk_inverse(math.radians(60), width / height, 0.1),
+                         to_sun, math.tan(math.radians(2.0)), TEX_BLUE_NOISE, TEX_GGX_LUT, frame)
+
+
+SERVE_RESOLUTIONS = ((256, 256), (512, 512), (1024, 1024), (1280, 720), (1920, 1080))
+SERVE_TRIS = (50_000, 4_000_000)
+
+
+def scene_serve_member(index: int, seed: int = 31) -> Scene:
+    """One resident scene of the serving workload: the batch scene's layout
+    (torus, displaced sphere, ground grid) with unique triangles log-uniform
+    in [50k, 4M]; camera, light, size and shadow count come per request."""
+    rng = Pcg32(seed * 104729 + index, 0xC3 + index)
+    lo, hi = math.log(SERVE_TRIS[0]), math.log(SERVE_TRIS[1])
+    target = math.exp(lo + (hi - lo) * rng.uniform())
+    sc = _procedural_scene(rng, target, 256, 256, seed + 1000 + index, f"serve-{index}")
+    sc.max_trace_depth, sc.shadow_ray_count = 2, 2
+    return sc
