@@ -441,20 +441,41 @@ __device__ __forceinline__ bool trav_step(Trav& s, STK& stack, const SV& sv, con
                 qnode_keys(s, entry, keys, refs);
             else
                 fnode_keys(s, entry, keys, refs);
-            sort8(keys);
-            if (keys[0] != 0xFFFFFFFFu) {
-                // push the other hit children farthest first; the nearest is
-                // next.  The stored tnear is rounded down: culling stays
-                // conservative.
+            if (ray_flags & RT_RAY_FLAG_TERMINATE_ON_FIRST_HIT) {
+                // Any accepted hit ends the ray and t never shrinks before
+                // that, so neither the visit order nor the stored tnear
+                // matters: the hit children go on the stack unsorted.
+                uint32_t mask = 0;
 #pragma unroll
-                for (int q = 7; q >= 1; q--) {
-                    uint32_t key = keys[q];
-                    if (key == 0xFFFFFFFFu) continue;
-                    if (s.sp < (int)kStackSize) stack.put(s.sp++, make_uint2(pick8(refs, key & 7u), key & ~7u));
-                    else atomicOr(status, 1u << RT_ERR_STACK_OVERFLOW);
+                for (int k = 0; k < 8; k++) mask |= (keys[k] != 0xFFFFFFFFu ? 1u : 0u) << k;
+                if (mask) {
+                    s.entry = pick8(refs, (uint32_t)(__ffs(mask) - 1));
+                    mask &= mask - 1u;
+                    while (mask) {
+                        const uint32_t k = (uint32_t)(__ffs(mask) - 1);
+                        mask &= mask - 1u;
+                        if (s.sp < (int)kStackSize) stack.put(s.sp++, make_uint2(pick8(refs, k), 0u));
+                        else atomicOr(status, 1u << RT_ERR_STACK_OVERFLOW);
+                    }
+                    return false;
                 }
-                s.entry = pick8(refs, keys[0] & 7u);
-                return false;
+            } else {
+                sort8(keys);
+                if (keys[0] != 0xFFFFFFFFu) {
+                    // push the other hit children farthest first; the nearest
+                    // is next.  The stored tnear is rounded down: culling stays
+                    // conservative.
+#pragma unroll
+                    for (int q = 7; q >= 1; q--) {
+                        uint32_t key = keys[q];
+                        if (key == 0xFFFFFFFFu) continue;
+                        const uint32_t ref = pick8(refs, key & 7u);
+                        if (s.sp < (int)kStackSize) stack.put(s.sp++, make_uint2(ref, key & ~7u));
+                        else atomicOr(status, 1u << RT_ERR_STACK_OVERFLOW);
+                    }
+                    s.entry = pick8(refs, keys[0] & 7u);
+                    return false;
+                }
             }
         }
     } else {
