@@ -52,6 +52,7 @@ L2_FLUSH_BYTES = 256 << 20
 NODE_BYTES, TRI_BYTES, RAY_BYTES, HIT_BYTES, INST_BYTES = 256, 48, 32, 16, 128
 QNODE_BYTES, RAY_HIT_BYTES = 96, 32
 PRECISION_RAYS = 4 << 20
+E2E_CHUNK = 1 << 20  # rays per chunk of the host-buffer query
 PRECISION_WORKLOAD = ("precision: displaced icosphere (level 9, every triangle bisected on its longest edge: "
                       "10,485,760 triangles, radius 10, 0.5 fbm displacement), 4,194,304 random rays per step "
                       "(origins U[-15,15]^3, directions uniform on S^2, tmin 0, tmax inf), closest hit")
@@ -555,21 +556,27 @@ def bench_precision(args):
                                    s["triangles_tested"] * TRI_BYTES + s["instances_visited"] * INST_BYTES)
         arm["gbs"] = arm["bytes_per_launch"] / (arm["total_ms"] / args.steps / 1e3) / 1e9
 
-    # end to end through the C ABI: rays from pinned host memory in, hits out
+    # end to end through the C ABI with host buffers: rt_trace_ray_buffer_host copies the rays in and
+    # the hits out from pinned host memory, chunk by chunk, overlapped with the traversal
     q = arms["quantized"]["scene"]
     rays_pinned = torch.from_numpy(rays.view(np.uint8).reshape(-1).copy()).pin_memory()
     hits_pinned = torch.empty(n * RAY_HIT_BYTES, dtype=torch.uint8).pin_memory()
-    rays_stage = torch.empty(n * RAY_BYTES, dtype=torch.uint8, device="cuda")
-    e2e_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    push0 = abi.RtPushConstantBufferAddresses()
+
+    def host_query():
+        dev.check(lib.rt_trace_ray_buffer_host(dev.ctx, q.tlas.device_address(), C.byref(push0), None, 0, 0xFF, 0,
+                                               rays_pinned.data_ptr(), n, hits_pinned.data_ptr(), E2E_CHUNK, sh))
+
+    host_query()
     torch.cuda.synchronize()
+    e2e_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     for i in range(args.steps):
         flush.fill_(i & 0xFF)
         e2e_ev[i][0].record(stream)
-        rays_stage.copy_(rays_pinned, non_blocking=True)
-        launch(q, rays_stage.data_ptr(), hits_dev.data_ptr())
-        hits_pinned.copy_(hits_dev, non_blocking=True)
+        host_query()
         e2e_ev[i][1].record(stream)
     torch.cuda.synchronize()
+    e2e_equal = bool(np.array_equal(hits_pinned.numpy(), hits_dev.cpu().numpy()))
     e2e_ms = sum(a.elapsed_time(b) for a, b in e2e_ev)
     e2e_value = n * world * args.steps / (e2e_ms / 1e3) / 1e6
 
@@ -598,7 +605,8 @@ def bench_precision(args):
                        "quantized": summary(qa), "fp32": summary(fa),
                        "speedup_quantized_over_fp32": qa["value"] / fa["value"]},
             "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": n * RAY_BYTES,
-                    "d2h_bytes_per_step": n * RAY_HIT_BYTES},
+                    "d2h_bytes_per_step": n * RAY_HIT_BYTES, "api": "rt_trace_ray_buffer_host",
+                    "chunk_rays": E2E_CHUNK, "hits_equal_device_query": e2e_equal},
             "roofline": {"bound": "hbm", "achieved": qa["gbs"], "peak": peak, "unit": "GB/s", "frac": qa["gbs"] / peak,
                          "traffic": profiled_traffic("k_trace_ray_buffer_precision.md"),
                          "kernel": "k_trace_ray_buffer (quantised BLAS)",

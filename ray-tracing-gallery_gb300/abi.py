@@ -355,6 +355,9 @@ EXPORTED_FUNCTIONS = {
                                                C.POINTER(RtShaderBindingTable), C.c_uint32, C.c_void_p]),
     "rt_ctx_set_traversal_config": (C.c_int32, [C.c_void_p, C.POINTER(RtTraversalConfig)]),
     "rt_ctx_get_traversal_config": (C.c_int32, [C.c_void_p, C.POINTER(RtTraversalConfig)]),
+    "rt_trace_ray_buffer_host": (C.c_int32, [C.c_void_p, C.c_uint64, C.POINTER(RtPushConstantBufferAddresses),
+                                              C.POINTER(RtShaderBindingTable), C.c_uint32, C.c_uint32, C.c_uint32,
+                                              C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p]),
     "rt_server_create": (C.c_int32, [C.c_void_p, C.POINTER(RtServerConfig), C.POINTER(C.c_void_p)]),
     "rt_server_destroy": (C.c_int32, [C.c_void_p]),
     "rt_server_add_scene": (C.c_int32, [C.c_void_p, C.POINTER(RtServeScene), C.POINTER(C.c_uint32)]),

@@ -97,6 +97,15 @@ struct rt_ctx {
     std::vector<Workspace> workspaces;
     KernelTimer timer;
     RtTraversalConfig traversal{128, 0, 20, 0};
+    // rt_trace_ray_buffer_host: two streams and their device staging (rays, then hits)
+    struct HostQuery {
+        std::mutex mu;
+        bool created = false;
+        cudaStream_t st[2] = {nullptr, nullptr};
+        cudaEvent_t start = nullptr, done[2] = {nullptr, nullptr};
+        uint8_t* staging[2] = {nullptr, nullptr};
+        uint64_t chunk = 0;  // rays each staging buffer holds
+    } hq;
 };
 
 bool rt::ctx_is_threadsafe(const rt_ctx* c) { return c && (c->flags & RT_CTX_THREADSAFE) != 0; }
@@ -204,6 +213,14 @@ RTCORE_API int32_t rt_ctx_destroy(rt_ctx* ctx) {
         for (int i = 0; i < KernelTimer::kMax; i++) cudaEventDestroy(ctx->timer.ev[i]);
     for (auto& w : ctx->workspaces)
         if (w.ptr) cudaFree(w.ptr);
+    if (ctx->hq.created) {
+        for (int k = 0; k < 2; k++) {
+            if (ctx->hq.staging[k]) cudaFree(ctx->hq.staging[k]);
+            cudaEventDestroy(ctx->hq.done[k]);
+            cudaStreamDestroy(ctx->hq.st[k]);
+        }
+        cudaEventDestroy(ctx->hq.start);
+    }
     if (ctx->dev) cudaFree(ctx->dev);
     delete ctx;
     return RT_OK;
@@ -740,6 +757,69 @@ RTCORE_API int32_t rt_cmd_trace_ray_buffer(rt_ctx* ctx, uint64_t tlas, const RtP
     p.kinds_built = blas_kinds_built();
     cudaError_t e = launch_trace_ray_buffer(p, ctx->num_sms, reinterpret_cast<cudaStream_t>(stream));
     if (e != cudaSuccess) return cuda_fail(e, "rt_cmd_trace_ray_buffer");
+    return RT_OK;
+}
+
+RTCORE_API int32_t rt_trace_ray_buffer_host(rt_ctx* ctx, uint64_t tlas, const RtPushConstantBufferAddresses* push,
+                                            const RtShaderBindingTable* sbt, uint32_t ray_flags,
+                                            uint32_t cull_mask, uint32_t sbt_offset, const RtRay* host_rays,
+                                            uint32_t ray_count, RtHit* host_hits, uint32_t chunk_rays,
+                                            void* stream) {
+    if (!ctx) return fail(RT_ERR_INVALID, "ctx is NULL");
+    if (ray_count == 0) return RT_OK;
+    if (!host_rays || !host_hits) return fail(RT_ERR_INVALID, "host_rays / host_hits is NULL");
+    cudaStream_t caller = reinterpret_cast<cudaStream_t>(stream);
+    if (stream_capturing(caller)) return fail(RT_ERR_INVALID, "rt_trace_ray_buffer_host cannot run in a capture");
+    const uint64_t chunk = std::min<uint64_t>(chunk_rays ? chunk_rays : (1u << 20), ray_count);
+    auto& hq = ctx->hq;
+    std::lock_guard<std::mutex> lk(hq.mu);
+    cudaError_t e = cudaSuccess;
+    if (!hq.created) {
+        for (int k = 0; k < 2 && e == cudaSuccess; k++) {
+            e = cudaStreamCreateWithFlags(&hq.st[k], cudaStreamNonBlocking);
+            if (e == cudaSuccess) e = cudaEventCreateWithFlags(&hq.done[k], cudaEventDisableTiming);
+        }
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&hq.start, cudaEventDisableTiming);
+        if (e != cudaSuccess) return cuda_fail(e, "rt_trace_ray_buffer_host (streams)");
+        hq.created = true;
+    }
+    if (hq.chunk < chunk) {
+        for (int k = 0; k < 2; k++) {
+            if (hq.staging[k]) {
+                cudaStreamSynchronize(hq.st[k]);
+                cudaFree(hq.staging[k]);
+                hq.staging[k] = nullptr;
+            }
+        }
+        hq.chunk = 0;
+        for (int k = 0; k < 2 && e == cudaSuccess; k++)
+            e = cudaMalloc(reinterpret_cast<void**>(&hq.staging[k]), chunk * (sizeof(RtRay) + sizeof(RtHit)));
+        if (e != cudaSuccess) return cuda_fail(e, "rt_trace_ray_buffer_host (staging)");
+        hq.chunk = chunk;
+    }
+    e = cudaEventRecord(hq.start, caller);
+    for (int k = 0; k < 2 && e == cudaSuccess; k++) e = cudaStreamWaitEvent(hq.st[k], hq.start, 0);
+    if (e != cudaSuccess) return cuda_fail(e, "rt_trace_ray_buffer_host (ordering)");
+    const uint64_t nchunks = (ray_count + chunk - 1) / chunk;
+    for (uint64_t i = 0; i < nchunks; i++) {
+        const int k = (int)(i & 1);
+        const uint64_t first = i * chunk, n = std::min<uint64_t>(chunk, ray_count - first);
+        uint8_t* rays_dev = hq.staging[k];
+        uint8_t* hits_dev = hq.staging[k] + hq.chunk * sizeof(RtRay);
+        e = cudaMemcpyAsync(rays_dev, host_rays + first, n * sizeof(RtRay), cudaMemcpyHostToDevice, hq.st[k]);
+        if (e != cudaSuccess) return cuda_fail(e, "rt_trace_ray_buffer_host (rays in)");
+        int32_t r = rt_cmd_trace_ray_buffer(ctx, tlas, push, sbt, ray_flags, cull_mask, sbt_offset,
+                                            reinterpret_cast<uint64_t>(rays_dev), (uint32_t)n,
+                                            reinterpret_cast<uint64_t>(hits_dev), hq.st[k]);
+        if (r != RT_OK) return r;
+        e = cudaMemcpyAsync(host_hits + first, hits_dev, n * sizeof(RtHit), cudaMemcpyDeviceToHost, hq.st[k]);
+        if (e != cudaSuccess) return cuda_fail(e, "rt_trace_ray_buffer_host (hits out)");
+    }
+    for (int k = 0; k < 2 && e == cudaSuccess; k++) {
+        e = cudaEventRecord(hq.done[k], hq.st[k]);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(caller, hq.done[k], 0);
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "rt_trace_ray_buffer_host (join)");
     return RT_OK;
 }
 

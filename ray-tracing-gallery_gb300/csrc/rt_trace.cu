@@ -52,11 +52,6 @@ constexpr uint32_t kNoItem = 0xFFFFFFFFu;
 constexpr uint32_t kMaxTraversalSteps = 1u << 22;
 constexpr int kTraceThreads = 128;
 constexpr int kMaxDepth = 64;
-// Resident 128-thread blocks per SM the trace kernels are compiled for
-// (6 -> at most 80 registers, 24 warps per SM).
-#ifndef RT_TRACE_MIN_BLOCKS
-#define RT_TRACE_MIN_BLOCKS 6
-#endif
 // Warp phase scheduling.  Each iteration of the traversal loop runs either
 // node steps (lanes whose next entry is an internal node) or the other steps
 // (leaves, instance entries, TLAS returns), so a warp never pays for both
@@ -70,6 +65,9 @@ constexpr int kMaxDepth = 64;
 // Resident warps per SM every trace kernel variant is compiled for (at most
 // 80 registers a thread); block size x blocks per SM = 24 warps.
 constexpr int kTraceWarpsPerSM = 24;
+// Kernels that decode only quantised BLAS nodes hold far fewer node registers
+// and run at 32 warps per SM (at most 64 registers a thread).
+constexpr int trace_warps_per_sm(uint32_t kinds) { return kinds == kBlasKindQ8 ? 32 : kTraceWarpsPerSM; }
 
 constexpr int kModeBounce = 0;   // closest hit of a bounce list -> hit records
 constexpr int kModeShadow = 1;   // any hit of generated shadow rays -> lit counters
@@ -831,7 +829,8 @@ __device__ __forceinline__ bool kinds_selected(uint32_t kinds_built, uint32_t tl
 }
 
 template <int MODE, bool STATS, uint32_t KINDS, int SD, int BLOCK>
-__global__ void __launch_bounds__(BLOCK, kTraceWarpsPerSM * 32 / BLOCK) k_trace(const __grid_constant__ WfParams P) {
+__global__ void __launch_bounds__(BLOCK, trace_warps_per_sm(KINDS) * 32 / BLOCK)
+    k_trace(const __grid_constant__ WfParams P) {
     if (kinds_selected(P.kinds_built, P.B.ctr->kinds, KINDS)) trace_wavefront<MODE, STATS, KINDS, SD, BLOCK>(P);
 }
 
@@ -1039,7 +1038,7 @@ __device__ __forceinline__ void trace_ray_buffer(const RayBufferParams& P, const
 }
 
 template <bool STATS, uint32_t KINDS>
-__global__ void __launch_bounds__(kTraceThreads, RT_TRACE_MIN_BLOCKS)
+__global__ void __launch_bounds__(kTraceThreads, trace_warps_per_sm(KINDS) * 32 / kTraceThreads)
     k_trace_ray_buffer(const __grid_constant__ RayBufferParams P) {
     const Env e = make_env(P.L.tlas, P.L.push.model_info, P.L.textures, RT_MAX_BOUND_IMAGES, P.L.status);
     if (kinds_selected(P.L.kinds_built, e.blas_kinds, KINDS)) trace_ray_buffer<STATS, KINDS>(P, e);

@@ -214,3 +214,31 @@ def test_autotune_picks_a_built_config(device):
             assert torch.equal(fr.image, ref[k])
     finally:
         device.check(device.lib.rt_ctx_set_traversal_config(device.ctx, C.byref(default)))
+
+
+def test_batch_of_more_scenes_than_one_setup_chunk(device):
+    """70 scenes: their records are written by two setup launches (64 + 6);
+    every image equals the same scene rendered as a batch of one."""
+    import torch
+
+    host = _host()
+    base = scenes.scene_small(24, 16)
+    gs = host.GpuScene(device, base, own_textures=True)
+    rng = scenes.Pcg32(77, 0x70)
+    frames = []
+    for i in range(70):
+        w, h = 8 + int(rng.next_u32() % 40), 4 + int(rng.next_u32() % 30)
+        fr = host.PerFrameResources(device, gs, w, h)
+        fr.write_uniforms(scenes.random_view_uniforms(rng, w, h, frame=i, distance=(6.0, 12.0), height_range=(2.0, 6.0)))
+        frames.append((fr, 1 + i % 3, i % 5))
+    for fr, d, s in frames:
+        host.trace_batch(device, [host.batch_scene(fr, d, s)])
+    torch.cuda.synchronize()
+    alone = _images(frames)
+    for fr, _, _ in frames:
+        fr.image.zero_()
+    host.trace_batch(device, [host.batch_scene(fr, d, s) for fr, d, s in frames])
+    torch.cuda.synchronize()
+    for k, (fr, _, _) in enumerate(frames):
+        assert torch.equal(fr.image, alone[k]), f"scene {k}"
+    assert sum(int(a.float().sum() > 0) for a in alone) > 60

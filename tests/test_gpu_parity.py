@@ -282,3 +282,25 @@ def test_mid_size_mesh_bit_exact(device):
     o, _ = O.OracleScene(sc).trace(rays, with_models=False)
     _assert_hits_equal(g, o, "icosphere l6")
     assert (g["instance_id"] != 0xFFFFFFFF).mean() > 0.2
+
+
+def test_host_buffer_query_matches_device_query(device):
+    """rt_trace_ray_buffer_host (chunked, two streams, ragged last chunk)
+    returns the same hits as rt_cmd_trace_ray_buffer."""
+    import torch
+
+    host = _host()
+    sc = scenes.scene_gallery(64, 48)
+    gs = _gpu_scene(device, sc)
+    rays = scenes.random_rays(20011, 17, 14.0)
+    rays["tmax"] = 1e4
+    ref = host.trace_ray_buffer(device, gs, rays)
+    rays_h = torch.from_numpy(rays.view(np.uint8).copy()).pin_memory()
+    for chunk in (3000, 0, 20011):
+        hits_h = torch.zeros(len(rays) * abi.HIT_DTYPE.itemsize, dtype=torch.uint8).pin_memory()
+        push = gs.push_constants(0)
+        device.check(device.lib.rt_trace_ray_buffer_host(device.ctx, gs.tlas.device_address(), C.byref(push), None,
+                                                         0, 0xFF, 0, rays_h.data_ptr(), len(rays), hits_h.data_ptr(),
+                                                         chunk, host.Device.stream_handle()))
+        torch.cuda.synchronize()
+        _assert_hits_equal(hits_h.numpy().view(abi.HIT_DTYPE), ref, f"host query, chunk {chunk}")
