@@ -628,13 +628,15 @@ BATCH_WORKLOAD = ("batch: 64 independent scenes (procedural torus + displaced UV
                   "replayed from a CUDA graph")
 
 
-def batch_setup(dev, count):
+def batch_setup(dev, count, width4: bool = False):
     from rtgallery import host
 
+    w = abi.RT_BUILD_EXT_NODE_WIDTH_4 if width4 else 0
     scs = scenes.batch_scenes(count)
     frames = []
     for sc in scs:
-        gs = host.GpuScene(dev, sc, own_textures=True)
+        gs = host.GpuScene(dev, sc, own_textures=True, blas_flags=abi.RT_BUILD_PREFER_FAST_TRACE | w,
+                           tlas_flags=abi.RT_BUILD_PREFER_FAST_TRACE | abi.RT_BUILD_ALLOW_UPDATE | w)
         fr = host.PerFrameResources(dev, gs, sc.width, sc.height)
         fr.write_uniforms(sc.uniforms)
         frames.append(fr)
@@ -757,14 +759,31 @@ def bench_batch(args):
     ms_single = timed(per_scene, args.steps)
     ms_batch = timed(batched, args.steps)
 
-    # the autotuner picks the traversal launch shape on this batch, then the graph is captured with it
+    # the autotuner picks the traversal launch shape on this batch, for 8-wide and for 4-wide BVHs of
+    # the same scenes (rebuilt); the graph is captured with the fastest width and launch shape
     report = abi.RtAutotuneReport()
     t_tune = time.perf_counter()
     dev.check(lib.rt_ctx_autotune(dev.ctx, arr, len(items), None, 3, sh, C.byref(report)))
-    tune_s = time.perf_counter() - t_tune
-    tuned = report.configs[report.best]
+    best8 = (report.median_ms[report.best], abi.RtTraversalConfig(*report.configs[report.best].as_tuple(), 0))
     default_ms = [report.median_ms[i] for i in range(report.count)
                   if report.configs[i].as_tuple() == (128, 0, 20)][0]
+    _, frames4 = batch_setup(dev, args.batch_scenes, width4=True)
+    items4 = [host.batch_scene(fr, sc.max_trace_depth, sc.shadow_ray_count) for fr, sc in zip(frames4, scs)]
+    arr4 = (abi.RtBatchScene * len(items4))(*items4)
+    with torch.cuda.stream(stream):
+        dev.check(lib.rt_cmd_trace_rays_batched(dev.ctx, arr4, len(items4), None, 0, sh))  # sizes, warm-up
+    torch.cuda.synchronize()
+    report4 = abi.RtAutotuneReport()
+    dev.check(lib.rt_ctx_autotune(dev.ctx, arr4, len(items4), None, 3, sh, C.byref(report4)))
+    best4 = (report4.median_ms[report4.best], abi.RtTraversalConfig(*report4.configs[report4.best].as_tuple(), 0))
+    tune_s = time.perf_counter() - t_tune
+    width = 4 if best4[0] < best8[0] else 8
+    tuned = best4[1] if width == 4 else best8[1]
+    dev.check(lib.rt_ctx_set_traversal_config(dev.ctx, C.byref(tuned)))
+    if width == 4:
+        arr, frames = arr4, frames4  # the same scenes and images, 4-wide BVHs
+    else:
+        del frames4
     graph = torch.cuda.CUDAGraph()
     with torch.cuda.graph(graph, stream=stream):
         batched()
@@ -840,11 +859,14 @@ def bench_batch(args):
                        "per_scene_launches_mrays_s": rays_per_step * args.steps / (ms_single / 1e3) / 1e6,
                        "batched_direct_mrays_s": rays_per_step * args.steps / (ms_batch / 1e3) / 1e6,
                        "batched_graph_mrays_s": value,
-                       "autotuned_config": {"block_size": tuned.block_size,
+                       "autotuned_config": {"node_width": width, "block_size": tuned.block_size,
                                             "shared_stack_depth": tuned.shared_stack_depth,
                                             "leaf_wait": tuned.leaf_wait},
-                       "autotune_configs": int(report.count), "autotune_s": tune_s,
-                       "autotune_best_ms": report.median_ms[report.best], "autotune_default_config_ms": default_ms,
+                       "autotune_configs": int(report.count + report4.count), "autotune_s": tune_s,
+                       "autotune_best_ms_width8": best8[0], "autotune_best_ms_width4": best4[0],
+                       "autotune_best_config_width8": best8[1].as_tuple(),
+                       "autotune_best_config_width4": best4[1].as_tuple(),
+                       "autotune_default_config_ms": default_ms,
                        "speedup_graph_batch_over_per_scene": ms_single / ms_graph,
                        "kernel_launches_per_step": launches_per_step, "scene_setup_s": setup_s,
                        "trace_ms_per_step": kt["trace_ms"], "shade_ms_per_step": kt["shade_ms"],

@@ -149,6 +149,7 @@ typedef struct RtAccelerationStructureInstance {
 #define RT_BUILD_PREFER_FAST_BUILD 0x8u
 #define RT_BUILD_LOW_MEMORY 0x10u
 #define RT_BUILD_QUANTIZED_NODES 0x100u /* 8-bit conservatively quantised child boxes */
+#define RT_BUILD_EXT_NODE_WIDTH_4 0x200u /* at most 4 children per node (same node layout) */
 
 /* gl_RayFlags*EXT */
 #define RT_RAY_FLAG_NONE 0x0u

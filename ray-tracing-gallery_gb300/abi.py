@@ -38,6 +38,7 @@ RT_BUILD_ALLOW_COMPACTION = 0x2
 RT_BUILD_PREFER_FAST_TRACE = 0x4
 RT_BUILD_PREFER_FAST_BUILD = 0x8
 RT_BUILD_QUANTIZED_NODES = 0x100
+RT_BUILD_EXT_NODE_WIDTH_4 = 0x200
 RT_RAY_FLAG_NONE = 0x0
 RT_RAY_FLAG_OPAQUE = 0x1
 RT_RAY_FLAG_NO_OPAQUE = 0x2

@@ -286,9 +286,8 @@ RTCORE_API int32_t rt_get_blas_build_sizes(const RtGeometryTriangles* geometries
     uint32_t n = 0;
     int32_t r = blas_prim_count(geometries, geometry_count, &n);
     if (r) return r;
-    const bool quantized = (build_flags & RT_BUILD_QUANTIZED_NODES) != 0;
-    AsLayout al = AsLayout::make(n, false, quantized);
-    ScratchLayout sl = ScratchLayout::make(n, false, quantized);
+    AsLayout al = AsLayout::make(n, false, build_flags);
+    ScratchLayout sl = ScratchLayout::make(n, false, build_flags);
     out->acceleration_structure_size = al.total;
     out->build_scratch_size = sl.build_total;
     out->update_scratch_size = sl.update_total;
@@ -302,9 +301,8 @@ RTCORE_API int32_t rt_cmd_build_blas(rt_ctx* ctx, const RtGeometryTriangles* geo
     uint32_t n = 0;
     int32_t r = blas_prim_count(geometries, geometry_count, &n);
     if (r) return r;
-    const bool quantized = (build_flags & RT_BUILD_QUANTIZED_NODES) != 0;
-    AsLayout al = AsLayout::make(n, false, quantized);
-    ScratchLayout sl = ScratchLayout::make(n, false, quantized);
+    AsLayout al = AsLayout::make(n, false, build_flags);
+    ScratchLayout sl = ScratchLayout::make(n, false, build_flags);
     if (!dst || !aligned(dst, RT_AS_ALIGNMENT)) return fail(RT_ERR_INVALID, "dst must be non-null and 256-byte aligned");
     if (dst_size < al.total)
         return fail(RT_ERR_INVALID, "dst_size %llu < required %llu", (unsigned long long)dst_size,
@@ -385,8 +383,8 @@ RTCORE_API int32_t rt_cmd_build_blas_static_scratch(rt_ctx* ctx, const RtGeometr
     if (r) return r;
     if (build_flags & RT_BUILD_QUANTIZED_NODES)
         return fail(RT_ERR_UNSUPPORTED, "RT_BUILD_QUANTIZED_NODES is not supported by the static-scratch build");
-    AsLayout al = AsLayout::make(n, false);
-    ScratchLayout sl = ScratchLayout::make(n, false);
+    AsLayout al = AsLayout::make(n, false, build_flags);
+    ScratchLayout sl = ScratchLayout::make(n, false, build_flags);
     if (!dst || !aligned(dst, RT_AS_ALIGNMENT)) return fail(RT_ERR_INVALID, "dst must be non-null and 256-byte aligned");
     if (dst_size < al.total)
         return fail(RT_ERR_INVALID, "dst_size %llu < required %llu", (unsigned long long)dst_size,
@@ -423,10 +421,9 @@ RTCORE_API int32_t rt_cmd_build_blas_static_scratch(rt_ctx* ctx, const RtGeometr
 
 RTCORE_API int32_t rt_get_tlas_build_sizes(uint32_t instance_count, uint32_t build_flags, RtBuildSizes* out) {
     if (!out) return fail(RT_ERR_INVALID, "out is NULL");
-    (void)build_flags;
     if (instance_count > kMaxPrimitives) return fail(RT_ERR_TOO_LARGE, "%u instances > %u", instance_count, kMaxPrimitives);
-    AsLayout al = AsLayout::make(instance_count, true);
-    ScratchLayout sl = ScratchLayout::make(instance_count, true);
+    AsLayout al = AsLayout::make(instance_count, true, build_flags);
+    ScratchLayout sl = ScratchLayout::make(instance_count, true, build_flags);
     out->acceleration_structure_size = al.total;
     out->build_scratch_size = sl.build_total;
     out->update_scratch_size = sl.update_total;
@@ -440,8 +437,8 @@ RTCORE_API int32_t rt_cmd_build_tlas(rt_ctx* ctx, uint64_t instances, uint32_t i
     if (instance_count > kMaxPrimitives) return fail(RT_ERR_TOO_LARGE, "%u instances > %u", instance_count, kMaxPrimitives);
     if (instance_count > 0 && (!instances || !aligned(instances, 16)))
         return fail(RT_ERR_INVALID, "instances must be non-null and 16-byte aligned");
-    AsLayout al = AsLayout::make(instance_count, true);
-    ScratchLayout sl = ScratchLayout::make(instance_count, true);
+    AsLayout al = AsLayout::make(instance_count, true, build_flags);
+    ScratchLayout sl = ScratchLayout::make(instance_count, true, build_flags);
     if (!dst || !aligned(dst, RT_AS_ALIGNMENT)) return fail(RT_ERR_INVALID, "dst must be non-null and 256-byte aligned");
     if (dst_size < al.total)
         return fail(RT_ERR_INVALID, "dst_size %llu < required %llu", (unsigned long long)dst_size,

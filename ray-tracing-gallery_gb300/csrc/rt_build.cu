@@ -505,6 +505,7 @@ struct CollapseCtx {
     uint32_t* parents;   // may be null
     BuildState* st;
     uint32_t leaf_max;
+    uint32_t width;      // children per node: 8, or 4 (RT_BUILD_EXT_NODE_WIDTH_4)
     uint32_t max_nodes;
     uint32_t n;          // primitives
 };
@@ -576,7 +577,7 @@ __device__ void collapse_task(const CollapseCtx& c, uint32_t bref, uint32_t slot
     refs[1] = root.y;
     cnt = 2;
     if (!ref_ok(c, refs[0]) || !ref_ok(c, refs[1])) cnt = 0;
-    while (cnt >= 2 && cnt < 8) {
+    while (cnt >= 2 && cnt < (int)c.width) {
         int best = -1;
         float best_area = -1.0f;
         for (int k = 0; k < cnt; k++) {
@@ -874,9 +875,13 @@ __device__ __forceinline__ int internal_children(const WideNode* nd) {
     return c;
 }
 
-__global__ void k_refit_nodes(AsHeader* h, const float4* sboxes, uint32_t* counters, uint32_t* err) {
+__global__ void k_refit_nodes(AsHeader* h, const float4* sboxes, uint32_t* counters, uint32_t cap, uint32_t* err) {
     uint32_t count = h->node_count;
     uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
+    if (count > cap) {  // a TLAS of more instances than this update was given
+        if (slot == 0) atomicOr(err, 1u << RT_ERR_INVALID);
+        return;
+    }
     if (slot >= count) return;
     uint8_t* base = reinterpret_cast<uint8_t*>(h);
     WideNode* nodes = reinterpret_cast<WideNode*>(base + h->nodes_offset);
@@ -1012,9 +1017,10 @@ inline uint32_t blocks_for(uint64_t n, uint32_t t) { return (uint32_t)((n + t - 
 // ---------------------------------------------------------------------------
 // Layouts
 // ---------------------------------------------------------------------------
-AsLayout AsLayout::make(uint32_t n, bool top, bool quantized) {
+AsLayout AsLayout::make(uint32_t n, bool top, uint32_t build_flags) {
+    const bool quantized = !top && (build_flags & RT_BUILD_QUANTIZED_NODES) != 0;
     AsLayout l;
-    l.max_nodes = (uint32_t)max_wide_nodes(n);
+    l.max_nodes = (uint32_t)max_wide_nodes(n, node_width(build_flags));
     l.node_bytes = (quantized && !top) ? kQNodeBytes : kNodeBytes;
     l.nodes = kHeaderBytes;
     uint64_t end = l.nodes + (uint64_t)l.max_nodes * l.node_bytes;
@@ -1029,7 +1035,9 @@ AsLayout AsLayout::make(uint32_t n, bool top, bool quantized) {
     return l;
 }
 
-ScratchLayout ScratchLayout::make(uint32_t n, bool top, bool quantized) {
+ScratchLayout ScratchLayout::make(uint32_t n, bool top, uint32_t build_flags) {
+    const bool quantized = !top && (build_flags & RT_BUILD_QUANTIZED_NODES) != 0;
+    const uint64_t cap = max_wide_nodes(n, node_width(build_flags));
     ScratchLayout s{};
     uint64_t nn = n ? n : 1;
     uint64_t ni = n > 1 ? n - 1 : 1;
@@ -1053,18 +1061,19 @@ ScratchLayout ScratchLayout::make(uint32_t n, bool top, bool quantized) {
     s.iparent = take(ni * 4);
     s.lparent = take(nn * 4);
     s.flags = take(ni * 4);
-    uint64_t f = std::min<uint64_t>(kFrontierCap, max_wide_nodes(n));
+    uint64_t f = std::min<uint64_t>(kFrontierCap, cap);
     s.frontier0 = take(f * 16);
     s.frontier1 = take(f * 16);
     s.temp_inst = top ? take(nn * kInstBytes) : 0;
-    s.fp32_nodes = (quantized && !top) ? take(max_wide_nodes(n) * kNodeBytes) : 0;
+    s.fp32_nodes = quantized ? take(cap * kNodeBytes) : 0;
     s.refit_counters = 0;
     s.build_total = o;
-    // update (refit) scratch: sorted boxes + one counter per node
+    // update (refit) scratch: sorted boxes + one counter per node, sized for
+    // either node width (the refit does not know which one the TLAS was built with)
     uint64_t u = 0;
     u = align_up(u + nn * 32, 256);
     s.refit_counters = u;
-    u = align_up(u + max_wide_nodes(n) * 4 + 4, 256);  // + error word
+    u = align_up(u + max_wide_nodes(n, 4) * 4 + 4, 256);  // + error word
     s.update_total = u;
     return s;
 }
@@ -1078,8 +1087,8 @@ cudaError_t build_common(uint32_t n, bool top, uint32_t build_flags, uint32_t ge
                          uint8_t* scratch, cudaStream_t stream, const BlasInput* blas,
                          const RtAccelerationStructureInstance* inst) {
     const bool quantized = !top && (build_flags & RT_BUILD_QUANTIZED_NODES) != 0;
-    ScratchLayout sl = ScratchLayout::make(n, top, quantized);
-    AsLayout al = AsLayout::make(n, top, quantized);
+    ScratchLayout sl = ScratchLayout::make(n, top, build_flags);
+    AsLayout al = AsLayout::make(n, top, build_flags);
     // quantised builds collapse into FP32 nodes in scratch, then quantise
     WideNode* fp32_nodes = quantized ? reinterpret_cast<WideNode*>(scratch + sl.fp32_nodes)
                                      : reinterpret_cast<WideNode*>(dst + al.nodes);
@@ -1130,6 +1139,7 @@ cudaError_t build_common(uint32_t n, bool top, uint32_t build_flags, uint32_t ge
         cc.parents = top ? reinterpret_cast<uint32_t*>(dst + al.parents) : nullptr;
         cc.st = st;
         cc.leaf_max = top ? kTlasLeafMax : kBlasLeafMax;
+        cc.width = node_width(build_flags);
         cc.max_nodes = al.max_nodes;
         cc.n = n;
         note_launch(), k_collapse_root<<<1, 32, 0, stream>>>(cc, n, fr[0]);
@@ -1155,6 +1165,7 @@ cudaError_t build_common(uint32_t n, bool top, uint32_t build_flags, uint32_t ge
         cc.parents = top ? reinterpret_cast<uint32_t*>(dst + al.parents) : nullptr;
         cc.st = st;
         cc.leaf_max = 1;
+        cc.width = node_width(build_flags);
         cc.max_nodes = al.max_nodes;
         cc.n = n;
         note_launch(), k_collapse_root<<<1, 32, 0, stream>>>(cc, 0, fr[0]);
@@ -1201,18 +1212,19 @@ cudaError_t launch_as_copy(const uint8_t* src, uint8_t* dst, uint64_t dst_size, 
 cudaError_t launch_tlas_update(const RtAccelerationStructureInstance* instances, uint32_t n, const uint8_t* src,
                                uint8_t* dst, uint64_t dst_size, uint8_t* scratch, cudaStream_t stream) {
     ScratchLayout sl = ScratchLayout::make(n, true);
-    AsLayout al = AsLayout::make(n, true);
+    // node capacity of either node width: the grid and the counters cover any TLAS of n instances
+    const uint32_t cap = (uint32_t)max_wide_nodes(n, 4);
     if (src != dst) {
         note_launch(), k_as_copy<<<1024, 256, 0, stream>>>(src, dst, dst_size, RT_COPY_MODE_CLONE);
     }
     float4* sboxes = reinterpret_cast<float4*>(scratch);
     uint32_t* counters = reinterpret_cast<uint32_t*>(scratch + sl.refit_counters);
     // the error word lives after the counters
-    uint32_t* err = counters + al.max_nodes;
-    cudaMemsetAsync(counters, 0, (size_t)al.max_nodes * 4 + 4, stream);
+    uint32_t* err = counters + cap;
+    cudaMemsetAsync(counters, 0, (size_t)cap * 4 + 4, stream);
     AsHeader* h = reinterpret_cast<AsHeader*>(dst);
     if (n > 0) note_launch(), k_refit_insts<<<blocks_for(n, 256), 256, 0, stream>>>(instances, n, h, sboxes, err);
-    note_launch(), k_refit_nodes<<<blocks_for(al.max_nodes, 128), 128, 0, stream>>>(h, sboxes, counters, err);
+    note_launch(), k_refit_nodes<<<blocks_for(cap, 128), 128, 0, stream>>>(h, sboxes, counters, cap, err);
     note_launch(), k_refit_status<<<1, 32, 0, stream>>>(h, err);
     return cudaGetLastError();
 }

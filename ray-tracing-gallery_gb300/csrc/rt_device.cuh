@@ -132,9 +132,14 @@ __host__ __device__ inline uint64_t align_up(uint64_t x, uint64_t a) { return (x
 // Upper bound of wide nodes for n primitives (see the collapse rule in
 // rt_build.cu): non-full nodes have >= 2 leaf children (<= n/2 of them),
 // full nodes absorb 7 binary nodes each (<= (n-1)/7), plus the root.
-__host__ __device__ inline uint64_t max_wide_nodes(uint64_t n) {
+__host__ __device__ inline uint64_t max_wide_nodes(uint64_t n, uint32_t width = 8) {
     if (n <= 1) return 1;
+    if (width <= 4) return n + 2;  // every wide node owns a distinct binary node
     return n / 2 + (n - 1) / 7 + 2;
+}
+// Children per node a build produces (RT_BUILD_EXT_NODE_WIDTH_4: 4, else 8).
+__host__ __device__ inline uint32_t node_width(uint32_t build_flags) {
+    return (build_flags & RT_BUILD_EXT_NODE_WIDTH_4) ? 4u : 8u;
 }
 
 // ---------------------------------------------------------------------------

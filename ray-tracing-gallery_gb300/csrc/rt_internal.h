@@ -46,7 +46,7 @@ struct ScratchLayout {
     uint64_t build_total;
     uint64_t update_total;
     uint32_t sort_blocks;
-    static ScratchLayout make(uint32_t n, bool top_level, bool quantized = false);
+    static ScratchLayout make(uint32_t n, bool top_level, uint32_t build_flags = 0);
 };
 
 // Byte offsets inside the AS blob.
@@ -54,7 +54,7 @@ struct AsLayout {
     uint64_t nodes, parents, prims, total;
     uint32_t max_nodes;
     uint32_t node_bytes;
-    static AsLayout make(uint32_t n, bool top_level, bool quantized = false);
+    static AsLayout make(uint32_t n, bool top_level, uint32_t build_flags = 0);
 };
 
 constexpr uint32_t kMaxPrimitives = (1u << 28) - 1;  // leaf refs carry 28 bits

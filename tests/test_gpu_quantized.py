@@ -4,9 +4,10 @@ A quantised node stores each child box as bytes on a per-node power-of-two
 grid, rounded outwards with a quarter grid step to spare, so the boxes only
 grow: traversal may visit more nodes, never fewer, and the closest hit is
 decided by the same watertight triangle test and the same (t, instance,
-geometry, primitive) order.  Every hit must therefore be bit-identical to the FP32-node
-build and to the oracle.  Rays from far away take the exact plane decode
-instead of the fast one; both are covered.
+geometry, primitive) order.  Every hit must therefore be bit-identical to
+the FP32-node build and to the oracle.  Rays from far away take the exact
+plane decode instead of the fast one; both are covered.  The same holds for
+structures collapsed to at most 4 children per node.
 """
 import ctypes as C
 
@@ -165,3 +166,50 @@ def test_quantized_build_sizes_are_smaller(device):
     device.check(device.lib.rt_get_blas_build_sizes(geo, 1, Q, C.byref(s_q)))
     assert s_q.acceleration_structure_size < s_f.acceleration_structure_size
     assert s_q.build_scratch_size >= s_f.build_scratch_size
+
+
+W4 = abi.RT_BUILD_EXT_NODE_WIDTH_4
+
+
+@pytest.mark.parametrize("name", list(SCENES))
+def test_node_width_4_hits_bit_exact(device, name):
+    """BLASes and TLAS collapsed to at most 4 children per node (FP32 and
+    quantised): same hits as the oracle; a TLAS refit of the 4-wide TLAS too."""
+    import torch
+
+    host = _host()
+    sc = SCENES[name]()
+    o = O.OracleScene(sc)
+    rays = scenes.random_rays(20000, 43, 60.0 if name == "full" else 16.0)
+    rays["tmax"] = 1e4
+    ref, _ = o.trace(rays)
+    tlas_flags = abi.RT_BUILD_PREFER_FAST_TRACE | abi.RT_BUILD_ALLOW_UPDATE | W4
+    for blas_flags in (abi.RT_BUILD_PREFER_FAST_TRACE | W4, Q | W4):
+        g = host.GpuScene(device, sc, blas_flags=blas_flags, tlas_flags=tlas_flags)
+        _same(host.trace_ray_buffer(device, g, rays), ref, f"{name} width 4, blas flags {blas_flags:#x}")
+        info_t = g.tlas.info(device)
+        assert info_t.status == abi.RT_OK
+        if len(sc.instances) > 4:
+            assert info_t.tree_depth >= 2
+    # refit the 4-wide TLAS after moving instances
+    g = host.GpuScene(device, sc, blas_flags=abi.RT_BUILD_PREFER_FAST_TRACE | W4, tlas_flags=tlas_flags)
+    inst = sc.instances.copy()
+    rng = scenes.Pcg32(5, 9)
+    for i in range(0, len(inst), 2):
+        inst["transform"][i, :, 3] += np.array([rng.uniform_range(-1, 1), 0.5, rng.uniform_range(-1, 1)], np.float32)
+    g.instances_buffer.copy_(torch.from_numpy(g.patch_instances(inst).view(np.uint8).reshape(-1)).cuda())
+    g.tlas.update_tlas(device, g.instances_buffer, len(inst), g.scratch)
+    assert g.tlas.info(device).status == abi.RT_OK
+    o.set_instances(inst)
+    _same(host.trace_ray_buffer(device, g, rays), o.trace(rays)[0], f"{name} width 4 after refit")
+
+
+def test_node_width_4_render_matches_oracle(device):
+    host = _host()
+    sc = scenes.scene_gallery(96, 64)
+    g = host.GpuScene(device, sc, blas_flags=abi.RT_BUILD_PREFER_FAST_TRACE | W4,
+                      tlas_flags=abi.RT_BUILD_PREFER_FAST_TRACE | abi.RT_BUILD_ALLOW_UPDATE | W4)
+    img, rad, st = host.render(device, sc, radiance=True, gpu_scene=g)
+    o_img, o_rad, o_st = O.OracleScene(sc).render()
+    assert st["traversals"] == o_st["traversals"] and st["status"] == 0
+    assert np.abs(rad - o_rad).max() <= 1e-3
