@@ -758,7 +758,48 @@ __global__ void k_raygen(const __grid_constant__ WfParams P) {
     count_rays(P.stats, x < W && y < H ? 1u : 0u, 0u, 0u);
 }
 
-// Persistent trace loop with per-lane ray replacement.
+// The next bounce ray of a mirror hit (closest_hit_mirror.glsl:11-29:
+// reflect about the interpolated world normal) or a portal hit
+// (lib.rs:300-312: same direction, origin lifted by (0, 5, 0)); a zero
+// direction for any other program or a mirror without model data, which
+// ends the reference's bounce loop (lib.rs:165-171).
+struct NextRay {
+    V3 o, d;
+};
+__device__ __forceinline__ NextRay next_bounce_ray(const Env& e, const RtShaderBindingTable* sbt, uint32_t inst,
+                                                uint32_t geom, uint32_t prim, float t, float hu, float hv, V3 ro,
+                                                V3 rd) {
+    NextRay r;
+    r.o = mk3(0.0f, 0.0f, 0.0f);
+    r.d = mk3(0.0f, 0.0f, 0.0f);
+    const InstRecord* ir = &e.insts[inst];
+    const RtHitGroup* g = hit_group(sbt, ir->sbt_flags, 0u);
+    const uint32_t prog = g ? g->closest_hit : RT_PROGRAM_NONE;
+    TriData td;
+    if (prog == RT_PROGRAM_CLOSEST_HIT_MIRROR && load_triangle(e, ir->custom_mask & 0xFFFFFFu, geom, prim, &td)) {
+        const V3 bary = mk3((1.0f - hu) - hv, hu, hv);
+        V3 ni = interp3(td.n[0], td.n[1], td.n[2], bary);
+        V3 n = normalize3(xform_normal_w2o_t(ir->w2o, ni));
+        float k = 2.0f * dot3(n, rd);
+        r.d = sub3(rd, mul3s(n, k));
+        r.o = add3(ro, mul3s(rd, t));
+    } else if (prog == RT_PROGRAM_CLOSEST_HIT_PORTAL) {
+        r.d = rd;
+        r.o = add3(add3(ro, mul3s(rd, t)), mk3(0.0f, 5.0f, 0.0f));
+    }
+    return r;
+}
+
+// Ray-list scene words carry the ray's bounce depth in their top byte.
+constexpr uint32_t kSceneBits = 24;
+constexpr uint32_t kSceneMask = (1u << kSceneBits) - 1u;
+
+// Persistent trace loop with per-lane ray replacement.  Bounce lists:
+// when a ray's closest hit is a mirror or a portal and the scene's depth
+// allows another bounce, the same lane traces the next ray at once (the
+// closest-hit program's arithmetic, bit for bit), so every bounce of a pixel
+// runs in one launch; the list slot then holds the last ray, its hit and its
+// depth for the shading kernel.
 template <int MODE, bool STATS, uint32_t KINDS, int SD, int BLOCK>
 __device__ __forceinline__ void trace_wavefront(const WfParams& P) {
     const SceneTable sv{P.B.scenes};
@@ -787,6 +828,7 @@ __device__ __forceinline__ void trace_wavefront(const WfParams& P) {
     uint32_t item = kNoItem;
     bool heat = false;
     uint32_t t0 = 0;  // clock() at the ray's start (heatmap only)
+    uint32_t depth = 0;  // bits 0-7: depth of the ray being traced; 8-15: depth the slot started at
     for (;;) {
         uint32_t my = warp_append(work, item == kNoItem);
         if (item == kNoItem) {
@@ -796,7 +838,9 @@ __device__ __forceinline__ void trace_wavefront(const WfParams& P) {
             if (MODE == kModeBounce) {
                 float4 a = P.B.rays[b & 1][2 * (size_t)item], c = P.B.rays[b & 1][2 * (size_t)item + 1];
                 pix = P.B.ray_pixel[b & 1][item];
-                sc = P.B.ray_scene[b & 1][item];
+                const uint32_t rs = P.B.ray_scene[b & 1][item];
+                sc = rs & kSceneMask;
+                depth = (rs >> kSceneBits) * 0x101u;
                 trav_begin(s, sv(sc), mk3(a.x, a.y, a.z), mk3(c.x, c.y, c.z), a.w, c.w);
             } else {
                 float4 a = P.B.shadow_rays[2 * (size_t)item], c = P.B.shadow_rays[2 * (size_t)item + 1];
@@ -813,9 +857,26 @@ __device__ __forceinline__ void trace_wavefront(const WfParams& P) {
             continue;
         // the ray is finished
         if (MODE == kModeBounce) {
+            if (s.hit_inst != kNoHit && (depth & 0xFFu) + 1 < P.B.scenes[s.scene].max_depth) {
+                const NextRay nr =
+                    next_bounce_ray(P.B.scenes[s.scene].env, &P.sbt, s.hit_inst, s.hit_geom, s.hit_prim, s.t, s.u,
+                                    s.v, s.wo, s.wd);
+                if (nr.d.x != 0.0f || nr.d.y != 0.0f || nr.d.z != 0.0f) {
+                    trav_begin(s, sv(s.scene), nr.o, nr.d, 0.01f, 10000.0f);
+                    depth++;
+                    atomicAdd(reinterpret_cast<unsigned long long*>(&P.stats->traversals), 1ull);
+                    atomicAdd(reinterpret_cast<unsigned long long*>(&P.stats->secondary_rays), 1ull);
+                    continue;
+                }
+            }
             P.B.hits[2 * (size_t)item] = make_uint4(__float_as_uint(s.t), __float_as_uint(s.u), __float_as_uint(s.v),
                                                     s.hit_inst);
             P.B.hits[2 * (size_t)item + 1] = make_uint4(s.hit_geom, s.hit_prim, s.front ? 1u : 0u, 0u);
+            if ((depth & 0xFFu) != (depth >> 8)) {  // the slot's ray, for the shading kernel, is the last one traced
+                P.B.rays[b & 1][2 * (size_t)item] = make_float4(s.wo.x, s.wo.y, s.wo.z, 0.01f);
+                P.B.rays[b & 1][2 * (size_t)item + 1] = make_float4(s.wd.x, s.wd.y, s.wd.z, 10000.0f);
+                P.B.ray_scene[b & 1][item] = s.scene | ((depth & 0xFFu) << kSceneBits);
+            }
         } else if (s.hit_inst == kNoHit) {
             atomicAdd(&P.B.lit[P.B.shadow_pixel[item]], 1u);  // shadow_ray_miss clears `shadowed`
         }
@@ -844,17 +905,23 @@ __global__ void __launch_bounds__(BLOCK, trace_warps_per_sm(KINDS) * 32 / BLOCK)
     if (kinds_selected(P.kinds_built, P.B.ctr->kinds, KINDS)) trace_wavefront<MODE, STATS, KINDS, SD, BLOCK>(P);
 }
 
-// The closest-hit and miss programs for every ray of bounce b.  Every lane
+// The closest-hit and miss programs for the last ray of every slot of bounce
+// list b (its depth is in the slot's scene word).  Mirror and portal hits
+// that reach it end their pixel's bounce loop (no depth left, or a zero
+// direction): the traversal already followed every other one.  The append
+// of a further bounce ray is kept for lists traced without that.  Every lane
 // of the (full) warps reaches the appends at the end.
 __global__ void k_shade(const __grid_constant__ WfParams P) {
     const uint32_t b = P.bounce;
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    uint32_t p = kNoPixel, sc = 0, nshadow = 0;
+    uint32_t p = kNoPixel, sc = 0, depth = 0, nshadow = 0;
     bool emit_ray = false, write_colour = false;
     V3 col = mk3(0.0f, 0.0f, 0.0f), nd = mk3(0, 0, 0), no = mk3(0, 0, 0);
     if (i < P.B.ctr->ray_count[b]) p = P.B.ray_pixel[b & 1][i];
     if (p != kNoPixel) {
-        sc = P.B.ray_scene[b & 1][i];
+        const uint32_t rs = P.B.ray_scene[b & 1][i];
+        sc = rs & kSceneMask;
+        depth = rs >> kSceneBits;
         const SceneRec& S = P.B.scenes[sc];
         const Env& e = S.env;
         const RtUniforms& U = *S.uniforms;
@@ -877,17 +944,10 @@ __global__ void k_shade(const __grid_constant__ WfParams P) {
             const uint32_t prog = g ? g->closest_hit : RT_PROGRAM_NONE;
             const V3 bary = mk3((1.0f - hu) - hv, hu, hv);
             TriData td;
-            if (prog == RT_PROGRAM_CLOSEST_HIT_MIRROR && load_triangle(e, custom, h1.x, h1.y, &td)) {
-                // closest_hit_mirror.glsl:11-29
-                V3 ni = interp3(td.n[0], td.n[1], td.n[2], bary);
-                V3 n = normalize3(xform_normal_w2o_t(ir->w2o, ni));
-                float k = 2.0f * dot3(n, rd);
-                nd = sub3(rd, mul3s(n, k));
-                no = add3(ro, mul3s(rd, t));
-            } else if (prog == RT_PROGRAM_CLOSEST_HIT_PORTAL) {
-                // lib.rs:300-312
-                nd = rd;
-                no = add3(add3(ro, mul3s(rd, t)), mk3(0.0f, 5.0f, 0.0f));
+            if (prog == RT_PROGRAM_CLOSEST_HIT_MIRROR || prog == RT_PROGRAM_CLOSEST_HIT_PORTAL) {
+                const NextRay nr = next_bounce_ray(e, &P.sbt, inst, h1.x, h1.y, t, hu, hv, ro, rd);
+                no = nr.o;
+                nd = nr.d;
             } else if (prog == RT_PROGRAM_CLOSEST_HIT_TEXTURED && load_triangle(e, custom, h1.x, h1.y, &td)) {
                 // closest_hit_textured.glsl:174-226
                 V3 ip = interp3(td.p[0], td.p[1], td.p[2], bary);
@@ -918,7 +978,7 @@ __global__ void k_shade(const __grid_constant__ WfParams P) {
             if (nshadow == 0 && !write_colour) {
                 // payload: break when new_ray_direction == 0 (lib.rs:165-171),
                 // and after the last iteration the colour stays reset (black)
-                if ((nd.x == 0.0f && nd.y == 0.0f && nd.z == 0.0f) || b + 1 >= S.max_depth) {
+                if ((nd.x == 0.0f && nd.y == 0.0f && nd.z == 0.0f) || depth + 1 >= S.max_depth) {
                     col = mk3(0.0f, 0.0f, 0.0f);
                     write_colour = true;
                 } else {
@@ -954,7 +1014,7 @@ __global__ void k_shade(const __grid_constant__ WfParams P) {
         R[2 * (size_t)ri] = make_float4(no.x, no.y, no.z, 0.01f);
         R[2 * (size_t)ri + 1] = make_float4(nd.x, nd.y, nd.z, 10000.0f);
         P.B.ray_pixel[(b + 1) & 1][ri] = p;
-        P.B.ray_scene[(b + 1) & 1][ri] = sc;
+        P.B.ray_scene[(b + 1) & 1][ri] = sc | ((depth + 1) << kSceneBits);
     }
 }
 
@@ -1319,13 +1379,13 @@ cudaError_t launch_trace_batch(const TraceBatch& tb, uint8_t* ws, int num_sms, c
     const bool stats = tb.stats != 0;
     note_launch(), k_raygen<<<(uint32_t)((L.slots + 255) / 256), 256, 0, stream>>>(P);
     mark(kKernOther);
-    for (uint32_t b = 0; b < L.max_depth; b++) {
-        P.bounce = b;
-        launch_trace_mode<kModeBounce>(P, tb.config, stats, num_sms, stream);
-        mark(kKernClosest);
-        note_launch(), k_shade<<<(uint32_t)((L.slots + 127) / 128), 128, 0, stream>>>(P);
-        mark(kKernShade);
-    }
+    // the traversal follows every mirror / portal bounce itself, so one closest-hit launch and one
+    // shading launch cover all bounces
+    P.bounce = 0;
+    launch_trace_mode<kModeBounce>(P, tb.config, stats, num_sms, stream);
+    mark(kKernClosest);
+    note_launch(), k_shade<<<(uint32_t)((L.slots + 127) / 128), 128, 0, stream>>>(P);
+    mark(kKernShade);
     if (L.any_shadow) {
         launch_trace_mode<kModeShadow>(P, tb.config, stats, num_sms, stream);
         mark(kKernShadow);
