@@ -8,12 +8,16 @@ from that frame's instance records, then the reference's pipeline
 with 4 blue-noise soft-shadow rays per textured hit and 1 reflection bounce.
 
 Metric: Mrays/s = traversals (primary + shadow + reflection, each traceRay
-counted once) / time.  `value` times the device work with the frames'
-instance records already resident (CUDA events on the launching stream, L2
-flushed between steps by writing a 256 MiB buffer outside the timed events);
-`e2e` times the same frame through the C ABI with host buffers: the frame's
-instance records copied from pinned host memory and the RGBA8 image copied
-back, inside the timed region.
+counted once) / time.  Frames run as the reference runs them, two in flight
+(host.FrameLoop: each with its own instance buffer, TLAS, uniforms, image and
+stream).  `value` times all K frames as one span of CUDA events (start on the
+launching stream, both frame streams joined at the end) with the frames'
+instance records already resident and the L2 flushed before every frame by a
+256 MiB write on its stream (inside the span); `e2e` times the same loop
+through the C ABI with host buffers: each frame's instance records copied in
+from pinned host memory and its RGBA8 image copied back, inside the span.
+Per-kernel times and the roofline come from serial frames outside the span.
+Other workloads: --workload precision / batch / serve (see their functions).
 
 --impl reference runs the CPU oracle (the restatement of the reference's
 shader logic; the reference itself needs a Vulkan ray-tracing driver, which
@@ -256,58 +260,69 @@ def bench_ours(args):
     frames_dev = [host.Device.upload(f) for f in frames_host]
     uniforms = [scenes.scene_full(k, W, H, models=models).uniforms for k in range(FRAMES)]
     uni_dev = [host.Device.upload(np.frombuffer(bytes(u), np.uint8)) for u in uniforms]
-    fr = host.PerFrameResources(dev, gs, W, H)
-    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    # the reference's frame loop: two frames in flight, each with its own instance buffer, TLAS,
+    # uniforms, image and stream; every frame rebuilds its TLAS from that frame's instance records
+    loop = host.FrameLoop(dev, gs, W, H, frames_in_flight=2)
+    flushes = [torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda") for _ in range(2)]
     stream = torch.cuda.current_stream()
-    sh = host.Device.stream_handle(stream)
-    scratch = gs.scratch
 
-    def step(k: int, inst_tensor, flags: int = 0):
-        gs.tlas.rebuild_tlas(dev, inst_tensor, n_inst, scratch, stream)
-        push = gs.push_constants(uni_dev[k % FRAMES].data_ptr(), gs.tlas)
-        d = abi.RtTraceRaysDesc()
-        d.width, d.height, d.max_trace_depth, d.shadow_ray_count = W, H, 2, 4
-        d.flags = flags
-        d.image_address = fr.image.data_ptr()
-        dev.check(lib.rt_cmd_trace_rays(dev.ctx, C.byref(push), None, C.byref(d), sh))
+    def frame(k: int, **kw):
+        # the L2 flush (a 256 MiB write) runs on the frame's stream before its work
+        return loop.record(k, 2, 4, uniforms_dev=uni_dev[k % FRAMES],
+                           before=lambda st: flushes[k & 1].fill_(k & 0xFF), **kw)
 
     def read_timings() -> dict:
         tt = abi.RtTraceTimings()
         dev.check(lib.rt_ctx_read_trace_timings(dev.ctx, C.byref(tt)))
         return tt.as_dict()
 
+    loop.begin()
     for k in range(args.warmup):
-        step(k, frames_dev[k % FRAMES])
+        frame(k, instances=frames_dev[k % FRAMES])
+    loop.end()
     torch.cuda.synchronize()
     dev.read_stats(reset=True)
 
-    # ---- device-resident timing (value) ----
+    # ---- device-resident timing (value): one span over all frames, both streams ----
     clocks = ClockSampler(local)
     clocks.start()
     launches0 = lib.rt_kernel_launch_count()
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    kernel_times = []
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
-    for i in range(args.steps):
-        flush.fill_(i & 0xFF)
-        ev[i][0].record(stream)
-        step(i, frames_dev[i % FRAMES], abi.RT_TRACE_FLAG_KERNEL_TIMINGS)
-        ev[i][1].record(stream)
-        kernel_times.append(read_timings())  # waits for this step; outside the device-timed events
+    e_begin, e_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e_begin.record(stream)
+    loop.begin()
+    for k in range(args.steps):
+        frame(k, instances=frames_dev[k % FRAMES])
+    loop.end()
+    e_end.record(stream)
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
     launches = lib.rt_kernel_launch_count() - launches0
     clk = clocks.stop()
-    step_ms = [a.elapsed_time(b) for a, b in ev]
+    total_ms = e_begin.elapsed_time(e_end)
+    stats = dev.read_stats(reset=True)
+    rays_local = stats["traversals"]
+
+    # ---- per-kernel split of serial frames (CUDA events after each kernel; outside the value span) ----
+    kernel_times, serial_ms = [], []
+    for k in range(min(args.steps, 10)):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        flushes[0].fill_(k & 0xFF)
+        torch.cuda.synchronize()
+        e0.record(loop.streams[0])
+        loop.record(2 * k, 2, 4, instances=frames_dev[k % FRAMES], uniforms_dev=uni_dev[k % FRAMES],
+                    flags=abi.RT_TRACE_FLAG_KERNEL_TIMINGS)
+        e1.record(loop.streams[0])
+        torch.cuda.synchronize()
+        serial_ms.append(e0.elapsed_time(e1))
+        kernel_times.append(read_timings())
     trace_ms = [kt["total_ms"] for kt in kernel_times]
     traversal_ms = [kt["trace_ms"] for kt in kernel_times]
     traversal_launches = kernel_times[0]["trace_launches"]
-    stats = dev.read_stats(reset=True)
-    total_ms = sum(step_ms)
-    rays_local = stats["traversals"]
+    dev.read_stats(reset=True)
     if dist:
         t = torch.tensor([total_ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -319,37 +334,28 @@ def bench_ours(args):
         rays_all = float(rays_local)
     value = rays_all / (total_ms / 1e3) / 1e6
 
-    # ---- end-to-end through the C ABI with host buffers (e2e) ----
+    # ---- end-to-end through the C ABI with host buffers (e2e): each frame's instance records come
+    # from pinned host memory and its RGBA8 image goes back to pinned host memory, on its stream ----
     pinned_frames = [torch.from_numpy(f.view(np.uint8).reshape(-1).copy()).pin_memory() for f in frames_host]
-    inst_staging = torch.empty(n_inst * 64, dtype=torch.uint8, device="cuda")
-    image_host = torch.empty((H, W, 4), dtype=torch.uint8).pin_memory()
-    e2e_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    images_host = [torch.empty((H, W, 4), dtype=torch.uint8).pin_memory() for _ in range(2)]
     dev.read_stats(reset=True)
     torch.cuda.synchronize()
-    for i in range(args.steps):
-        flush.fill_(i & 0xFF)
-        e2e_ev[i][0].record(stream)
-        inst_staging.copy_(pinned_frames[i % FRAMES], non_blocking=True)
-        step(i, inst_staging)
-        image_host.copy_(fr.image, non_blocking=True)
-        e2e_ev[i][1].record(stream)
+    e_begin.record(stream)
+    loop.begin()
+    for k in range(args.steps):
+        frame(k, instances_host=pinned_frames[k % FRAMES], image_host=images_host[k & 1])
+    loop.end()
+    e_end.record(stream)
     torch.cuda.synchronize()
     e2e_stats = dev.read_stats(reset=True)
-    e2e_ms = sum(a.elapsed_time(b) for a, b in e2e_ev)
+    e2e_ms = e_begin.elapsed_time(e_end)
     e2e_value = e2e_stats["traversals"] / (e2e_ms / 1e3) / 1e6 * (world if world > 1 else 1)
 
     # ---- roofline of the dominant kernel (trace) ----
     # algorithmic bytes per launch from an untimed statistics run of frame 0
-    step(0, frames_dev[0])
-    torch.cuda.synchronize()
     dev.read_stats(reset=True)
-    gs.tlas.rebuild_tlas(dev, frames_dev[0], n_inst, scratch, stream)
-    push = gs.push_constants(uni_dev[0].data_ptr(), gs.tlas)
-    d = abi.RtTraceRaysDesc()
-    d.width, d.height, d.max_trace_depth, d.shadow_ray_count = W, H, 2, 4
-    d.flags = abi.RT_TRACE_FLAG_COLLECT_STATS
-    d.image_address = fr.image.data_ptr()
-    dev.check(lib.rt_cmd_trace_rays(dev.ctx, C.byref(push), None, C.byref(d), sh))
+    loop.record(0, 2, 4, instances=frames_dev[0], uniforms_dev=uni_dev[0], flags=abi.RT_TRACE_FLAG_COLLECT_STATS)
+    torch.cuda.synchronize()
     s = dev.read_stats(reset=True)
     # the traversal kernel (k_trace) is the dominant kernel; per frame it runs
     # once per bounce (closest hit) and once for the shadow rays
@@ -373,12 +379,14 @@ def bench_ours(args):
             "config": {"workload": WORKLOAD, "width": W, "height": H, "instances": n_inst,
                        "instanced_triangles": sc0.instanced_triangles, "frames": FRAMES,
                        "path": "plain FP32 8-wide BVH", "parallelism": f"replicas x{world}",
-                       "l2": "flushed between steps (256 MiB write outside the timed events)",
+                       "frame_loop": "2 frames in flight (own instance buffer, TLAS, uniforms, image, stream)",
+                       "l2": "flushed before every frame on its stream (256 MiB write, inside the timed span)",
                        "traversals_per_step": rays_local / args.steps, "blas_build_ms": blas_build_ms,
+                       "serial_ms_per_frame": sum(serial_ms) / len(serial_ms),
                        "trace_pipeline_ms_per_step": sum(trace_ms) / len(trace_ms),
                        "traversal_ms_per_step": sum(traversal_ms) / len(traversal_ms),
                        "shade_ms_per_step": sum(kt["shade_ms"] for kt in kernel_times) / len(kernel_times),
-                       "tlas_build_ms_per_step": (sum(step_ms) - sum(trace_ms)) / args.steps},
+                       "tlas_build_and_flush_ms_per_step": (sum(serial_ms) - sum(trace_ms)) / len(serial_ms)},
             "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": n_inst * 64,
                     "d2h_bytes_per_step": W * H * 4},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",

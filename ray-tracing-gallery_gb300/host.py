@@ -343,6 +343,61 @@ class PerFrameResources:
                                                             Device.stream_handle(stream)))
 
 
+class FrameLoop:
+    """The reference's double-buffered frame loop (src/main.rs:600-668,
+    1131-1170): `frames_in_flight` frames, each with its own instance buffer,
+    TLAS clone, uniforms, image and CUDA stream (the Vulkan fences and
+    semaphores become stream order).  Frame k uses slot k % frames_in_flight,
+    so frame N+1's instance upload, TLAS rebuild and ray generation run while
+    frame N is still being traced."""
+
+    def __init__(self, device: Device, gpu_scene: GpuScene, width: int, height: int, frames_in_flight: int = 2,
+                 radiance: bool = False):
+        self.device = device
+        self.gpu_scene = gpu_scene
+        self.slots = [PerFrameResources(device, gpu_scene, width, height, radiance=radiance, clone_tlas=True)
+                      for _ in range(frames_in_flight)]
+        self.streams = [torch.cuda.Stream() for _ in range(frames_in_flight)]
+        self.scratch = [ScratchBuffer(f"frame scratch {i}") for i in range(frames_in_flight)]
+
+    def begin(self) -> None:
+        """Orders every slot after the work already queued on the current stream."""
+        ev = torch.cuda.Event()
+        ev.record()
+        for s in self.streams:
+            s.wait_event(ev)
+
+    def record(self, k: int, max_trace_depth: int, shadow_ray_count: int, instances=None, instances_host=None,
+               uniforms_dev=None, image_host=None, flags: int = 0, before=None) -> PerFrameResources:
+        """Frame k: new instance records (a device tensor, or pinned host bytes
+        copied in on the slot's stream), TLAS rebuild, uniforms (a device copy),
+        the trace, and optionally the image copied to pinned host memory."""
+        i = k % len(self.slots)
+        fr, st = self.slots[i], self.streams[i]
+        with torch.cuda.stream(st):
+            if before is not None:
+                before(st)
+            if instances_host is not None:
+                fr.instances_buffer.copy_(instances_host, non_blocking=True)
+                instances = fr.instances_buffer
+            if instances is not None:
+                fr.tlas.rebuild_tlas(self.device, instances, fr.num_instances, self.scratch[i], st)
+            if uniforms_dev is not None:
+                fr.uniforms_buffer.copy_(uniforms_dev, non_blocking=True)
+            fr.record(max_trace_depth, shadow_ray_count, flags, stream=st)
+            if image_host is not None:
+                image_host.copy_(fr.image, non_blocking=True)
+        return fr
+
+    def end(self) -> None:
+        """Makes the current stream wait for every slot."""
+        cur = torch.cuda.current_stream()
+        for s in self.streams:
+            ev = torch.cuda.Event()
+            ev.record(s)
+            cur.wait_event(ev)
+
+
 def batch_scene(frame: PerFrameResources, max_trace_depth: int, shadow_ray_count: int,
                 flags: int = 0) -> abi.RtBatchScene:
     """The RtBatchScene of one frame (its scene's own texture table, if any)."""
