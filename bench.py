@@ -92,6 +92,20 @@ def dist_env():
     return rank, world, local
 
 
+def reduce_over_ranks(dist, total_ms: float, rays: float, device: str = "cuda") -> tuple[float, float]:
+    """Whole-job numbers of N replicas: the slowest rank's time and the sum of
+    every rank's rays (no data is exchanged otherwise).  `dist` None = one rank."""
+    if dist is None:
+        return total_ms, rays
+    import torch
+
+    t = torch.tensor([total_ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    r = torch.tensor([rays], dtype=torch.float64, device=device)
+    dist.all_reduce(r, op=dist.ReduceOp.SUM)
+    return float(t.item()), float(r.item())
+
+
 def profiled_traffic(name: str = "k_trace_full_1080p.md"):
     """DRAM bytes per traversal launch from the committed ncu summary of this
     workload (profiles/<name>, line `dram_bytes_per_launch: N`)."""
@@ -323,15 +337,7 @@ def bench_ours(args):
     traversal_ms = [kt["trace_ms"] for kt in kernel_times]
     traversal_launches = kernel_times[0]["trace_launches"]
     dev.read_stats(reset=True)
-    if dist:
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-        r = torch.tensor([float(rays_local)], device="cuda")
-        dist.all_reduce(r)
-        rays_all = float(r.item())
-    else:
-        rays_all = float(rays_local)
+    total_ms, rays_all = reduce_over_ranks(dist, total_ms, float(rays_local))
     value = rays_all / (total_ms / 1e3) / 1e6
 
     # ---- end-to-end through the C ABI with host buffers (e2e): each frame's instance records come
@@ -546,11 +552,7 @@ def bench_precision(args):
     launches = lib.rt_kernel_launch_count() - launches0
     clk = clocks.stop()
     for arm in arms.values():
-        total_ms = sum(arm["ms"])
-        if dist:
-            t = torch.tensor([total_ms], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            total_ms = float(t.item())
+        total_ms, _ = reduce_over_ranks(dist, sum(arm["ms"]), 0.0)
         arm["total_ms"] = total_ms
         arm["value"] = n * world * args.steps / (total_ms / 1e3) / 1e6
 
@@ -812,10 +814,7 @@ def bench_batch(args):
     if dist:
         dist.barrier()
     clk = clocks.stop()
-    if dist:
-        t = torch.tensor([ms_graph], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_graph = float(t.item())
+    ms_graph, _ = reduce_over_ranks(dist, ms_graph, 0.0)
     value = rays_per_step * world * args.steps / (ms_graph / 1e3) / 1e6
 
     # kernel split and roofline of the traversal (a direct call with per-kernel events)

@@ -304,3 +304,37 @@ def test_host_buffer_query_matches_device_query(device):
                                                          chunk, host.Device.stream_handle()))
         torch.cuda.synchronize()
         _assert_hits_equal(hits_h.numpy().view(abi.HIT_DTYPE), ref, f"host query, chunk {chunk}")
+
+
+def test_double_buffered_frame_loop_matches_serial_frames(device):
+    """host.FrameLoop (two frames in flight on two streams, each with its own
+    TLAS rebuilt from that frame's instances) renders every frame exactly as
+    a serial loop over one frame resource does."""
+    import torch
+
+    host = _host()
+    W, H = 160, 96
+    models = scenes.full_scene_models()
+    sc0 = scenes.scene_full(0, W, H, models=models)
+    gs = _gpu_scene(device, sc0)
+    frames = [host.Device.upload(gs.patch_instances(scenes.full_scene_instances(k))) for k in range(6)]
+    unis = [host.Device.upload(np.frombuffer(bytes(scenes.scene_full(k, W, H, models=models).uniforms), np.uint8))
+            for k in range(6)]
+    serial = host.PerFrameResources(device, gs, W, H, clone_tlas=True)
+    ref = []
+    for k in range(6):
+        serial.tlas.rebuild_tlas(device, frames[k], gs.num_instances, gs.scratch)
+        serial.uniforms_buffer.copy_(unis[k])
+        serial.record(2, 4)
+        torch.cuda.synchronize()
+        ref.append(serial.image.clone())
+    loop = host.FrameLoop(device, gs, W, H, frames_in_flight=2)
+    got = [torch.empty_like(r, device="cpu").pin_memory() for r in ref]
+    loop.begin()
+    for k in range(6):
+        loop.record(k, 2, 4, instances=frames[k], uniforms_dev=unis[k], image_host=got[k])
+    loop.end()
+    torch.cuda.synchronize()
+    for k in range(6):
+        assert torch.equal(got[k], ref[k].cpu()), f"frame {k}"
+    assert len({int(r.float().sum()) for r in ref}) > 1  # the frames differ
