@@ -17,6 +17,8 @@ instance records already resident and the L2 flushed before every frame by a
 through the C ABI with host buffers: each frame's instance records copied in
 from pinned host memory and its RGBA8 image copied back, inside the span.
 Per-kernel times and the roofline come from serial frames outside the span.
+--workload scene runs the same loop on the reference's default scene built
+from GLB / PNG files (DefaultSceneFrames: 1280x720, TLAS refit per frame).
 Other workloads: --workload precision / batch / serve (see their functions).
 
 --impl reference runs the CPU oracle (the restatement of the reference's
@@ -69,12 +71,13 @@ def parse_args():
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--width", type=int, default=WIDTH)
-    p.add_argument("--height", type=int, default=HEIGHT)
-    p.add_argument("--workload", default="frame", choices=["frame", "precision", "batch", "serve"],
-                   help="frame: the full 1080p frame (default); precision: 10,485,760-triangle icosphere, "
-                        "4M random rays, quantised vs FP32 nodes; batch: 64 scenes in one batched launch; "
-                        "serve: Poisson request stream over 32 resident scenes")
+    p.add_argument("--width", type=int, default=None, help="frame: 1920, scene: 1280")
+    p.add_argument("--height", type=int, default=None, help="frame: 1080, scene: 720")
+    p.add_argument("--workload", default="frame", choices=["frame", "scene", "precision", "batch", "serve"],
+                   help="frame: the full 1080p frame (default); scene: the reference's default scene from "
+                        "GLB / PNG files at 1280x720 with a TLAS refit per frame; precision: 10,485,760-triangle "
+                        "icosphere, 4M random rays, quantised vs FP32 nodes; batch: 64 scenes in one batched "
+                        "launch; serve: Poisson request stream over 32 resident scenes")
     p.add_argument("--batch-scenes", type=int, default=64, help=argparse.SUPPRESS)
     p.add_argument("--serve-seconds", type=float, default=120.0, help="serve: length of the request stream")
     p.add_argument("--serve-rate", type=float, default=400.0, help=argparse.SUPPRESS)
@@ -82,7 +85,85 @@ def parse_args():
     p.add_argument("--serve-budget-gb", type=float, default=150.0, help=argparse.SUPPRESS)
     p.add_argument("--precision-level", type=int, default=9, help=argparse.SUPPRESS)
     p.add_argument("--precision-rays", type=int, default=PRECISION_RAYS, help=argparse.SUPPRESS)
-    return p.parse_args()
+    args = p.parse_args()
+    dw, dh = (1280, 720) if args.workload == "scene" else (WIDTH, HEIGHT)
+    args.width = args.width or dw
+    args.height = args.height or dh
+    return args
+
+
+class FullSceneFrames:
+    """The default workload: the full plain feature set (module docstring)."""
+
+    key = "frame"
+    description = WORKLOAD
+    path = "plain FP32 8-wide BVH"
+    depth, shadows, refit = 2, 4, False
+    profile = "k_trace_full_1080p.md"
+    data = "synthetic (procedural scenes from seeds)"
+
+    def __init__(self, width: int, height: int):
+        self.width, self.height = width, height
+        self.models = scenes.full_scene_models()
+
+    def scene(self, k: int):
+        return scenes.scene_full(k % FRAMES, self.width, self.height, models=self.models)
+
+    def instances(self, k: int) -> np.ndarray:
+        return scenes.full_scene_instances(k % FRAMES)
+
+    def uniforms(self, k: int):
+        return self.scene(k).uniforms
+
+    def loop_note(self) -> str:
+        return "2 frames in flight (own instance buffer, TLAS, uniforms, image, stream)"
+
+
+class DefaultSceneFrames:
+    """The reference's default scene (src/scene.rs:35-204) assembled from GLB /
+    PNG files that librtcore decodes (the package's stand-in files of the
+    reference's kinds and sizes), rendered as the reference's loop renders
+    it: the figure turns 0.05 rad per frame, the frame's instance records are
+    written and its TLAS refitted in place, two frames in flight."""
+
+    key = "scene"
+    description = ("the reference's default scene from GLB / PNG files decoded by librtcore (textured plane x10, "
+                   "two linked tori, a 45,448-triangle textured figure turning 0.05 rad per frame, portal plane, "
+                   "alpha-masked fence, 100 small tori half of them mirrors), 3 bounce iterations, 2 blue-noise "
+                   "soft shadows (radius 0.05), TLAS refitted in place every frame")
+    path = "plain FP32 8-wide BVH, TLAS refit"
+    depth, shadows, refit = 3, 2, True
+    profile = None
+    data = "synthetic stand-in asset files (GLB / PNG written from seeds), decoded by librtcore"
+
+    def __init__(self, width: int, height: int):
+        from rtgallery import assets
+
+        self.assets = assets
+        self.width, self.height = width, height
+        self.sc0 = assets.default_scene(assets.standin_assets(), width, height, frame=0)
+
+    def scene(self, k: int):
+        import copy
+
+        sc = copy.copy(self.sc0)
+        sc.instances = self.instances(k)
+        sc.uniforms = self.uniforms(k)
+        return sc
+
+    def instances(self, k: int) -> np.ndarray:
+        return self.assets.default_scene_instances(0, k % FRAMES)
+
+    def uniforms(self, k: int):
+        return self.assets.default_scene_uniforms(self.width, self.height, k % FRAMES + 1)
+
+    def loop_note(self) -> str:
+        return "2 frames in flight (own instance buffer, TLAS refitted in place, uniforms, image, stream)"
+
+
+def frame_workload(args):
+    cls = DefaultSceneFrames if args.workload == "scene" else FullSceneFrames
+    return cls(args.width, args.height)
 
 
 def dist_env():
@@ -178,20 +259,20 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
-def cpu_baseline(sc_frames, width, height, budget_s: float = 12.0) -> dict:
+def cpu_baseline(wl, budget_s: float = 12.0) -> dict:
     """The oracle (FP32, all host threads) rendering bands of the workload's
     frames until about `budget_s` seconds of CPU work."""
     from oracle.oracle import OracleScene, default_threads
 
     threads = default_threads()
-    models = scenes.full_scene_models()
+    height = wl.height
     rays = 0
     t_total = 0.0
     frames_done = 0
     band = max(8, height // 8)
     o = None
     for k in range(FRAMES):
-        sc = scenes.scene_full(k % FRAMES, width, height, models=models)
+        sc = wl.scene(k)
         if o is None:
             o = OracleScene(sc)
         else:
@@ -217,12 +298,12 @@ def bench_reference(args):
     from oracle.oracle import OracleScene, default_threads
 
     threads = default_threads()
-    models = scenes.full_scene_models()
+    wl = frame_workload(args)
     band = max(8, args.height // 16)
     o = None
     times, rays = [], 0
     for k in range(args.warmup + args.steps):
-        sc = scenes.scene_full(k % FRAMES, args.width, args.height, models=models)
+        sc = wl.scene(k)
         if o is None:
             o = OracleScene(sc)
         t = time.perf_counter()
@@ -239,7 +320,7 @@ def bench_reference(args):
         "impl": "reference", "metric": "Mrays/s", "value": value, "unit": "Mrays/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "sample": f"{band}-row band of each frame", "width": args.width,
+        "config": {"workload": wl.description, "sample": f"{band}-row band of each frame", "width": args.width,
                    "height": args.height},
         "cpu_baseline": {"value": value, "unit": "Mrays/s", "cores": threads, "kind": "port",
                          "sample": f"{band} of {args.height} rows per frame, {args.steps} frames"},
@@ -263,26 +344,28 @@ def bench_ours(args):
     dev = host.Device()
     lib = dev.lib
     W, H = args.width, args.height
-    models = scenes.full_scene_models()
-    sc0 = scenes.scene_full(0, W, H, models=models)
+    wl = frame_workload(args)
+    DEPTH, SHADOWS = wl.depth, wl.shadows
+    sc0 = wl.scene(0)
     t0 = time.perf_counter()
     gs = host.GpuScene(dev, sc0)
     torch.cuda.synchronize()
     blas_build_ms = 1e3 * (time.perf_counter() - t0)
     n_inst = gs.num_instances
-    frames_host = [gs.patch_instances(scenes.full_scene_instances(k)) for k in range(FRAMES)]
+    frames_host = [gs.patch_instances(wl.instances(k)) for k in range(FRAMES)]
     frames_dev = [host.Device.upload(f) for f in frames_host]
-    uniforms = [scenes.scene_full(k, W, H, models=models).uniforms for k in range(FRAMES)]
+    uniforms = [wl.uniforms(k) for k in range(FRAMES)]
     uni_dev = [host.Device.upload(np.frombuffer(bytes(u), np.uint8)) for u in uniforms]
     # the reference's frame loop: two frames in flight, each with its own instance buffer, TLAS,
-    # uniforms, image and stream; every frame rebuilds its TLAS from that frame's instance records
+    # uniforms, image and stream; every frame rebuilds (or refits) its TLAS from that frame's
+    # instance records
     loop = host.FrameLoop(dev, gs, W, H, frames_in_flight=2)
     flushes = [torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda") for _ in range(2)]
     stream = torch.cuda.current_stream()
 
     def frame(k: int, **kw):
         # the L2 flush (a 256 MiB write) runs on the frame's stream before its work
-        return loop.record(k, 2, 4, uniforms_dev=uni_dev[k % FRAMES],
+        return loop.record(k, DEPTH, SHADOWS, uniforms_dev=uni_dev[k % FRAMES], refit=wl.refit,
                            before=lambda st: flushes[k & 1].fill_(k & 0xFF), **kw)
 
     def read_timings() -> dict:
@@ -327,8 +410,8 @@ def bench_ours(args):
         flushes[0].fill_(k & 0xFF)
         torch.cuda.synchronize()
         e0.record(loop.streams[0])
-        loop.record(2 * k, 2, 4, instances=frames_dev[k % FRAMES], uniforms_dev=uni_dev[k % FRAMES],
-                    flags=abi.RT_TRACE_FLAG_KERNEL_TIMINGS)
+        loop.record(2 * k, DEPTH, SHADOWS, instances=frames_dev[k % FRAMES], uniforms_dev=uni_dev[k % FRAMES],
+                    flags=abi.RT_TRACE_FLAG_KERNEL_TIMINGS, refit=wl.refit)
         e1.record(loop.streams[0])
         torch.cuda.synchronize()
         serial_ms.append(e0.elapsed_time(e1))
@@ -360,7 +443,8 @@ def bench_ours(args):
     # ---- roofline of the dominant kernel (trace) ----
     # algorithmic bytes per launch from an untimed statistics run of frame 0
     dev.read_stats(reset=True)
-    loop.record(0, 2, 4, instances=frames_dev[0], uniforms_dev=uni_dev[0], flags=abi.RT_TRACE_FLAG_COLLECT_STATS)
+    loop.record(0, DEPTH, SHADOWS, instances=frames_dev[0], uniforms_dev=uni_dev[0],
+                flags=abi.RT_TRACE_FLAG_COLLECT_STATS, refit=wl.refit)
     torch.cuda.synchronize()
     s = dev.read_stats(reset=True)
     # the traversal kernel (k_trace) is the dominant kernel; per frame it runs
@@ -371,21 +455,22 @@ def bench_ours(args):
     avg_launch_s = sum(traversal_ms) / len(traversal_ms) / traversal_launches / 1e3
     peak, peak_kind = measured_peaks()
     achieved = bytes_per_launch / avg_launch_s / 1e9
-    traffic = profiled_traffic()
+    traffic = profiled_traffic(wl.profile) if wl.profile else None
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(None, W, H)
+        cpu = cpu_baseline(wl)
 
     if rank == 0:
         line = {
             "metric": "Mrays/s", "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (procedural scenes from seeds)",
-            "config": {"workload": WORKLOAD, "width": W, "height": H, "instances": n_inst,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": wl.data,
+            "config": {"workload": wl.description, "width": W, "height": H, "instances": n_inst,
                        "instanced_triangles": sc0.instanced_triangles, "frames": FRAMES,
-                       "path": "plain FP32 8-wide BVH", "parallelism": f"replicas x{world}",
-                       "frame_loop": "2 frames in flight (own instance buffer, TLAS, uniforms, image, stream)",
+                       "max_trace_depth": DEPTH, "shadow_rays": SHADOWS,
+                       "path": wl.path, "parallelism": f"replicas x{world}",
+                       "frame_loop": wl.loop_note(),
                        "l2": "flushed before every frame on its stream (256 MiB write, inside the timed span)",
                        "traversals_per_step": rays_local / args.steps, "blas_build_ms": blas_build_ms,
                        "serial_ms_per_frame": sum(serial_ms) / len(serial_ms),

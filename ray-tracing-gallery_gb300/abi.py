@@ -263,6 +263,22 @@ class RtServeStats(C.Structure):
         return {f: getattr(self, f) for f, _ in self._fields_}
 
 
+# include/rtassets.h
+class RtGlbInfo(C.Structure):
+    _fields_ = [("vertex_count", C.c_uint32), ("geometry_count", C.c_uint32), ("image_count", C.c_uint32),
+                ("primitive_count", C.c_uint32), ("triangle_count", C.c_uint64)]
+
+
+class RtGlbGeometry(C.Structure):
+    _fields_ = [("index_count", C.c_uint32), ("opaque", C.c_uint32), ("diffuse_image", C.c_int32),
+                ("metallic_roughness_image", C.c_int32), ("normal_map_image", C.c_int32), ("_padding", C.c_uint32)]
+
+
+class RtGlbImage(C.Structure):
+    _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("format", C.c_uint32), ("filter", C.c_uint32),
+                ("byte_size", C.c_uint64)]
+
+
 class RtRay(C.Structure):
     _fields_ = [("origin", C.c_float * 3), ("tmin", C.c_float), ("direction", C.c_float * 3), ("tmax", C.c_float)]
 
@@ -365,6 +381,15 @@ EXPORTED_FUNCTIONS = {
     "rt_server_submit": (C.c_int32, [C.c_void_p, C.POINTER(RtServeRequest), C.POINTER(C.c_uint64)]),
     "rt_server_wait": (C.c_int32, [C.c_void_p, C.c_uint64, C.c_uint32, C.POINTER(RtServeResult)]),
     "rt_server_stats": (C.c_int32, [C.c_void_p, C.POINTER(RtServeStats)]),
+    "rt_png_decode_rgba8": (C.c_int32, [C.c_void_p, C.c_uint64, C.c_void_p, C.c_uint64, C.POINTER(C.c_uint32),
+                                         C.POINTER(C.c_uint32)]),
+    "rt_glb_load": (C.c_int32, [C.c_void_p, C.c_uint64, C.POINTER(C.c_void_p)]),
+    "rt_glb_info": (C.c_int32, [C.c_void_p, C.POINTER(RtGlbInfo)]),
+    "rt_glb_read_vertices": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "rt_glb_read_geometry": (C.c_int32, [C.c_void_p, C.c_uint32, C.POINTER(RtGlbGeometry), C.c_void_p,
+                                          C.c_uint64]),
+    "rt_glb_read_image": (C.c_int32, [C.c_void_p, C.c_uint32, C.POINTER(RtGlbImage), C.c_void_p, C.c_uint64]),
+    "rt_glb_destroy": (C.c_int32, [C.c_void_p]),
     "rt_ctx_autotune": (C.c_int32, [C.c_void_p, C.POINTER(RtBatchScene), C.c_uint32, C.POINTER(RtShaderBindingTable),
                                      C.c_uint32, C.c_void_p, C.POINTER(RtAutotuneReport)]),
     "rt_cmd_trace_ray_buffer": (C.c_int32, [C.c_void_p, C.c_uint64, C.POINTER(RtPushConstantBufferAddresses),
@@ -457,3 +482,4 @@ def check_layouts() -> None:
     assert C.sizeof(RtServerConfig) == 24 and C.sizeof(RtServeScene) == 40
     assert C.sizeof(RtServeRequest) == 224 and RtServeRequest.image_device.offset == 200
     assert C.sizeof(RtServeResult) == 32 and C.sizeof(RtServeStats) == 64
+    assert C.sizeof(RtGlbInfo) == C.sizeof(RtGlbGeometry) == C.sizeof(RtGlbImage) == 24

@@ -19,7 +19,7 @@ CSRC = PKG_DIR / "csrc"
 BUILD_DIR = PKG_DIR / "_build"
 INCLUDE_DIR = PKG_DIR.parent / "include"
 LIB_NAME = "librtcore.so"
-SOURCES = ["rt_api.cu", "rt_build.cu", "rt_trace.cu", "rt_serve.cu"]
+SOURCES = ["rt_api.cu", "rt_build.cu", "rt_trace.cu", "rt_serve.cu", "rt_assets.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = [
     "-O3",
@@ -49,7 +49,7 @@ def library_path() -> Path:
 def _inputs() -> list[Path]:
     files = [CSRC / s for s in SOURCES]
     files += sorted(CSRC.glob("*.cuh")) + sorted(CSRC.glob("*.h"))
-    files += [INCLUDE_DIR / "rtcore.h", Path(__file__)]
+    files += sorted(INCLUDE_DIR.glob("*.h")) + [Path(__file__)]
     return files
 
 

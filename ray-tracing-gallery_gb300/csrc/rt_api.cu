@@ -14,6 +14,7 @@
 #include <string>
 #include <vector>
 
+#include "rt_error.h"
 #include "rt_internal.h"
 
 using namespace rt;
@@ -40,6 +41,20 @@ int32_t fail(int32_t code, const char* fmt, ...) {
     g_last_error = buf;
     return code;
 }
+
+}  // namespace
+
+int32_t rt::report_error(int32_t code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return code;
+}
+
+namespace {
 
 int32_t cuda_fail(cudaError_t e, const char* what) {
     return fail(e == cudaErrorMemoryAllocation ? RT_ERR_OOM : RT_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));

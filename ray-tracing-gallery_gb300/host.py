@@ -368,10 +368,13 @@ class FrameLoop:
             s.wait_event(ev)
 
     def record(self, k: int, max_trace_depth: int, shadow_ray_count: int, instances=None, instances_host=None,
-               uniforms_dev=None, image_host=None, flags: int = 0, before=None) -> PerFrameResources:
+               uniforms_dev=None, image_host=None, flags: int = 0, before=None,
+               refit: bool = False) -> PerFrameResources:
         """Frame k: new instance records (a device tensor, or pinned host bytes
-        copied in on the slot's stream), TLAS rebuild, uniforms (a device copy),
-        the trace, and optionally the image copied to pinned host memory."""
+        copied in on the slot's stream), TLAS rebuild (or, with refit, the
+        in-place update of DefaultScene::write_resources, scene.rs:167-204),
+        uniforms (a device copy), the trace, and optionally the image copied
+        to pinned host memory."""
         i = k % len(self.slots)
         fr, st = self.slots[i], self.streams[i]
         with torch.cuda.stream(st):
@@ -380,7 +383,9 @@ class FrameLoop:
             if instances_host is not None:
                 fr.instances_buffer.copy_(instances_host, non_blocking=True)
                 instances = fr.instances_buffer
-            if instances is not None:
+            if instances is not None and refit:
+                fr.tlas.update_tlas(self.device, instances, fr.num_instances, self.scratch[i], st)
+            elif instances is not None:
                 fr.tlas.rebuild_tlas(self.device, instances, fr.num_instances, self.scratch[i], st)
             if uniforms_dev is not None:
                 fr.uniforms_buffer.copy_(uniforms_dev, non_blocking=True)

@@ -10,12 +10,14 @@ import pytest
 from rtgallery import abi
 
 ROOT = Path(__file__).resolve().parent.parent
-HEADER = ROOT / "include" / "rtcore.h"
+HEADERS = sorted((ROOT / "include").glob("*.h"))
 
 
 def declared_functions() -> set[str]:
-    text = HEADER.read_text()
-    return set(re.findall(r"RTCORE_API\s+[\w\s\*]+?\b(rt_\w+)\s*\(", text))
+    names = set()
+    for h in HEADERS:
+        names |= set(re.findall(r"RTCORE_API\s+[\w\s\*]+?\b(rt_\w+)\s*\(", h.read_text()))
+    return names
 
 
 def test_layouts_match_reference():
@@ -24,7 +26,7 @@ def test_layouts_match_reference():
 
 def test_header_static_asserts_compile(tmp_path):
     src = tmp_path / "t.c"
-    src.write_text('#include "rtcore.h"\nint main(void){return 0;}\n')
+    src.write_text("".join(f'#include "{h.name}"\n' for h in HEADERS) + "int main(void){return 0;}\n")
     r = subprocess.run(["gcc", "-std=c11", "-Wall", "-Werror", "-I", str(ROOT / "include"), str(src), "-o",
                         str(tmp_path / "t")], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
