@@ -1,20 +1,25 @@
 // rt_build.cu — BLAS / TLAS construction, TLAS refit and AS copies.
 //
-// Build = LBVH (Karras 2012) collapsed to 8-wide nodes:
+// Build = a binary hierarchy over Morton-ordered primitives, collapsed to
+// 8-wide nodes:
 //   1. primitive boxes (triangles, or instance world boxes) + centroid bounds
 //   2. 30-bit Morton codes of the centroids
 //   3. stable LSD radix sort, 8-bit digits, 4 passes (reduce-then-scan:
 //      per-tile digit histograms, one exclusive scan, stable scatter ranked
 //      with warp match_any)
-//   4. Karras hierarchy over the sorted codes (index-augmented for ties)
-//   5. bottom-up boxes with one arrival counter per internal node
-//   6. collapse to 8-wide nodes: a node takes its binary children and
+//   4. the binary hierarchy: PLOC clustering (RT_BUILD_PREFER_FAST_TRACE;
+//      boxes and subtree sizes come with each merge), or the Karras LBVH
+//      (index-augmented for ties) with bottom-up boxes from one arrival
+//      counter per internal node
+//   5. collapse to 8-wide nodes: a node takes its binary children and
 //      repeatedly opens the child of largest surface area until it has 8
 //      children or none can open; a subtree of <= leaf_max primitives is a
-//      leaf (a contiguous range of the sorted order).  The first kLevels
-//      wide levels run as one launch each, the rest as one depth-first task
-//      per thread.
-//   7. primitive records written in leaf order.
+//      leaf.  Each task carries the first position of its primitives in the
+//      final order; its children's primitives follow each other in slot
+//      order, and a leaf child writes its primitives' positions (perm).  The
+//      first kLevels wide levels run as one launch each, the rest as one
+//      depth-first task per thread.
+//   6. primitive records written in that final order.
 // Everything runs on the caller's stream; no host synchronisation.
 //
 // Replaces vkCmdBuildAccelerationStructuresKHR as called by
@@ -24,6 +29,7 @@
 // (src/util_structs.rs:359-405).
 #include <algorithm>
 #include <cfloat>
+#include <cmath>
 #include <cstring>
 
 #include "rt_internal.h"
@@ -49,6 +55,8 @@ struct BuildState {
     uint32_t error;
     uint32_t depth;
     uint32_t blas_kinds;  // TLAS: kBlasKind* bits of the BLASes its instances enter
+    uint32_t ploc_count[2];  // PLOC clusters entering the round (double-buffered by round parity)
+    uint32_t merge_counter;  // PLOC merges so far (internal node ids count down from n - 2)
 };
 
 __device__ __forceinline__ uint32_t f2o(float f) {
@@ -112,6 +120,8 @@ __global__ void k_init_state(BuildState* st) {
         st->error = 0;
         st->depth = 1;
         st->blas_kinds = 0;
+        st->ploc_count[0] = st->ploc_count[1] = 0;
+        st->merge_counter = 0;
     }
 }
 
@@ -496,6 +506,326 @@ __global__ void k_bottom_up(const uint4* inodes, const uint32_t* lparent, const 
     }
 }
 
+// ---- PLOC hierarchy (RT_BUILD_PREFER_FAST_TRACE) --------------------------------
+// Parallel locally-ordered clustering (Meister & Bittner, "Parallel
+// Locally-Ordered Clustering for Bounding Volume Hierarchy Construction",
+// IEEE TVCG 2018).  The clusters start as the Morton-ordered primitives.
+// Each round every cluster finds, among the kPlocRadius clusters on either
+// side of it, the one whose merged box has the smallest surface area; mutual
+// nearest neighbours merge into a new internal node at the lower position,
+// and the surviving clusters are compacted in order.  Internal node ids are
+// handed out from n - 2 down, so the last merge (the root) is node 0, where
+// the collapse starts.  Rounds over more than kPlocSmall clusters run as
+// grid-wide launches (their cluster count stays on the device: a round that
+// finds kPlocSmall or fewer clusters does nothing); one CTA with every
+// cluster in shared memory finishes.  If a round merges nothing (equal or NaN
+// areas), the next one merges neighbour pairs (i, i ^ 1) so the loop always
+// ends.  The host launches ploc_grid_rounds(n) grid-wide rounds: enough
+// nearest-neighbour rounds for the count to fall to kPlocSmall at the
+// measured rate (about 0.58 of the primitives survive the first round, 0.81
+// of the clusters each later one), then pair rounds, each halving the count,
+// in case it has not.
+constexpr int kPlocRadius = 16;
+constexpr uint32_t kPlocSmall = 4096;
+constexpr uint32_t kPlocChunk = 256;        // clusters per block of the neighbour search
+constexpr uint32_t kPlocScanBlock = 1024;   // clusters per block of the compaction scan
+constexpr uint32_t kPlocSmallThreads = 1024;
+constexpr uint32_t kPlocSmallPer = kPlocSmall / kPlocSmallThreads;
+constexpr size_t kPlocSmallSmem = (size_t)kPlocSmall * 9 * 4;  // 6 box floats, ref, neighbour, keep
+
+__device__ __forceinline__ float merged_half_area(float ax, float ay, float az, float bx, float by, float bz,
+                                                  float cx, float cy, float cz, float dx, float dy, float dz) {
+    // boxes (a, b) and (c, d) as lo, hi corners
+    float ex = fmaxf(bx, dx) - fminf(ax, cx), ey = fmaxf(by, dy) - fminf(ay, cy), ez = fmaxf(bz, dz) - fminf(az, cz);
+    return ex * ey + ey * ez + ez * ex;
+}
+
+// Internal node id of the next merge, or kNone past the n - 1 that exist.
+__device__ __forceinline__ uint32_t ploc_claim(BuildState* st, uint32_t n) {
+    uint32_t k = atomicAdd(&st->merge_counter, 1u);
+    if (k + 2u > n) {
+        atomicOr(&st->error, 1u << RT_ERR_BAD_AS);
+        return kNone;
+    }
+    return n - 2u - k;
+}
+
+__device__ __forceinline__ uint32_t ploc_size(const uint32_t* counts, uint32_t r) {
+    return (r & kLeafBit) ? 1u : __ldcg(&counts[r]);
+}
+
+__global__ void k_ploc_init(const float4* sboxes, uint32_t n, uint32_t* cref, float4* cbox, BuildState* st) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) st->ploc_count[0] = n;
+    if (i >= n) return;
+    cref[i] = kLeafBit | i;
+    cbox[2 * (size_t)i] = sboxes[2 * (size_t)i];
+    cbox[2 * (size_t)i + 1] = sboxes[2 * (size_t)i + 1];
+}
+
+__global__ void __launch_bounds__(kPlocChunk) k_ploc_nn(const float4* cbox, uint32_t* nn, const BuildState* st,
+                                                          int round, int forced) {
+    const uint32_t count = st->ploc_count[round & 1];
+    if (count <= kPlocSmall) return;
+    __shared__ float4 slo[kPlocChunk + 2 * kPlocRadius], shi[kPlocChunk + 2 * kPlocRadius];
+    for (uint32_t c0 = blockIdx.x * kPlocChunk; c0 < count; c0 += gridDim.x * kPlocChunk) {
+        for (uint32_t t = threadIdx.x; t < kPlocChunk + 2 * kPlocRadius; t += blockDim.x) {
+            int64_t g = (int64_t)c0 - kPlocRadius + t;
+            if (g >= 0 && g < (int64_t)count) {
+                slo[t] = __ldcg(&cbox[2 * g]);
+                shi[t] = __ldcg(&cbox[2 * g + 1]);
+            }
+        }
+        __syncthreads();
+        const uint32_t i = c0 + threadIdx.x;
+        if (i < count) {
+            uint32_t best = i;
+            if (forced) {
+                best = (i ^ 1u) < count ? (i ^ 1u) : i;
+            } else {
+                const int li = (int)threadIdx.x + kPlocRadius;
+                const float4 a = slo[li], b = shi[li];
+                float bd = INFINITY;
+                for (int o = -kPlocRadius; o <= kPlocRadius; o++) {
+                    int64_t j = (int64_t)i + o;
+                    if (o == 0 || j < 0 || j >= (int64_t)count) continue;
+                    const float4 c = slo[li + o], d = shi[li + o];
+                    float h = merged_half_area(a.x, a.y, a.z, b.x, b.y, b.z, c.x, c.y, c.z, d.x, d.y, d.z);
+                    if (h < bd) {  // ties keep the lower position
+                        bd = h;
+                        best = (uint32_t)j;
+                    }
+                }
+            }
+            nn[i] = best;
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void k_ploc_merge(const uint32_t* cref, const float4* cbox, const uint32_t* nn, uint32_t* tref,
+                             float4* tbox, uint32_t* keep, uint4* inodes, float4* iboxes, uint32_t* counts,
+                             BuildState* st, int round, uint32_t n) {
+    const uint32_t count = st->ploc_count[round & 1];
+    if (count <= kPlocSmall) return;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+        const uint32_t j = __ldcg(&nn[i]);
+        uint32_t r = __ldcg(&cref[i]);
+        float4 lo = __ldcg(&cbox[2 * (size_t)i]), hi = __ldcg(&cbox[2 * (size_t)i + 1]);
+        uint32_t k = 1u;
+        if (j != i && j < count && __ldcg(&nn[j]) == i) {
+            if (i < j) {
+                const uint32_t rj = __ldcg(&cref[j]);
+                const float4 lj = __ldcg(&cbox[2 * (size_t)j]), hj = __ldcg(&cbox[2 * (size_t)j + 1]);
+                lo = make_float4(fminf(lo.x, lj.x), fminf(lo.y, lj.y), fminf(lo.z, lj.z), 0.0f);
+                hi = make_float4(fmaxf(hi.x, hj.x), fmaxf(hi.y, hj.y), fmaxf(hi.z, hj.z), 0.0f);
+                const uint32_t id = ploc_claim(st, n);
+                if (id != kNone) {
+                    inodes[id] = make_uint4(r, rj, 0u, 0u);
+                    iboxes[2 * (size_t)id] = lo;
+                    iboxes[2 * (size_t)id + 1] = hi;
+                    counts[id] = ploc_size(counts, r) + ploc_size(counts, rj);
+                    r = id;
+                }
+            } else {
+                k = 0u;
+            }
+        }
+        tref[i] = r;
+        tbox[2 * (size_t)i] = lo;
+        tbox[2 * (size_t)i + 1] = hi;
+        keep[i] = k;
+    }
+}
+
+// Exclusive scan of keep within each block of kPlocScanBlock clusters; the
+// block totals go to blk (scanned by k_scan_exclusive).
+__global__ void __launch_bounds__(kPlocScanBlock) k_ploc_block_scan(const uint32_t* keep, uint32_t* scan,
+                                                                     uint32_t* blk, const BuildState* st,
+                                                                     int round) {
+    const uint32_t count = st->ploc_count[round & 1];
+    __shared__ uint32_t warp_sums[32];
+    const uint32_t i = blockIdx.x * kPlocScanBlock + threadIdx.x;
+    if (count <= kPlocSmall || blockIdx.x * kPlocScanBlock >= count) {
+        if (threadIdx.x == 0) blk[blockIdx.x] = 0u;
+        return;
+    }
+    const uint32_t v = i < count ? __ldcg(&keep[i]) : 0u;
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    uint32_t incl = v;
+    for (int off = 1; off < 32; off <<= 1) {
+        uint32_t o = __shfl_up_sync(0xFFFFFFFFu, incl, off);
+        if (lane >= (uint32_t)off) incl += o;
+    }
+    if (lane == 31u) warp_sums[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = warp_sums[lane], wi = w;
+        for (int off = 1; off < 32; off <<= 1) {
+            uint32_t o = __shfl_up_sync(0xFFFFFFFFu, wi, off);
+            if (lane >= (uint32_t)off) wi += o;
+        }
+        warp_sums[lane] = wi - w;
+        if (lane == 31u) blk[blockIdx.x] = wi;
+    }
+    __syncthreads();
+    if (i < count) scan[i] = warp_sums[warp] + incl - v;
+}
+
+__global__ void k_ploc_scatter(const uint32_t* tref, const float4* tbox, const uint32_t* keep, const uint32_t* scan,
+                               const uint32_t* blk, uint32_t* cref, float4* cbox, BuildState* st, int round) {
+    const uint32_t count = st->ploc_count[round & 1];
+    if (count <= kPlocSmall) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) st->ploc_count[(round + 1) & 1] = count;
+        return;
+    }
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+        const uint32_t k = __ldcg(&keep[i]);
+        const uint32_t pos = __ldcg(&blk[i / kPlocScanBlock]) + __ldcg(&scan[i]);
+        if (k) {
+            cref[pos] = __ldcg(&tref[i]);
+            cbox[2 * (size_t)pos] = __ldcg(&tbox[2 * (size_t)i]);
+            cbox[2 * (size_t)pos + 1] = __ldcg(&tbox[2 * (size_t)i + 1]);
+        }
+        if (i == count - 1u) st->ploc_count[(round + 1) & 1] = pos + k;
+    }
+}
+
+// The last rounds, in one CTA: every cluster (at most kPlocSmall) in shared
+// memory; thread t owns the contiguous positions [t * per, t * per + per).
+__global__ void __launch_bounds__(kPlocSmallThreads) k_ploc_small(const uint32_t* cref, const float4* cbox,
+                                                                   uint4* inodes, float4* iboxes, uint32_t* counts,
+                                                                   BuildState* st, int round, uint32_t n) {
+    extern __shared__ float psm[];
+    float* lx = psm;
+    float* ly = lx + kPlocSmall;
+    float* lz = ly + kPlocSmall;
+    float* hx = lz + kPlocSmall;
+    float* hy = hx + kPlocSmall;
+    float* hz = hy + kPlocSmall;
+    uint32_t* ref = reinterpret_cast<uint32_t*>(hz + kPlocSmall);
+    uint32_t* nbr = ref + kPlocSmall;
+    uint32_t* keep = nbr + kPlocSmall;
+    __shared__ uint32_t warp_sums[32];
+    __shared__ uint32_t s_count, s_forced;
+    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    uint32_t count = st->ploc_count[round & 1];
+    if (count > kPlocSmall || count == 0u) {
+        if (tid == 0) atomicOr(&st->error, 1u << RT_ERR_BAD_AS);
+        return;
+    }
+    for (uint32_t t = tid; t < count; t += blockDim.x) {
+        float4 a = __ldcg(&cbox[2 * (size_t)t]), b = __ldcg(&cbox[2 * (size_t)t + 1]);
+        lx[t] = a.x; ly[t] = a.y; lz[t] = a.z;
+        hx[t] = b.x; hy[t] = b.y; hz[t] = b.z;
+        ref[t] = __ldcg(&cref[t]);
+    }
+    if (tid == 0) s_forced = 0u;
+    __syncthreads();
+    for (uint32_t guard = 0; count > 1u; guard++) {
+        if (guard > kPlocSmall) {  // every round merges at least one pair: never reached
+            if (tid == 0) atomicOr(&st->error, 1u << RT_ERR_BAD_AS);
+            return;
+        }
+        const uint32_t per = (count + blockDim.x - 1) / blockDim.x;
+        const uint32_t b0 = min(count, tid * per), b1 = min(count, b0 + per);
+        const bool forced = s_forced != 0u;
+        for (uint32_t i = b0; i < b1; i++) {
+            uint32_t best = i;
+            if (forced) {
+                best = (i ^ 1u) < count ? (i ^ 1u) : i;
+            } else {
+                float bd = INFINITY;
+                const uint32_t j0 = i >= (uint32_t)kPlocRadius ? i - kPlocRadius : 0u;
+                const uint32_t j1 = min(count - 1u, i + kPlocRadius);
+                for (uint32_t j = j0; j <= j1; j++) {
+                    if (j == i) continue;
+                    float h = merged_half_area(lx[i], ly[i], lz[i], hx[i], hy[i], hz[i], lx[j], ly[j], lz[j], hx[j],
+                                               hy[j], hz[j]);
+                    if (h < bd) {
+                        bd = h;
+                        best = j;
+                    }
+                }
+            }
+            nbr[i] = best;
+        }
+        __syncthreads();
+        uint32_t local = 0;
+        for (uint32_t i = b0; i < b1; i++) {
+            const uint32_t j = nbr[i];
+            uint32_t k = 1u;
+            if (j != i && nbr[j] == i) {
+                if (i < j) {
+                    const float ax = fminf(lx[i], lx[j]), ay = fminf(ly[i], ly[j]), az = fminf(lz[i], lz[j]);
+                    const float bx = fmaxf(hx[i], hx[j]), by = fmaxf(hy[i], hy[j]), bz = fmaxf(hz[i], hz[j]);
+                    const uint32_t id = ploc_claim(st, n);
+                    if (id != kNone) {
+                        inodes[id] = make_uint4(ref[i], ref[j], 0u, 0u);
+                        iboxes[2 * (size_t)id] = make_float4(ax, ay, az, 0.0f);
+                        iboxes[2 * (size_t)id + 1] = make_float4(bx, by, bz, 0.0f);
+                        counts[id] = ploc_size(counts, ref[i]) + ploc_size(counts, ref[j]);
+                        ref[i] = id;
+                    }
+                    lx[i] = ax; ly[i] = ay; lz[i] = az;
+                    hx[i] = bx; hy[i] = by; hz[i] = bz;
+                } else {
+                    k = 0u;
+                }
+            }
+            keep[i] = k;
+            local += k;
+        }
+        // block-wide exclusive scan of the per-thread survivor counts
+        uint32_t incl = local;
+        for (int off = 1; off < 32; off <<= 1) {
+            uint32_t o = __shfl_up_sync(0xFFFFFFFFu, incl, off);
+            if (lane >= (uint32_t)off) incl += o;
+        }
+        __syncthreads();  // merges done (other threads read ref / box of their pair above)
+        if (lane == 31u) warp_sums[warp] = incl;
+        __syncthreads();
+        if (warp == 0) {
+            uint32_t w = warp_sums[lane], wi = w;
+            for (int off = 1; off < 32; off <<= 1) {
+                uint32_t o = __shfl_up_sync(0xFFFFFFFFu, wi, off);
+                if (lane >= (uint32_t)off) wi += o;
+            }
+            warp_sums[lane] = wi - w;
+            if (lane == 31u) s_count = wi;
+        }
+        __syncthreads();
+        // in-order compaction through registers
+        uint32_t pos = warp_sums[warp] + incl - local;
+        float v[kPlocSmallPer][6];
+        uint32_t rr[kPlocSmallPer], kk[kPlocSmallPer];
+#pragma unroll
+        for (uint32_t q = 0; q < kPlocSmallPer; q++) {
+            const uint32_t i = b0 + q;
+            kk[q] = i < b1 ? keep[i] : 0u;
+            if (i < b1) {
+                v[q][0] = lx[i]; v[q][1] = ly[i]; v[q][2] = lz[i];
+                v[q][3] = hx[i]; v[q][4] = hy[i]; v[q][5] = hz[i];
+                rr[q] = ref[i];
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (uint32_t q = 0; q < kPlocSmallPer; q++) {
+            if (!kk[q]) continue;
+            lx[pos] = v[q][0]; ly[pos] = v[q][1]; lz[pos] = v[q][2];
+            hx[pos] = v[q][3]; hy[pos] = v[q][4]; hz[pos] = v[q][5];
+            ref[pos] = rr[q];
+            pos++;
+        }
+        const uint32_t next = s_count;
+        __syncthreads();
+        if (tid == 0) s_forced = next == count ? 1u : 0u;
+        count = next;
+        __syncthreads();
+    }
+}
+
 // ---- collapse to 8-wide -------------------------------------------------------
 struct CollapseCtx {
     const uint4* inodes;
@@ -504,19 +834,43 @@ struct CollapseCtx {
     WideNode* nodes;
     uint32_t* parents;   // may be null
     BuildState* st;
+    const uint32_t* counts;  // primitives under each internal node (PLOC); null = the Karras ranges
+    uint32_t* perm;          // final primitive order: position -> Morton-sorted position
     uint32_t leaf_max;
     uint32_t width;      // children per node: 8, or 4 (RT_BUILD_EXT_NODE_WIDTH_4)
     uint32_t max_nodes;
     uint32_t n;          // primitives
 };
 
-__device__ __forceinline__ void ref_range(const CollapseCtx& c, uint32_t r, uint32_t* first, uint32_t* last) {
-    if (r & kLeafBit) {
-        *first = *last = r & ~kLeafBit;
-    } else {
-        uint4 nd = c.inodes[r];
-        *first = nd.z;
-        *last = nd.w;
+// Primitives under a binary reference.
+__device__ __forceinline__ uint32_t ref_count(const CollapseCtx& c, uint32_t r) {
+    if (r & kLeafBit) return 1u;
+    if (c.counts) return c.counts[r];
+    uint4 nd = c.inodes[r];
+    return nd.w - nd.z + 1u;
+}
+
+// A leaf child's primitives take positions [first, first + count) of the
+// final order, left to right.  The subtree holds at most leaf_max (<= 8)
+// primitives, so the walk needs a few stack entries.
+__device__ void write_leaf_order(const CollapseCtx& c, uint32_t r, uint32_t first) {
+    uint32_t stack[8];
+    int sp = 0;
+    stack[sp++] = r;
+    uint32_t k = first;
+    while (sp > 0) {
+        const uint32_t x = stack[--sp];
+        if (x & kLeafBit) {
+            if (k < c.n) c.perm[k++] = x & ~kLeafBit;
+            continue;
+        }
+        if (x + 1u >= c.n || sp + 2 > 8) {
+            atomicOr(&c.st->error, 1u << RT_ERR_BAD_AS);
+            return;
+        }
+        const uint4 nd = c.inodes[x];
+        stack[sp++] = nd.y;
+        stack[sp++] = nd.x;
     }
 }
 __device__ __forceinline__ void ref_box(const CollapseCtx& c, uint32_t r, float lo[3], float hi[3]) {
@@ -564,8 +918,11 @@ __device__ __forceinline__ bool ref_ok(const CollapseCtx& c, uint32_t r) {
     return (r & kLeafBit) ? ((r & ~kLeafBit) < c.n) : (r + 1u < c.n);
 }
 
+// One wide node from binary node bref; its primitives take positions
+// [first, first + count) of the final order.
 template <class Push>
-__device__ void collapse_task(const CollapseCtx& c, uint32_t bref, uint32_t slot, uint32_t depth, Push push) {
+__device__ void collapse_task(const CollapseCtx& c, uint32_t bref, uint32_t slot, uint32_t depth, uint32_t first,
+                              Push push) {
     uint32_t refs[8];
     int cnt;
     if (bref + 1u >= c.n || slot >= c.max_nodes) {
@@ -583,9 +940,7 @@ __device__ void collapse_task(const CollapseCtx& c, uint32_t bref, uint32_t slot
         for (int k = 0; k < cnt; k++) {
             uint32_t r = refs[k];
             if (r & kLeafBit) continue;
-            uint32_t f, l;
-            ref_range(c, r, &f, &l);
-            if (l - f + 1 <= c.leaf_max) continue;
+            if (ref_count(c, r) <= c.leaf_max) continue;
             float lo[3], hi[3];
             ref_box(c, r, lo, hi);
             float a = half_area(lo, hi);
@@ -606,15 +961,23 @@ __device__ void collapse_task(const CollapseCtx& c, uint32_t bref, uint32_t slot
     if (cnt == 0) atomicOr(&c.st->error, 1u << RT_ERR_BAD_AS);  // malformed hierarchy: empty node
     float lo[8][3], hi[8][3];
     uint32_t ref[8], meta[8];
+    uint32_t at = first;  // the children's primitives follow each other in slot order
     for (int k = 0; k < cnt; k++) {
         uint32_t r = refs[k];
-        uint32_t f, l;
-        ref_range(c, r, &f, &l);
         ref_box(c, r, lo[k], hi[k]);
-        uint32_t size = l - f + 1;
+        const uint32_t size = ref_count(c, r);
+        const uint32_t f = at;
+        at += size;
+        if (size == 0u || at > c.n) {  // malformed hierarchy
+            atomicOr(&c.st->error, 1u << RT_ERR_BAD_AS);
+            meta[k] = 0;
+            ref[k] = 0;
+            continue;
+        }
         if ((r & kLeafBit) || size <= c.leaf_max) {
             meta[k] = size;
             ref[k] = f;
+            write_leaf_order(c, r, f);
         } else {
             uint32_t cs = atomicAdd(&c.st->node_counter, 1u);
             if (cs >= c.max_nodes) {
@@ -626,7 +989,7 @@ __device__ void collapse_task(const CollapseCtx& c, uint32_t bref, uint32_t slot
             meta[k] = kMetaInternal;
             ref[k] = cs;
             if (c.parents) c.parents[cs] = slot;
-            push(r, cs, depth + 1);
+            push(r, cs, depth + 1, f);
         }
     }
     write_node(&c.nodes[slot], lo, hi, ref, meta, cnt);
@@ -649,6 +1012,7 @@ __global__ void k_collapse_root(CollapseCtx c, uint32_t n, uint4* frontier0) {
             ref[0] = 0;
             meta[0] = n;
             cnt = 1;
+            for (uint32_t i = 0; i < n; i++) c.perm[i] = i;
         }
         write_node(&c.nodes[0], lo, hi, ref, meta, cnt);
         return;
@@ -661,9 +1025,9 @@ __global__ void k_collapse_level(CollapseCtx c, int level, const uint4* fin, uin
     uint32_t count = c.st->frontier_count[level];
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < count; t += gridDim.x * blockDim.x) {
         uint4 task = fin[t];
-        collapse_task(c, task.x, task.y, task.z, [&](uint32_t r, uint32_t s, uint32_t d) {
+        collapse_task(c, task.x, task.y, task.z, task.w, [&](uint32_t r, uint32_t s, uint32_t d, uint32_t f) {
             uint32_t k = atomicAdd(&c.st->frontier_count[level + 1], 1u);
-            if (k < kFrontierCap) fout[k] = make_uint4(r, s, d, 0u);
+            if (k < kFrontierCap) fout[k] = make_uint4(r, s, d, f);
             else atomicOr(&c.st->error, 1u << RT_ERR_TOO_LARGE);
         });
     }
@@ -673,19 +1037,19 @@ __global__ void k_collapse_tail(CollapseCtx c, const uint4* fin) {
     uint32_t count = c.st->frontier_count[kLevels];
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < count; t += gridDim.x * blockDim.x) {
         uint2 stack[kTailStack];
-        uint32_t dstack[kTailStack];
+        uint2 dstack[kTailStack];   // depth, first primitive position
         int sp = 0;
         uint4 task = fin[t];
         stack[sp] = make_uint2(task.x, task.y);
-        dstack[sp++] = task.z;
+        dstack[sp++] = make_uint2(task.z, task.w);
         while (sp > 0) {
             --sp;
             uint2 e = stack[sp];
-            uint32_t d = dstack[sp];
-            collapse_task(c, e.x, e.y, d, [&](uint32_t r, uint32_t s, uint32_t dd) {
+            uint2 d = dstack[sp];
+            collapse_task(c, e.x, e.y, d.x, d.y, [&](uint32_t r, uint32_t s, uint32_t dd, uint32_t f) {
                 if (sp < kTailStack) {
                     stack[sp] = make_uint2(r, s);
-                    dstack[sp++] = dd;
+                    dstack[sp++] = make_uint2(dd, f);
                 } else {
                     atomicOr(&c.st->error, 1u << RT_ERR_STACK_OVERFLOW);
                 }
@@ -695,10 +1059,11 @@ __global__ void k_collapse_tail(CollapseCtx c, const uint4* fin) {
 }
 
 // ---- primitive records ----------------------------------------------------------
-__global__ void k_write_tris(const __grid_constant__ BlasInput in, const uint32_t* vals, TriRecord* tris) {
+__global__ void k_write_tris(const __grid_constant__ BlasInput in, const uint32_t* vals, const uint32_t* perm,
+                             TriRecord* tris) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= in.n) return;
-    uint32_t p = vals[i];
+    uint32_t p = vals[min(perm[i], in.n - 1u)];
     int g;
     uint32_t prim;
     float v[3][3];
@@ -715,10 +1080,11 @@ __global__ void k_write_tris(const __grid_constant__ BlasInput in, const uint32_
     tris[i] = r;
 }
 
-__global__ void k_write_insts(const InstRecord* temp, const uint32_t* vals, uint32_t n, InstRecord* out) {
+__global__ void k_write_insts(const InstRecord* temp, const uint32_t* vals, const uint32_t* perm, uint32_t n,
+                              InstRecord* out) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    out[i] = temp[vals[i]];
+    out[i] = temp[vals[min(perm[i], n - 1u)]];
 }
 
 // ---- 8-bit quantised nodes ----------------------------------------------------
@@ -1012,6 +1378,23 @@ __global__ void k_as_copy(const uint8_t* src, uint8_t* dst, uint64_t dst_size, u
 
 inline uint32_t blocks_for(uint64_t n, uint32_t t) { return (uint32_t)((n + t - 1) / t); }
 
+// PLOC hierarchy for builds that prefer trace speed (the reference's BLAS and
+// TLAS flags); the Karras LBVH for PREFER_FAST_BUILD or no preference, and
+// whenever one leaf holds everything.
+inline bool uses_ploc(uint32_t n, bool top, uint32_t build_flags) {
+    return (build_flags & RT_BUILD_PREFER_FAST_TRACE) && !(build_flags & RT_BUILD_PREFER_FAST_BUILD) &&
+           n > (top ? kTlasLeafMax : kBlasLeafMax);
+}
+
+// Grid-wide PLOC rounds for n > kPlocSmall primitives: nearest-neighbour
+// rounds to reach kPlocSmall clusters at the measured survival rates with a
+// margin of 6, then pair rounds that reach it from n even if none merged.
+inline void ploc_grid_rounds(uint32_t n, int* nn_rounds, int* pair_rounds) {
+    const double x = 0.58 * (double)n / (double)kPlocSmall;
+    *nn_rounds = 1 + (x > 1.0 ? (int)std::ceil(std::log(x) / -std::log(0.81)) : 0) + 6;
+    *pair_rounds = 1 + (int)std::ceil(std::log2((double)n / (double)kPlocSmall));
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -1066,6 +1449,19 @@ ScratchLayout ScratchLayout::make(uint32_t n, bool top, uint32_t build_flags) {
     s.frontier1 = take(f * 16);
     s.temp_inst = top ? take(nn * kInstBytes) : 0;
     s.fp32_nodes = quantized ? take(cap * kNodeBytes) : 0;
+    s.perm = take(nn * 4);
+    s.ploc = uses_ploc(n, top, build_flags);
+    if (s.ploc) {
+        s.ploc_ref0 = take(nn * 4);
+        s.ploc_ref1 = take(nn * 4);
+        s.ploc_box0 = take(nn * 32);
+        s.ploc_box1 = take(nn * 32);
+        s.ploc_nn = take(nn * 4);
+        s.ploc_keep = take(nn * 4);
+        s.ploc_scan = take(nn * 4);
+        s.ploc_blk = take(((nn + kPlocScanBlock - 1) / kPlocScanBlock) * 4);
+        s.counts = take(ni * 4);
+    }
     s.refit_counters = 0;
     s.build_total = o;
     // update (refit) scratch: sorted boxes + one counter per node, sized for
@@ -1125,16 +1521,55 @@ cudaError_t build_common(uint32_t n, bool top, uint32_t build_flags, uint32_t ge
             }
         }
         note_launch(), k_gather_boxes<<<blocks_for(n, T), T, 0, stream>>>(boxes, vals[cur], n, sboxes);
-        if (n > 1) {
+        uint32_t* counts = nullptr;
+        if (sl.ploc) {
+            counts = reinterpret_cast<uint32_t*>(scratch + sl.counts);
+            uint32_t* cref[2] = {reinterpret_cast<uint32_t*>(scratch + sl.ploc_ref0),
+                                 reinterpret_cast<uint32_t*>(scratch + sl.ploc_ref1)};
+            float4* cbox[2] = {reinterpret_cast<float4*>(scratch + sl.ploc_box0),
+                               reinterpret_cast<float4*>(scratch + sl.ploc_box1)};
+            uint32_t* nnb = reinterpret_cast<uint32_t*>(scratch + sl.ploc_nn);
+            uint32_t* keep = reinterpret_cast<uint32_t*>(scratch + sl.ploc_keep);
+            uint32_t* scan = reinterpret_cast<uint32_t*>(scratch + sl.ploc_scan);
+            uint32_t* blk = reinterpret_cast<uint32_t*>(scratch + sl.ploc_blk);
+            note_launch(), k_ploc_init<<<blocks_for(n, T), T, 0, stream>>>(sboxes, n, cref[0], cbox[0], st);
+            int round = 0;
+            if (n > kPlocSmall) {
+                // grid-wide rounds until kPlocSmall clusters remain (later rounds do nothing)
+                const uint32_t g = std::min<uint32_t>(blocks_for(n, kPlocChunk), 4096u);
+                const uint32_t nblk = blocks_for(n, kPlocScanBlock);
+                int nn_rounds = 0, pair_rounds = 0;
+                ploc_grid_rounds(n, &nn_rounds, &pair_rounds);
+                for (; round < nn_rounds + pair_rounds; round++) {
+                    const int forced = round >= nn_rounds;
+                    note_launch(), k_ploc_nn<<<g, kPlocChunk, 0, stream>>>(cbox[0], nnb, st, round, forced);
+                    note_launch(), k_ploc_merge<<<g, 256, 0, stream>>>(cref[0], cbox[0], nnb, cref[1], cbox[1], keep,
+                                                                      inodes, iboxes, counts, st, round, n);
+                    note_launch(), k_ploc_block_scan<<<nblk, kPlocScanBlock, 0, stream>>>(keep, scan, blk, st, round);
+                    note_launch(), k_scan_exclusive<<<1, 1024, 0, stream>>>(blk, nblk);
+                    note_launch(), k_ploc_scatter<<<g, 256, 0, stream>>>(cref[1], cbox[1], keep, scan, blk, cref[0],
+                                                                        cbox[0], st, round);
+                }
+            }
+            // a per-device attribute: set on every build (a host-side call, no device work)
+            const cudaError_t smem_ok =
+                cudaFuncSetAttribute(k_ploc_small, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPlocSmallSmem);
+            if (smem_ok != cudaSuccess) return smem_ok;
+            note_launch(), k_ploc_small<<<1, kPlocSmallThreads, kPlocSmallSmem, stream>>>(cref[0], cbox[0], inodes,
+                                                                                        iboxes, counts, st, round, n);
+        } else if (n > 1) {
             note_launch(), k_karras<<<blocks_for(n - 1, T), T, 0, stream>>>(keys[cur], n, inodes, iparent, lparent);
             cudaMemsetAsync(flags, 0, (size_t)(n - 1) * 4, stream);
             note_launch(), k_bottom_up<<<blocks_for(n, T), T, 0, stream>>>(inodes, lparent, iparent, sboxes, iboxes,
                                                                              flags, n, &st->error);
         }
+        uint32_t* perm = reinterpret_cast<uint32_t*>(scratch + sl.perm);
         CollapseCtx cc;
         cc.inodes = inodes;
         cc.iboxes = iboxes;
         cc.sboxes = sboxes;
+        cc.counts = counts;
+        cc.perm = perm;
         cc.nodes = fp32_nodes;
         cc.parents = top ? reinterpret_cast<uint32_t*>(dst + al.parents) : nullptr;
         cc.st = st;
@@ -1154,10 +1589,11 @@ cudaError_t build_common(uint32_t n, bool top, uint32_t build_flags, uint32_t ge
             note_launch(), k_collapse_tail<<<g, 128, 0, stream>>>(cc, fr[kLevels & 1]);
         }
         if (top) {
-            note_launch(), k_write_insts<<<blocks_for(n, T), T, 0, stream>>>(temp, vals[cur], n,
+            note_launch(), k_write_insts<<<blocks_for(n, T), T, 0, stream>>>(temp, vals[cur], perm, n,
                                                               reinterpret_cast<InstRecord*>(dst + al.prims));
         } else {
-            note_launch(), k_write_tris<<<blocks_for(n, T), T, 0, stream>>>(*blas, vals[cur], reinterpret_cast<TriRecord*>(dst + al.prims));
+            note_launch(), k_write_tris<<<blocks_for(n, T), T, 0, stream>>>(*blas, vals[cur], perm,
+                                                                             reinterpret_cast<TriRecord*>(dst + al.prims));
         }
     } else {
         CollapseCtx cc{};

@@ -43,6 +43,12 @@ struct ScratchLayout {
     uint64_t boxes, sboxes, keys0, keys1, vals0, vals1, hist, inodes, iboxes, iparent, lparent, flags;
     uint64_t frontier0, frontier1, state, temp_inst, refit_counters;
     uint64_t fp32_nodes;       // quantised builds: FP32 nodes before quantisation
+    uint64_t perm;             // final primitive order
+    // PLOC builds (RT_BUILD_PREFER_FAST_TRACE): cluster refs / boxes (two
+    // buffers), neighbours, survivor flags and their scan, block totals,
+    // primitives per internal node
+    uint64_t ploc_ref0, ploc_ref1, ploc_box0, ploc_box1, ploc_nn, ploc_keep, ploc_scan, ploc_blk, counts;
+    bool ploc;
     uint64_t build_total;
     uint64_t update_total;
     uint32_t sort_blocks;
