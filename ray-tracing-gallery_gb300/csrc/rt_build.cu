@@ -57,6 +57,7 @@ struct BuildState {
     uint32_t blas_kinds;  // TLAS: kBlasKind* bits of the BLASes its instances enter
     uint32_t ploc_count[2];  // PLOC clusters entering the round (double-buffered by round parity)
     uint32_t merge_counter;  // PLOC merges so far (internal node ids count down from n - 2)
+    uint32_t radius_bits;    // BLAS: largest vertex distance from the bounds centre (float bits, rounded up)
 };
 
 __device__ __forceinline__ uint32_t f2o(float f) {
@@ -65,6 +66,21 @@ __device__ __forceinline__ uint32_t f2o(float f) {
 }
 __device__ __forceinline__ float o2f(uint32_t u) {
     return __uint_as_float((u & 0x80000000u) ? (u & 0x7FFFFFFFu) : ~u);
+}
+
+// Centre of the primitive bounds, computed the same way wherever it is used.
+__device__ __forceinline__ float bounds_center(const BuildState* st, int k) {
+    return 0.5f * (o2f(st->bb[k]) + o2f(st->bb[3 + k]));
+}
+
+// Distance of v from c, rounded up (every operation rounds towards +inf).
+__device__ __forceinline__ float distance_ru(const float v[3], const float c[3]) {
+    float s = 0.0f;
+    for (int k = 0; k < 3; k++) {
+        float d = fmaxf(__fsub_ru(v[k], c[k]), __fsub_ru(c[k], v[k]));
+        s = __fadd_ru(s, __fmul_ru(d, d));
+    }
+    return __fsqrt_ru(s);
 }
 
 __device__ __forceinline__ void pad_box(float lo[3], float hi[3]) {
@@ -122,6 +138,7 @@ __global__ void k_init_state(BuildState* st) {
         st->blas_kinds = 0;
         st->ploc_count[0] = st->ploc_count[1] = 0;
         st->merge_counter = 0;
+        st->radius_bits = 0;
     }
 }
 
@@ -253,6 +270,27 @@ __device__ bool fill_instance(const RtAccelerationStructureInstance& r, uint32_t
                 hi[0] = fmaxf(hi[0], q.x);
                 hi[1] = fmaxf(hi[1], q.y);
                 hi[2] = fmaxf(hi[2], q.z);
+            }
+            // Cut to the box of the transformed bounding sphere: the ellipsoid
+            // M S + t has half-extent r |row_k(M)| along world axis k.  The
+            // transformed centre is widened by its rounding error (a few ulps
+            // of |M c| + |t|); the padding below adds more.
+            const float rad = bh->sphere_radius;
+            if (rad > 0.0f && rad <= FLT_MAX) {
+                const float* M = rec->o2w;
+                V3 cw = xform_point(M, mk3(bh->sphere_center[0], bh->sphere_center[1], bh->sphere_center[2]));
+                const float cwv[3] = {cw.x, cw.y, cw.z};
+                for (int k = 0; k < 3; k++) {
+                    const float a = M[4 * k], b = M[4 * k + 1], d = M[4 * k + 2];
+                    const float row = __fsqrt_ru(__fadd_ru(__fadd_ru(__fmul_ru(a, a), __fmul_ru(b, b)), __fmul_ru(d, d)));
+                    const float mc = __fadd_ru(__fadd_ru(__fmul_ru(fabsf(a), fabsf(bh->sphere_center[0])),
+                                                         __fmul_ru(fabsf(b), fabsf(bh->sphere_center[1]))),
+                                               __fadd_ru(__fmul_ru(fabsf(d), fabsf(bh->sphere_center[2])),
+                                                         fabsf(M[4 * k + 3])));
+                    const float e = __fadd_ru(__fmul_ru(rad, row), __fmul_ru(mc, 4.8e-7f));  // + 4 ulps of |M c| + |t|
+                    lo[k] = fmaxf(lo[k], __fsub_rd(cwv[k], e));
+                    hi[k] = fminf(hi[k], __fadd_ru(cwv[k], e));
+                }
             }
             float ext = fmaxf(fmaxf(hi[0] - lo[0], hi[1] - lo[1]), hi[2] - lo[2]);
             for (int k = 0; k < 3; k++) {
@@ -1060,7 +1098,7 @@ __global__ void k_collapse_tail(CollapseCtx c, const uint4* fin) {
 
 // ---- primitive records ----------------------------------------------------------
 __global__ void k_write_tris(const __grid_constant__ BlasInput in, const uint32_t* vals, const uint32_t* perm,
-                             TriRecord* tris) {
+                             TriRecord* tris, BuildState* st) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= in.n) return;
     uint32_t p = vals[min(perm[i], in.n - 1u)];
@@ -1072,6 +1110,17 @@ __global__ void k_write_tris(const __grid_constant__ BlasInput in, const uint32_
         float qn = __int_as_float(0x7FC00000);
         for (int c = 0; c < 3; c++) v[c][0] = v[c][1] = v[c][2] = qn;
     }
+    // bounding sphere radius: the largest vertex distance from the bounds
+    // centre over the triangles that have a box (finite vertices)
+    uint32_t rb = 0;
+    if (ok && finite3(v[0]) && finite3(v[1]) && finite3(v[2])) {
+        const float c[3] = {bounds_center(st, 0), bounds_center(st, 1), bounds_center(st, 2)};
+        float r = fmaxf(fmaxf(distance_ru(v[0], c), distance_ru(v[1], c)), distance_ru(v[2], c));
+        rb = __float_as_uint(r);  // an overflow (+inf) turns the sphere off
+    }
+    const unsigned active = __activemask();
+    rb = __reduce_max_sync(active, rb);
+    if ((threadIdx.x & 31u) == (uint32_t)(__ffs(active) - 1) && rb) atomicMax(&st->radius_bits, rb);
     uint32_t flags = (in.g[g].flags & RT_GEOMETRY_OPAQUE) ? 1u : 0u;
     TriRecord r;
     r.v0 = make_float4(v[0][0], v[0][1], v[0][2], __uint_as_float(prim));
@@ -1202,6 +1251,11 @@ __global__ void k_finalize(AsHeader* h, const BuildState* st, HeaderStatic hs) {
     h->depth = st->depth;
     h->leaf_max = hs.leaf_max;
     h->blas_kinds = hs.type == kAsTypeTop ? st->blas_kinds : 0u;
+    // the sphere is written only where every triangle's distance was taken
+    const float rad = __uint_as_float(st->radius_bits);
+    const bool sphere = hs.type == kAsTypeBottom && hs.prim_count > 0 && st->radius_bits != 0u && rad <= FLT_MAX;
+    for (int k = 0; k < 3; k++) h->sphere_center[k] = sphere ? bounds_center(st, k) : 0.0f;
+    h->sphere_radius = sphere ? __fmul_ru(rad, 1.0000010f) : 0.0f;
     uint64_t nodes_end = hs.nodes_offset + (uint64_t)nc * hs.node_bytes;
     uint64_t par = hs.parents_offset ? align_up(nodes_end, 256) : 0;
     uint64_t par_end = par ? par + (uint64_t)nc * 4 : nodes_end;
@@ -1593,7 +1647,8 @@ cudaError_t build_common(uint32_t n, bool top, uint32_t build_flags, uint32_t ge
                                                               reinterpret_cast<InstRecord*>(dst + al.prims));
         } else {
             note_launch(), k_write_tris<<<blocks_for(n, T), T, 0, stream>>>(*blas, vals[cur], perm,
-                                                                             reinterpret_cast<TriRecord*>(dst + al.prims));
+                                                                             reinterpret_cast<TriRecord*>(dst + al.prims),
+                                                                             st);
         }
     } else {
         CollapseCtx cc{};

@@ -53,7 +53,12 @@ struct AsHeader {
     uint32_t leaf_max;
     uint32_t blas_kinds;      // TLAS: kBlasKind* bits of the BLASes its instances enter
     uint64_t compacted_size;
-    uint8_t _pad[kHeaderBytes - 112];
+    // BLAS: a sphere holding every triangle (centre = centre of bounds_lo / hi,
+    // radius rounded up); radius 0 = none.  An instance's world box is its
+    // transformed bounds box cut to the transformed sphere's box.
+    float sphere_center[3];
+    float sphere_radius;
+    uint8_t _pad[kHeaderBytes - 128];
 };
 static_assert(sizeof(AsHeader) == kHeaderBytes, "header size");
 

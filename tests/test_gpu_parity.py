@@ -246,6 +246,51 @@ def test_edge_cases(device):
             assert (g["instance_id"] == 0xFFFFFFFF).all(), name
 
 
+def test_instance_boxes_under_shear_and_nonuniform_scale(device):
+    """An instance's TLAS box is its transformed BLAS box cut to the box of
+    its transformed bounding sphere (an ellipsoid under a general affine
+    map).  Sheared, non-uniformly scaled, mirrored and far-translated
+    instances of a torus and a displaced sphere, rays grazing them: every hit
+    equals the oracle's."""
+    host = _host()
+    rng = scenes.Pcg32(77, 3)
+    tor = scenes.torus(1.0, 0.35, 48, 24)
+    sph = scenes.uv_sphere(64, 32, 1.0, 0.05, 5)
+    models = [scenes.Model(p, n, u, [scenes.Geometry(i, True)], nm) for (p, n, u, i), nm in ((tor, "torus"), (sph, "sphere"))]
+    xf, mdl = [], []
+    for k in range(24):
+        m = scenes.random_rotation(rng) @ np.diag([rng.uniform_range(0.2, 3.0) * (-1 if k % 5 == 0 else 1),
+                                                    rng.uniform_range(0.2, 3.0), rng.uniform_range(0.2, 3.0)])
+        m = m @ np.array([[1.0, rng.uniform_range(-1, 1), 0.0], [0.0, 1.0, rng.uniform_range(-1, 1)], [0.0, 0.0, 1.0]])
+        t = [rng.uniform_range(-6, 6), rng.uniform_range(-6, 6), rng.uniform_range(-6, 6)]
+        if k == 23:  # far away, about 2 units across
+            t = [3.0e4, -2.0e4, 1.0e4]
+            m = 2.0 * scenes.random_rotation(rng) @ np.array([[1.0, 0.3, 0.0], [0.0, 1.0, 0.0], [0.0, 0.0, 1.0]])
+        a = np.zeros((3, 4))
+        a[:, :3], a[:, 3] = m, t
+        xf.append(a)
+        mdl.append(k % 2)
+    inst = scenes.instance_records(np.array(xf), np.array(mdl), np.array(mdl), 0,
+                                   flags=abi.RT_INSTANCE_TRIANGLE_FACING_CULL_DISABLE)
+    sc = scenes.Scene(models, {}, inst, scenes.make_uniforms(np.eye(4).reshape(-1), np.eye(4).reshape(-1), (0, 1, 0),
+                                                              0.0, 0, 0), 8, 8)
+    gs = _gpu_scene(device, sc)
+    o = O.OracleScene(sc)
+    rays = scenes.random_rays(60000, 13, 9.0)
+    rays["tmax"] = 1e4
+    # plus rays aimed at the far instance's centre
+    far = scenes.random_rays(2000, 14, 2.0)
+    far["origin"] += np.float32([3.0e4, -2.0e4, 1.0e4]) + np.float32([0, 0, -20.0])
+    far["direction"] = np.float32([0, 0, 1]) + 0.05 * far["direction"]
+    far["direction"] /= np.linalg.norm(far["direction"], axis=1, keepdims=True)
+    far["tmax"] = 1e4
+    for name, rr in (("near", rays), ("far", far)):
+        g = host.trace_ray_buffer(device, gs, rr, with_models=False)
+        h, _ = o.trace(rr, with_models=False)
+        _assert_hits_equal(g, h, name)
+        assert (h["instance_id"] != 0xFFFFFFFF).sum() > 50, name
+
+
 def test_invalid_vertex_index_reports_status(device):
     sc = _one_model_scene([[0, 0, 0], [1, 0, 0], [0, 1, 0]], [0, 1, 7],
                           scenes.instance_records(scenes.affine(np.eye(3), [0, 0, 0])[None], [0], [0], 0))
