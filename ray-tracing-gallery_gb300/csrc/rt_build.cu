@@ -419,19 +419,78 @@ __global__ void __launch_bounds__(1024) k_scan_exclusive(uint32_t* data, uint32_
     }
 }
 
+struct SortTileShared {
+    uint32_t digit_base[256];
+    uint32_t run[256];
+    uint32_t warp_cnt[kSortThreads / 32][256];
+};
+
+// Stable scatter of tile `tile` (kSortTile keys) by digit (key >> shift) & 255,
+// to digit_base[d] plus the key's rank among the tile's keys of digit d.
+// Expects digit_base filled, run zeroed and a barrier before the call.
+__device__ void scatter_tile(SortTileShared& sm, const uint32_t* kin, const uint32_t* vin, uint32_t* kout,
+                             uint32_t* vout, uint32_t n, int shift, uint32_t tile);
+
+// All four passes of the radix sort in one block, for n <= kSortTile keys:
+// k0 / v0 -> k1 / v1 -> k0 / v0 ..., the result in k0 / v0.
+__global__ void __launch_bounds__(kSortThreads) k_radix_sort_small(uint32_t* k0, uint32_t* v0, uint32_t* k1,
+                                                                   uint32_t* v1, uint32_t n) {
+    __shared__ SortTileShared sm;
+    __shared__ uint32_t warp_sums[kSortThreads / 32];
+    uint32_t* kin = k0;
+    uint32_t* vin = v0;
+    uint32_t* kout = k1;
+    uint32_t* vout = v1;
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    for (int pass = 0; pass < 4; pass++) {
+        const int shift = pass * 8;
+        for (int d = threadIdx.x; d < 256; d += blockDim.x) {
+            sm.digit_base[d] = 0;
+            sm.run[d] = 0;
+        }
+        __syncthreads();
+        for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) atomicAdd(&sm.digit_base[(kin[i] >> shift) & 255u], 1u);
+        __syncthreads();
+        // exclusive scan of the 256 digit counts (one per thread; kSortThreads == 256)
+        const uint32_t c = sm.digit_base[threadIdx.x];
+        uint32_t incl = c;
+        for (int off = 1; off < 32; off <<= 1) {
+            uint32_t o = __shfl_up_sync(0xFFFFFFFFu, incl, off);
+            if (lane >= (uint32_t)off) incl += o;
+        }
+        if (lane == 31u) warp_sums[warp] = incl;
+        __syncthreads();
+        uint32_t before = 0;
+        for (uint32_t w = 0; w < warp; w++) before += warp_sums[w];
+        sm.digit_base[threadIdx.x] = before + incl - c;
+        __syncthreads();
+        scatter_tile(sm, kin, vin, kout, vout, n, shift, 0);
+        __syncthreads();
+        uint32_t* t = kin; kin = kout; kout = t;
+        t = vin; vin = vout; vout = t;
+    }
+}
+
 __global__ void __launch_bounds__(kSortThreads) k_radix_scatter(const uint32_t* kin, const uint32_t* vin,
                                                                 uint32_t* kout, uint32_t* vout, uint32_t n,
                                                                 int shift, const uint32_t* hist, uint32_t nblocks) {
-    __shared__ uint32_t digit_base[256];
-    __shared__ uint32_t run[256];
-    __shared__ uint32_t warp_cnt[kSortThreads / 32][256];
+    __shared__ SortTileShared sm;
     for (int d = threadIdx.x; d < 256; d += blockDim.x) {
-        digit_base[d] = hist[(size_t)d * nblocks + blockIdx.x];
-        run[d] = 0;
+        sm.digit_base[d] = hist[(size_t)d * nblocks + blockIdx.x];
+        sm.run[d] = 0;
     }
+    __syncthreads();
+    scatter_tile(sm, kin, vin, kout, vout, n, shift, blockIdx.x);
+}
+
+__device__ void scatter_tile(SortTileShared& sm, const uint32_t* kin, const uint32_t* vin, uint32_t* kout,
+                             uint32_t* vout, uint32_t n, int shift, uint32_t tile) {
+    uint32_t* digit_base = sm.digit_base;
+    uint32_t* run = sm.run;
+    auto& warp_cnt = sm.warp_cnt;
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t lanemask_lt = (1u << lane) - 1u;
-    uint32_t base = blockIdx.x * kSortTile;
+    uint32_t base = tile * kSortTile;
     for (int j = 0; j < kSortItems; j++) {
         for (int i = threadIdx.x; i < (kSortThreads / 32) * 256; i += blockDim.x) (&warp_cnt[0][0])[i] = 0;
         __syncthreads();
@@ -569,7 +628,7 @@ constexpr uint32_t kPlocChunk = 256;        // clusters per block of the neighbo
 constexpr uint32_t kPlocScanBlock = 1024;   // clusters per block of the compaction scan
 constexpr uint32_t kPlocSmallThreads = 1024;
 constexpr uint32_t kPlocSmallPer = kPlocSmall / kPlocSmallThreads;
-constexpr size_t kPlocSmallSmem = (size_t)kPlocSmall * 9 * 4;  // 6 box floats, ref, neighbour, keep
+constexpr size_t kPlocSmallSmem = (size_t)kPlocSmall * 10 * 4;  // 6 box floats, ref, neighbour, keep, size
 
 __device__ __forceinline__ float merged_half_area(float ax, float ay, float az, float bx, float by, float bz,
                                                   float cx, float cy, float cz, float dx, float dy, float dz) {
@@ -730,7 +789,11 @@ __global__ void k_ploc_scatter(const uint32_t* tref, const float4* tbox, const u
 }
 
 // The last rounds, in one CTA: every cluster (at most kPlocSmall) in shared
-// memory; thread t owns the contiguous positions [t * per, t * per + per).
+// memory with its size; node ids are claimed from a shared counter.  With
+// few clusters, G = 2..32 threads share one cluster's neighbour search (each
+// takes every G-th offset, then a shuffle reduction keeps the smallest area,
+// the lower position on ties); otherwise thread t owns the contiguous
+// positions [t * per, t * per + per).
 __global__ void __launch_bounds__(kPlocSmallThreads) k_ploc_small(const uint32_t* cref, const float4* cbox,
                                                                    uint4* inodes, float4* iboxes, uint32_t* counts,
                                                                    BuildState* st, int round, uint32_t n) {
@@ -744,8 +807,9 @@ __global__ void __launch_bounds__(kPlocSmallThreads) k_ploc_small(const uint32_t
     uint32_t* ref = reinterpret_cast<uint32_t*>(hz + kPlocSmall);
     uint32_t* nbr = ref + kPlocSmall;
     uint32_t* keep = nbr + kPlocSmall;
+    uint32_t* sz = keep + kPlocSmall;
     __shared__ uint32_t warp_sums[32];
-    __shared__ uint32_t s_count, s_forced;
+    __shared__ uint32_t s_count, s_forced, s_merges, s_error;
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
     uint32_t count = st->ploc_count[round & 1];
     if (count > kPlocSmall || count == 0u) {
@@ -756,9 +820,15 @@ __global__ void __launch_bounds__(kPlocSmallThreads) k_ploc_small(const uint32_t
         float4 a = __ldcg(&cbox[2 * (size_t)t]), b = __ldcg(&cbox[2 * (size_t)t + 1]);
         lx[t] = a.x; ly[t] = a.y; lz[t] = a.z;
         hx[t] = b.x; hy[t] = b.y; hz[t] = b.z;
-        ref[t] = __ldcg(&cref[t]);
+        const uint32_t r = __ldcg(&cref[t]);
+        ref[t] = r;
+        sz[t] = ploc_size(counts, r);
     }
-    if (tid == 0) s_forced = 0u;
+    if (tid == 0) {
+        s_forced = 0u;
+        s_merges = st->merge_counter;
+        s_error = 0u;
+    }
     __syncthreads();
     for (uint32_t guard = 0; count > 1u; guard++) {
         if (guard > kPlocSmall) {  // every round merges at least one pair: never reached
@@ -768,25 +838,56 @@ __global__ void __launch_bounds__(kPlocSmallThreads) k_ploc_small(const uint32_t
         const uint32_t per = (count + blockDim.x - 1) / blockDim.x;
         const uint32_t b0 = min(count, tid * per), b1 = min(count, b0 + per);
         const bool forced = s_forced != 0u;
-        for (uint32_t i = b0; i < b1; i++) {
+        uint32_t g = 1;  // threads per cluster in the neighbour search
+        while (g < 32u && count * g * 2u <= blockDim.x) g <<= 1;
+        if (g > 1u) {
+            const uint32_t i = tid / g, sub = tid % g;
+            const bool on = i < count;
             uint32_t best = i;
-            if (forced) {
-                best = (i ^ 1u) < count ? (i ^ 1u) : i;
-            } else {
-                float bd = INFINITY;
-                const uint32_t j0 = i >= (uint32_t)kPlocRadius ? i - kPlocRadius : 0u;
-                const uint32_t j1 = min(count - 1u, i + kPlocRadius);
-                for (uint32_t j = j0; j <= j1; j++) {
-                    if (j == i) continue;
+            float bd = INFINITY;
+            if (on && !forced) {
+                for (uint32_t k = sub; k <= 2u * kPlocRadius; k += g) {
+                    const int64_t j = (int64_t)i - kPlocRadius + k;
+                    if (k == (uint32_t)kPlocRadius || j < 0 || j >= (int64_t)count) continue;
                     float h = merged_half_area(lx[i], ly[i], lz[i], hx[i], hy[i], hz[i], lx[j], ly[j], lz[j], hx[j],
                                                hy[j], hz[j]);
                     if (h < bd) {
                         bd = h;
-                        best = j;
+                        best = (uint32_t)j;
                     }
                 }
             }
-            nbr[i] = best;
+            // groups of g lanes are aligned inside the warp (g divides 32)
+            for (uint32_t off = 1; off < g; off <<= 1) {
+                const float ob = __shfl_xor_sync(0xFFFFFFFFu, bd, off);
+                const uint32_t oj = __shfl_xor_sync(0xFFFFFFFFu, best, off);
+                if (ob < bd || (ob == bd && oj < best && ob < INFINITY)) {
+                    bd = ob;
+                    best = oj;
+                }
+            }
+            if (on && sub == 0u) nbr[i] = forced ? ((i ^ 1u) < count ? (i ^ 1u) : i) : best;
+        } else {
+            for (uint32_t i = b0; i < b1; i++) {
+                uint32_t best = i;
+                if (forced) {
+                    best = (i ^ 1u) < count ? (i ^ 1u) : i;
+                } else {
+                    float bd = INFINITY;
+                    const uint32_t j0 = i >= (uint32_t)kPlocRadius ? i - kPlocRadius : 0u;
+                    const uint32_t j1 = min(count - 1u, i + kPlocRadius);
+                    for (uint32_t j = j0; j <= j1; j++) {
+                        if (j == i) continue;
+                        float h = merged_half_area(lx[i], ly[i], lz[i], hx[i], hy[i], hz[i], lx[j], ly[j], lz[j],
+                                                   hx[j], hy[j], hz[j]);
+                        if (h < bd) {
+                            bd = h;
+                            best = j;
+                        }
+                    }
+                }
+                nbr[i] = best;
+            }
         }
         __syncthreads();
         uint32_t local = 0;
@@ -797,13 +898,18 @@ __global__ void __launch_bounds__(kPlocSmallThreads) k_ploc_small(const uint32_t
                 if (i < j) {
                     const float ax = fminf(lx[i], lx[j]), ay = fminf(ly[i], ly[j]), az = fminf(lz[i], lz[j]);
                     const float bx = fmaxf(hx[i], hx[j]), by = fmaxf(hy[i], hy[j]), bz = fmaxf(hz[i], hz[j]);
-                    const uint32_t id = ploc_claim(st, n);
-                    if (id != kNone) {
+                    const uint32_t m = atomicAdd(&s_merges, 1u);
+                    if (m + 2u <= n) {
+                        const uint32_t id = n - 2u - m;
+                        const uint32_t size = sz[i] + sz[j];
                         inodes[id] = make_uint4(ref[i], ref[j], 0u, 0u);
                         iboxes[2 * (size_t)id] = make_float4(ax, ay, az, 0.0f);
                         iboxes[2 * (size_t)id + 1] = make_float4(bx, by, bz, 0.0f);
-                        counts[id] = ploc_size(counts, ref[i]) + ploc_size(counts, ref[j]);
+                        counts[id] = size;
                         ref[i] = id;
+                        sz[i] = size;
+                    } else {
+                        s_error = 1u;
                     }
                     lx[i] = ax; ly[i] = ay; lz[i] = az;
                     hx[i] = bx; hy[i] = by; hz[i] = bz;
@@ -820,7 +926,7 @@ __global__ void __launch_bounds__(kPlocSmallThreads) k_ploc_small(const uint32_t
             uint32_t o = __shfl_up_sync(0xFFFFFFFFu, incl, off);
             if (lane >= (uint32_t)off) incl += o;
         }
-        __syncthreads();  // merges done (other threads read ref / box of their pair above)
+        __syncthreads();  // merges done (other threads read ref / box / size of their pair above)
         if (lane == 31u) warp_sums[warp] = incl;
         __syncthreads();
         if (warp == 0) {
@@ -836,7 +942,7 @@ __global__ void __launch_bounds__(kPlocSmallThreads) k_ploc_small(const uint32_t
         // in-order compaction through registers
         uint32_t pos = warp_sums[warp] + incl - local;
         float v[kPlocSmallPer][6];
-        uint32_t rr[kPlocSmallPer], kk[kPlocSmallPer];
+        uint32_t rr[kPlocSmallPer], ss[kPlocSmallPer], kk[kPlocSmallPer];
 #pragma unroll
         for (uint32_t q = 0; q < kPlocSmallPer; q++) {
             const uint32_t i = b0 + q;
@@ -845,6 +951,7 @@ __global__ void __launch_bounds__(kPlocSmallThreads) k_ploc_small(const uint32_t
                 v[q][0] = lx[i]; v[q][1] = ly[i]; v[q][2] = lz[i];
                 v[q][3] = hx[i]; v[q][4] = hy[i]; v[q][5] = hz[i];
                 rr[q] = ref[i];
+                ss[q] = sz[i];
             }
         }
         __syncthreads();
@@ -854,6 +961,7 @@ __global__ void __launch_bounds__(kPlocSmallThreads) k_ploc_small(const uint32_t
             lx[pos] = v[q][0]; ly[pos] = v[q][1]; lz[pos] = v[q][2];
             hx[pos] = v[q][3]; hy[pos] = v[q][4]; hz[pos] = v[q][5];
             ref[pos] = rr[q];
+            sz[pos] = ss[q];
             pos++;
         }
         const uint32_t next = s_count;
@@ -861,6 +969,10 @@ __global__ void __launch_bounds__(kPlocSmallThreads) k_ploc_small(const uint32_t
         if (tid == 0) s_forced = next == count ? 1u : 0u;
         count = next;
         __syncthreads();
+    }
+    if (tid == 0) {
+        st->merge_counter = s_merges;
+        if (s_error) atomicOr(&st->error, 1u << RT_ERR_BAD_AS);
     }
 }
 
@@ -961,59 +1073,64 @@ __device__ __forceinline__ bool ref_ok(const CollapseCtx& c, uint32_t r) {
 template <class Push>
 __device__ void collapse_task(const CollapseCtx& c, uint32_t bref, uint32_t slot, uint32_t depth, uint32_t first,
                               Push push) {
-    uint32_t refs[8];
-    int cnt;
+    // Each child's box, size and surface area are loaded once, when it joins
+    // the node: choosing the child to open reads no memory, and opening one
+    // loads only its two children (independent loads).  area < 0: the child
+    // cannot be opened (a leaf, or a subtree small enough to be one).
+    uint32_t refs[8], size[8];
+    float lo[8][3], hi[8][3], area[8];
+    int cnt = 0;
     if (bref + 1u >= c.n || slot >= c.max_nodes) {
         atomicOr(&c.st->error, 1u << RT_ERR_BAD_AS);
         return;
     }
-    uint4 root = c.inodes[bref];
-    refs[0] = root.x;
-    refs[1] = root.y;
-    cnt = 2;
-    if (!ref_ok(c, refs[0]) || !ref_ok(c, refs[1])) cnt = 0;
+    auto load = [&](int k, uint32_t r) {
+        refs[k] = r;
+        ref_box(c, r, lo[k], hi[k]);
+        size[k] = ref_count(c, r);
+        area[k] = (!(r & kLeafBit) && size[k] > c.leaf_max) ? half_area(lo[k], hi[k]) : -1.0f;
+    };
+    const uint4 root = c.inodes[bref];
+    if (ref_ok(c, root.x) && ref_ok(c, root.y)) {
+        load(0, root.x);
+        load(1, root.y);
+        cnt = 2;
+    }
     while (cnt >= 2 && cnt < (int)c.width) {
         int best = -1;
         float best_area = -1.0f;
         for (int k = 0; k < cnt; k++) {
-            uint32_t r = refs[k];
-            if (r & kLeafBit) continue;
-            if (ref_count(c, r) <= c.leaf_max) continue;
-            float lo[3], hi[3];
-            ref_box(c, r, lo, hi);
-            float a = half_area(lo, hi);
-            if (a > best_area) {
-                best_area = a;
+            if (area[k] > best_area) {
+                best_area = area[k];
                 best = k;
             }
         }
         if (best < 0) break;
-        uint4 nd = c.inodes[refs[best]];
+        const uint4 nd = c.inodes[refs[best]];
         if (!ref_ok(c, nd.x) || !ref_ok(c, nd.y)) {
             cnt = 0;
             break;
         }
-        refs[best] = nd.x;
-        refs[cnt++] = nd.y;
+        load(best, nd.x);
+        load(cnt, nd.y);
+        cnt++;
     }
     if (cnt == 0) atomicOr(&c.st->error, 1u << RT_ERR_BAD_AS);  // malformed hierarchy: empty node
-    float lo[8][3], hi[8][3];
     uint32_t ref[8], meta[8];
     uint32_t at = first;  // the children's primitives follow each other in slot order
     for (int k = 0; k < cnt; k++) {
-        uint32_t r = refs[k];
-        ref_box(c, r, lo[k], hi[k]);
-        const uint32_t size = ref_count(c, r);
+        const uint32_t r = refs[k];
+        const uint32_t sz = size[k];
         const uint32_t f = at;
-        at += size;
-        if (size == 0u || at > c.n) {  // malformed hierarchy
+        at += sz;
+        if (sz == 0u || at > c.n) {  // malformed hierarchy
             atomicOr(&c.st->error, 1u << RT_ERR_BAD_AS);
             meta[k] = 0;
             ref[k] = 0;
             continue;
         }
-        if ((r & kLeafBit) || size <= c.leaf_max) {
-            meta[k] = size;
+        if ((r & kLeafBit) || sz <= c.leaf_max) {
+            meta[k] = sz;
             ref[k] = f;
             write_leaf_order(c, r, f);
         } else {
@@ -1563,7 +1680,10 @@ cudaError_t build_common(uint32_t n, bool top, uint32_t build_flags, uint32_t ge
         else note_launch(), k_blas_prims<<<blocks_for(n, T), T, 0, stream>>>(*blas, boxes, st);
         note_launch(), k_morton<<<blocks_for(n, T), T, 0, stream>>>(boxes, n, st, keys[0], vals[0]);
         int cur = 0;
-        if (n > 1) {
+        if (n > 1 && n <= kSortTile) {
+            // one block sorts all four digits; the result lands back in keys[0] / vals[0]
+            note_launch(), k_radix_sort_small<<<1, kSortThreads, 0, stream>>>(keys[0], vals[0], keys[1], vals[1], n);
+        } else if (n > 1) {
             for (int pass = 0; pass < 4; pass++) {
                 int shift = pass * 8;
                 note_launch(), k_radix_hist<<<sl.sort_blocks, kSortThreads, 0, stream>>>(keys[cur], n, shift, hist, sl.sort_blocks);
