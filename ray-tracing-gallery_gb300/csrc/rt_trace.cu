@@ -22,7 +22,8 @@
 // misses and terminal hits write the pixel's colour; mirror / portal hits
 // append the next bounce ray; textured hits store their BRDF terms and
 // shadow origin and append the pixel to the shadow list.  Appends are
-// warp-aggregated (one atomic per warp), which compacts the wavefronts.
+// block-aggregated (one atomic per list per block), which compacts the
+// wavefronts.
 #include <algorithm>
 #include <cstring>
 #include <mutex>
@@ -590,21 +591,16 @@ __device__ __forceinline__ void flush_counters(RtStats* st, const Counters& c) {
     }
 }
 
-// Rays counted where they are created (one atomic per warp), so the
-// traversal loops carry no counters: every created ray is traced.
-__device__ __forceinline__ void count_rays(RtStats* st, uint32_t primary, uint32_t secondary, uint32_t shadow) {
-    const uint32_t lane = threadIdx.x & 31u;
-    uint32_t v[3] = {primary, secondary, shadow};
-#pragma unroll
-    for (int k = 0; k < 3; k++)
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xFFFFFFFFu, v[k], o);
-    if (lane == 0 && (v[0] | v[1] | v[2])) {
-        atomicAdd(reinterpret_cast<unsigned long long*>(&st->traversals), (unsigned long long)v[0] + v[1] + v[2]);
-        if (v[0]) atomicAdd(reinterpret_cast<unsigned long long*>(&st->primary_rays), (unsigned long long)v[0]);
-        if (v[1]) atomicAdd(reinterpret_cast<unsigned long long*>(&st->secondary_rays), (unsigned long long)v[1]);
-        if (v[2]) atomicAdd(reinterpret_cast<unsigned long long*>(&st->shadow_rays), (unsigned long long)v[2]);
-    }
+// Rays are counted without per-ray atomics, so the traversal loops carry no
+// counters: primary rays once per scene (k_setup), the shadow and bounce
+// rays k_shade appended from the list totals (k_output, one thread), mirror /
+// portal continuations in the traversal.  (Same-address atomics serialise in
+// L2: counting per warp in the ray generation kernel took most of its time.)
+__device__ __forceinline__ void count_list_rays(RtStats* st, uint32_t shadow, uint32_t bounce) {
+    if (!st || !(shadow | bounce)) return;
+    atomicAdd(reinterpret_cast<unsigned long long*>(&st->traversals), (unsigned long long)shadow + bounce);
+    if (shadow) atomicAdd(reinterpret_cast<unsigned long long*>(&st->shadow_rays), (unsigned long long)shadow);
+    if (bounce) atomicAdd(reinterpret_cast<unsigned long long*>(&st->secondary_rays), (unsigned long long)bounce);
 }
 
 // ---------------------------------------------------------------------------
@@ -690,6 +686,7 @@ struct SetupParams {
     SceneLayout lay[kSetupChunk];
     RtTextureDesc textures[RT_MAX_BOUND_IMAGES];  // the context's table
     WfBuffers B;
+    RtStats* stats;
     uint32_t* status;
     uint32_t first, count;
     uint32_t copy_textures;
@@ -719,6 +716,12 @@ __global__ void k_setup(const __grid_constant__ SetupParams P) {
     r.pixel_begin = P.lay[t].pixel_begin;
     P.B.scenes[P.first + t] = r;
     atomicOr(&P.B.ctr->kinds, r.env.blas_kinds ? r.env.blas_kinds : kBlasKindF32);
+    // every pixel traces one primary ray: counted here, once per scene
+    const unsigned long long px = (unsigned long long)r.width * r.height;
+    if (px && P.stats) {
+        atomicAdd(reinterpret_cast<unsigned long long*>(&P.stats->traversals), px);
+        atomicAdd(reinterpret_cast<unsigned long long*>(&P.stats->primary_rays), px);
+    }
 }
 
 // ray_generation, lib.rs:126-142 (camera ray, fixed operation order)
@@ -755,7 +758,6 @@ __global__ void k_raygen(const __grid_constant__ WfParams P) {
     }
     P.B.ray_scene[0][i] = sc;
     if (i == 0) P.B.ctr->ray_count[0] = P.total_slots;
-    count_rays(P.stats, x < W && y < H ? 1u : 0u, 0u, 0u);
 }
 
 // The next bounce ray of a mirror hit (closest_hit_mirror.glsl:11-29:
@@ -991,6 +993,7 @@ __global__ void k_shade(const __grid_constant__ WfParams P) {
     const uint32_t si = warp_append(&P.B.ctr->shade_count, nshadow > 0);
     if (nshadow > 0) P.B.shade_list[si] = p;
     const uint32_t first = warp_append_n(&P.B.ctr->shadow_count, nshadow);
+    const uint32_t ri = warp_append(&P.B.ctr->ray_count[b + 1], emit_ray);
     if (nshadow > 0) {
         // the textured hit's shadow rays (closest_hit_textured.glsl:159-172)
         const SceneRec& S = P.B.scenes[sc];
@@ -1007,8 +1010,6 @@ __global__ void k_shade(const __grid_constant__ WfParams P) {
             P.B.shadow_scene[first + k] = sc;
         }
     }
-    count_rays(P.stats, 0u, emit_ray ? 1u : 0u, nshadow);
-    const uint32_t ri = warp_append(&P.B.ctr->ray_count[b + 1], emit_ray);
     if (emit_ray) {
         float4* R = P.B.rays[(b + 1) & 1];
         R[2 * (size_t)ri] = make_float4(no.x, no.y, no.z, 0.01f);
@@ -1035,6 +1036,11 @@ __global__ void k_resolve(const __grid_constant__ WfParams P) {
 __global__ void k_output(const __grid_constant__ WfParams P) {
     const uint32_t gp = blockIdx.x * blockDim.x + threadIdx.x;
     if (gp >= P.total_pixels) return;
+    if (gp == 0) {  // the shadow and bounce rays the shading launch appended
+        uint32_t bounce = 0;
+        for (uint32_t d = 1; d <= kMaxDepth; d++) bounce += P.B.ctr->ray_count[d];
+        count_list_rays(P.stats, P.B.ctr->shadow_count, bounce);
+    }
     const SceneRec& S = P.B.scenes[scene_of<true>(P, gp)];
     const uint32_t p = gp - S.pixel_begin;
     float4 c4 = P.B.colour[gp];
@@ -1370,6 +1376,7 @@ cudaError_t launch_trace_batch(const TraceBatch& tb, uint8_t* ws, int num_sms, c
             sp.copy_textures = first == 0;
             if (first == 0) memcpy(sp.textures, tb.ctx_textures, sizeof sp.textures);
             sp.B = P.B;
+            sp.stats = P.stats;
             sp.status = tb.status;
             sp.first = first;
             sp.count = n;
