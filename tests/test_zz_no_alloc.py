@@ -92,7 +92,8 @@ def test_static_scratch_build_matches_caller_scratch_build(device, call):
     reference = gm.blas  # built by rt_cmd_build_blas with caller scratch
 
     sizes = abi.RtBuildSizes()
-    device.check(device.lib.rt_get_blas_build_sizes(geo, len(geo), 0, C.byref(sizes)))
+    # sizes for the flags of the build (PREFER_FAST_TRACE builds take more nodes and scratch)
+    device.check(device.lib.rt_get_blas_build_sizes(geo, len(geo), abi.RT_BUILD_PREFER_FAST_TRACE, C.byref(sizes)))
     assert sizes.build_scratch_size <= abi.RT_STATIC_SCRATCH_BYTES
     dst = host.Device.alloc(sizes.acceleration_structure_size)
     torch.cuda.synchronize()
