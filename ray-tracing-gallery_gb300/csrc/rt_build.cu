@@ -700,16 +700,9 @@ __global__ void __launch_bounds__(kPlocChunk) k_ploc_nn(const float4* cbox, uint
     }
 }
 
-// Parent link of a merged cluster (leaf or internal node) for the bottom-up
-// collapse costs.
-__device__ __forceinline__ void ploc_set_parent(uint32_t* lparent, uint32_t* iparent, uint32_t r, uint32_t id) {
-    if (r & kLeafBit) lparent[r & ~kLeafBit] = id;
-    else iparent[r] = id;
-}
-
 __global__ void k_ploc_merge(const uint32_t* cref, const float4* cbox, const uint32_t* nn, uint32_t* tref,
                              float4* tbox, uint32_t* keep, uint4* inodes, float4* iboxes, uint32_t* counts,
-                             uint32_t* lparent, uint32_t* iparent, BuildState* st, int round, uint32_t n) {
+                             BuildState* st, int round, uint32_t n) {
     const uint32_t count = st->ploc_count[round & 1];
     if (count <= kPlocSmall) return;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
@@ -729,8 +722,6 @@ __global__ void k_ploc_merge(const uint32_t* cref, const float4* cbox, const uin
                     iboxes[2 * (size_t)id] = lo;
                     iboxes[2 * (size_t)id + 1] = hi;
                     counts[id] = ploc_size(counts, r) + ploc_size(counts, rj);
-                    ploc_set_parent(lparent, iparent, r, id);
-                    ploc_set_parent(lparent, iparent, rj, id);
                     r = id;
                 }
             } else {
@@ -805,7 +796,6 @@ __global__ void k_ploc_scatter(const uint32_t* tref, const float4* tbox, const u
 // positions [t * per, t * per + per).
 __global__ void __launch_bounds__(kPlocSmallThreads) k_ploc_small(const uint32_t* cref, const float4* cbox,
                                                                    uint4* inodes, float4* iboxes, uint32_t* counts,
-                                                                   uint32_t* lparent, uint32_t* iparent,
                                                                    BuildState* st, int round, uint32_t n) {
     extern __shared__ float psm[];
     float* lx = psm;
@@ -916,8 +906,6 @@ __global__ void __launch_bounds__(kPlocSmallThreads) k_ploc_small(const uint32_t
                         iboxes[2 * (size_t)id] = make_float4(ax, ay, az, 0.0f);
                         iboxes[2 * (size_t)id + 1] = make_float4(bx, by, bz, 0.0f);
                         counts[id] = size;
-                        ploc_set_parent(lparent, iparent, ref[i], id);
-                        ploc_set_parent(lparent, iparent, ref[j], id);
                         ref[i] = id;
                         sz[i] = size;
                     } else {
@@ -985,106 +973,6 @@ __global__ void __launch_bounds__(kPlocSmallThreads) k_ploc_small(const uint32_t
     if (tid == 0) {
         st->merge_counter = s_merges;
         if (s_error) atomicOr(&st->error, 1u << RT_ERR_BAD_AS);
-        iparent[0] = kNone;  // the root
-    }
-}
-
-// ---- SAH-optimal collapse costs (RT_BUILD_PREFER_FAST_TRACE) --------------------
-// The dynamic programme of Ylitie, Karras & Laine ("Efficient Incoherent Ray
-// Traversal on GPUs Through Compressed Wide BVHs", HPG 2017, section 4.1),
-// restated for this node layout.  For binary node n and i slots of its
-// parent's wide node, C(n, i) is the least SAH cost of representing the
-// subtree n with at most i children there:
-//   C(n, 1)  = min(leaf: A(n) cp P(n) if P(n) <= leaf_max,
-//                  own wide node: A(n) cn + D(n, W))
-//   C(n, i)  = min(C(n, 1), D(n, i))                        for i >= 2
-//   D(n, j)  = min over 1 <= k < j of C(left, k) + C(right, j - k)
-// (A = half surface area, P = primitives, W = node width; a primitive is a
-// leaf of cost A cp).  Decisions per node, 4 bits each: for i = 2..7 the
-// left share k of D(n, i), or 0 when one child slot is cheaper; bits 24-27
-// the left share of D(n, W) (used when n is a wide node); bit 28 set when
-// C(n, 1) is a leaf.
-constexpr float kDpNodeCost = 1.0f;
-constexpr float kDpPrimCost = 0.5f;
-constexpr uint32_t kDpBlasLeafMax = 4;  // the largest leaf the costs may choose
-
-__device__ __forceinline__ float box_half_area(const float4* b, size_t i) {
-    const float4 l = __ldcg(&b[2 * i]), h = __ldcg(&b[2 * i + 1]);
-    const float dx = fmaxf(h.x - l.x, 0.0f), dy = fmaxf(h.y - l.y, 0.0f), dz = fmaxf(h.z - l.z, 0.0f);
-    return dx * dy + dy * dz + dz * dx;
-}
-
-// Costs C(r, 1..7) of a binary reference into c[1..7].
-__device__ __forceinline__ void dp_load(const float* dpc, const float4* sboxes, uint32_t r, float c[8]) {
-    if (r & kLeafBit) {
-        const float a = box_half_area(sboxes, r & ~kLeafBit) * kDpPrimCost;
-        for (int i = 1; i < 8; i++) c[i] = a;
-    } else {
-        const float4 a = __ldcg(reinterpret_cast<const float4*>(dpc) + 2 * (size_t)r);
-        const float4 b = __ldcg(reinterpret_cast<const float4*>(dpc) + 2 * (size_t)r + 1);
-        c[1] = a.x; c[2] = a.y; c[3] = a.z; c[4] = a.w; c[5] = b.x; c[6] = b.y; c[7] = b.z;
-    }
-}
-
-// Bottom-up over the binary hierarchy (one thread per primitive, the second
-// arrival at a node computes it, as k_bottom_up does).
-__global__ void k_collapse_costs(const uint4* inodes, const uint32_t* lparent, const uint32_t* iparent,
-                                 const float4* sboxes, const float4* iboxes, const uint32_t* counts,
-                                 uint32_t* flags, float* dpc, uint32_t* dec, uint32_t n, uint32_t width,
-                                 uint32_t leaf_max, uint32_t* err) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    uint32_t p = lparent[i];
-    for (int guard = 0; p != kNone; guard++) {
-        if (guard >= 4096 || p + 1u >= n) {  // deeper than n, or out of range: malformed
-            atomicOr(err, 1u << RT_ERR_BAD_AS);
-            return;
-        }
-        __threadfence();
-        if (atomicAdd(&flags[p], 1u) == 0u) return;
-        const uint4 nd = __ldcg(&inodes[p]);
-        float cl[8], cr[8];
-        dp_load(dpc, sboxes, nd.x, cl);
-        dp_load(dpc, sboxes, nd.y, cr);
-        // D(p, j) for j = 2..W and its left share
-        float d[9];
-        uint32_t ks[9];
-        for (uint32_t j = 2; j <= width; j++) {
-            float best = INFINITY;
-            uint32_t bk = 1;
-            for (uint32_t k = 1; k < j; k++) {
-                const float v = cl[k] + cr[j - k];
-                if (v < best) {
-                    best = v;
-                    bk = k;
-                }
-            }
-            d[j] = best;
-            ks[j] = bk;
-        }
-        const float area = box_half_area(iboxes, p);
-        const uint32_t prims = __ldcg(&counts[p]);
-        const float own = area * kDpNodeCost + d[width];
-        const float leaf = prims <= leaf_max ? area * kDpPrimCost * (float)prims : INFINITY;
-        const bool is_leaf = leaf <= own;
-        const float c1 = is_leaf ? leaf : own;
-        float c[8];
-        uint32_t code = (ks[width] << 24) | (is_leaf ? 1u << 28 : 0u);
-        c[1] = c1;
-        for (uint32_t k = 2; k < 8; k++) {
-            const uint32_t j = min(k, width);
-            if (d[j] < c1) {
-                c[k] = d[j];
-                code |= ks[j] << (4 * (k - 2));
-            } else {
-                c[k] = c1;
-            }
-        }
-        float4* out = reinterpret_cast<float4*>(dpc) + 2 * (size_t)p;
-        out[0] = make_float4(c[1], c[2], c[3], c[4]);
-        out[1] = make_float4(c[5], c[6], c[7], 0.0f);
-        dec[p] = code;
-        p = __ldcg(&iparent[p]);
     }
 }
 
@@ -1098,7 +986,6 @@ struct CollapseCtx {
     BuildState* st;
     const uint32_t* counts;  // primitives under each internal node (PLOC); null = the Karras ranges
     uint32_t* perm;          // final primitive order: position -> Morton-sorted position
-    const uint32_t* dec;     // SAH-optimal collapse decisions (k_collapse_costs); null = greedy opening
     uint32_t leaf_max;
     uint32_t width;      // children per node: 8, or 4 (RT_BUILD_EXT_NODE_WIDTH_4)
     uint32_t max_nodes;
@@ -1204,39 +1091,12 @@ __device__ void collapse_task(const CollapseCtx& c, uint32_t bref, uint32_t slot
         area[k] = (!(r & kLeafBit) && size[k] > c.leaf_max) ? half_area(lo[k], hi[k]) : -1.0f;
     };
     const uint4 root = c.inodes[bref];
-    if (c.dec) {
-        // SAH-optimal collapse: bref's D(bref, W) split, then each part
-        // expanded by its own decision for the slots it received (a part of
-        // one slot, or a node whose single slot is cheaper, becomes a child)
-        const uint32_t kl = (c.dec[bref] >> 24) & 15u;
-        uint2 st[8];
-        int sp = 0;
-        if (ref_ok(c, root.x) && ref_ok(c, root.y) && kl >= 1u && kl < c.width) {
-            st[sp++] = make_uint2(root.y, c.width - kl);
-            st[sp++] = make_uint2(root.x, kl);
-        }
-        while (sp > 0) {
-            const uint2 e = st[--sp];
-            const uint32_t r = e.x, k = e.y;
-            const uint32_t split = (!(r & kLeafBit) && k >= 2u) ? (c.dec[r] >> (4 * (k - 2))) & 15u : 0u;
-            if (split == 0u) {
-                if (cnt < 8) load(cnt++, r);
-                continue;
-            }
-            const uint4 nd = c.inodes[r];
-            if (split >= k || sp + 2 > 8 || !ref_ok(c, nd.x) || !ref_ok(c, nd.y)) {
-                cnt = 0;
-                break;
-            }
-            st[sp++] = make_uint2(nd.y, k - split);
-            st[sp++] = make_uint2(nd.x, split);
-        }
-    } else if (ref_ok(c, root.x) && ref_ok(c, root.y)) {
+    if (ref_ok(c, root.x) && ref_ok(c, root.y)) {
         load(0, root.x);
         load(1, root.y);
         cnt = 2;
     }
-    while (!c.dec && cnt >= 2 && cnt < (int)c.width) {
+    while (cnt >= 2 && cnt < (int)c.width) {
         int best = -1;
         float best_area = -1.0f;
         for (int k = 0; k < cnt; k++) {
@@ -1269,9 +1129,7 @@ __device__ void collapse_task(const CollapseCtx& c, uint32_t bref, uint32_t slot
             ref[k] = 0;
             continue;
         }
-        const bool leaf = (r & kLeafBit) || (c.dec ? ((c.dec[r] >> 28) & 1u) != 0u && sz <= c.leaf_max
-                                                   : sz <= c.leaf_max);
-        if (leaf) {
+        if ((r & kLeafBit) || sz <= c.leaf_max) {
             meta[k] = sz;
             ref[k] = f;
             write_leaf_order(c, r, f);
@@ -1699,21 +1557,6 @@ inline bool uses_ploc(uint32_t n, bool top, uint32_t build_flags) {
            n > (top ? kTlasLeafMax : kBlasLeafMax);
 }
 
-// Largest leaf of a build: the SAH-optimal collapse (PLOC builds) chooses
-// BLAS leaves of up to kDpBlasLeafMax triangles; the greedy one cuts at
-// kBlasLeafMax.
-inline uint32_t leaf_max_of(uint32_t n, bool top, uint32_t build_flags) {
-    if (top) return kTlasLeafMax;
-    return uses_ploc(n, top, build_flags) ? kDpBlasLeafMax : kBlasLeafMax;
-}
-
-// Wide-node capacity.  The greedy collapse stops opening only at leaves, so
-// its non-full nodes have >= 2 leaf children (max_wide_nodes); a node of the
-// SAH-optimal collapse owns a distinct binary node, so n + 2 bounds those.
-inline uint64_t node_capacity(uint32_t n, bool top, uint32_t build_flags) {
-    return uses_ploc(n, top, build_flags) ? (uint64_t)n + 2 : max_wide_nodes(n, node_width(build_flags));
-}
-
 // Grid-wide PLOC rounds for n > kPlocSmall primitives: nearest-neighbour
 // rounds to reach kPlocSmall clusters at the measured survival rates with a
 // margin of 6, then pair rounds that reach it from n even if none merged.
@@ -1731,7 +1574,7 @@ inline void ploc_grid_rounds(uint32_t n, int* nn_rounds, int* pair_rounds) {
 AsLayout AsLayout::make(uint32_t n, bool top, uint32_t build_flags) {
     const bool quantized = !top && (build_flags & RT_BUILD_QUANTIZED_NODES) != 0;
     AsLayout l;
-    l.max_nodes = (uint32_t)node_capacity(n, top, build_flags);
+    l.max_nodes = (uint32_t)max_wide_nodes(n, node_width(build_flags));
     l.node_bytes = (quantized && !top) ? kQNodeBytes : kNodeBytes;
     l.nodes = kHeaderBytes;
     uint64_t end = l.nodes + (uint64_t)l.max_nodes * l.node_bytes;
@@ -1748,7 +1591,7 @@ AsLayout AsLayout::make(uint32_t n, bool top, uint32_t build_flags) {
 
 ScratchLayout ScratchLayout::make(uint32_t n, bool top, uint32_t build_flags) {
     const bool quantized = !top && (build_flags & RT_BUILD_QUANTIZED_NODES) != 0;
-    const uint64_t cap = node_capacity(n, top, build_flags);
+    const uint64_t cap = max_wide_nodes(n, node_width(build_flags));
     ScratchLayout s{};
     uint64_t nn = n ? n : 1;
     uint64_t ni = n > 1 ? n - 1 : 1;
@@ -1789,8 +1632,6 @@ ScratchLayout ScratchLayout::make(uint32_t n, bool top, uint32_t build_flags) {
         s.ploc_scan = take(nn * 4);
         s.ploc_blk = take(((nn + kPlocScanBlock - 1) / kPlocScanBlock) * 4);
         s.counts = take(ni * 4);
-        s.dpc = take(ni * 32);
-        s.dec = take(ni * 4);
     }
     s.refit_counters = 0;
     s.build_total = o;
@@ -1855,7 +1696,6 @@ cudaError_t build_common(uint32_t n, bool top, uint32_t build_flags, uint32_t ge
         }
         note_launch(), k_gather_boxes<<<blocks_for(n, T), T, 0, stream>>>(boxes, vals[cur], n, sboxes);
         uint32_t* counts = nullptr;
-        uint32_t* dec = nullptr;
         if (sl.ploc) {
             counts = reinterpret_cast<uint32_t*>(scratch + sl.counts);
             uint32_t* cref[2] = {reinterpret_cast<uint32_t*>(scratch + sl.ploc_ref0),
@@ -1878,8 +1718,7 @@ cudaError_t build_common(uint32_t n, bool top, uint32_t build_flags, uint32_t ge
                     const int forced = round >= nn_rounds;
                     note_launch(), k_ploc_nn<<<g, kPlocChunk, 0, stream>>>(cbox[0], nnb, st, round, forced);
                     note_launch(), k_ploc_merge<<<g, 256, 0, stream>>>(cref[0], cbox[0], nnb, cref[1], cbox[1], keep,
-                                                                      inodes, iboxes, counts, lparent, iparent, st,
-                                                                      round, n);
+                                                                      inodes, iboxes, counts, st, round, n);
                     note_launch(), k_ploc_block_scan<<<nblk, kPlocScanBlock, 0, stream>>>(keep, scan, blk, st, round);
                     note_launch(), k_scan_exclusive<<<1, 1024, 0, stream>>>(blk, nblk);
                     note_launch(), k_ploc_scatter<<<g, 256, 0, stream>>>(cref[1], cbox[1], keep, scan, blk, cref[0],
@@ -1890,14 +1729,8 @@ cudaError_t build_common(uint32_t n, bool top, uint32_t build_flags, uint32_t ge
             const cudaError_t smem_ok =
                 cudaFuncSetAttribute(k_ploc_small, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPlocSmallSmem);
             if (smem_ok != cudaSuccess) return smem_ok;
-            note_launch(), k_ploc_small<<<1, kPlocSmallThreads, kPlocSmallSmem, stream>>>(
-                cref[0], cbox[0], inodes, iboxes, counts, lparent, iparent, st, round, n);
-            // SAH-optimal collapse costs, bottom-up over the PLOC hierarchy
-            dec = reinterpret_cast<uint32_t*>(scratch + sl.dec);
-            cudaMemsetAsync(flags, 0, (size_t)(n - 1) * 4, stream);
-            note_launch(), k_collapse_costs<<<blocks_for(n, T), T, 0, stream>>>(
-                inodes, lparent, iparent, sboxes, iboxes, counts, flags, reinterpret_cast<float*>(scratch + sl.dpc),
-                dec, n, node_width(build_flags), top ? kTlasLeafMax : kDpBlasLeafMax, &st->error);
+            note_launch(), k_ploc_small<<<1, kPlocSmallThreads, kPlocSmallSmem, stream>>>(cref[0], cbox[0], inodes,
+                                                                                        iboxes, counts, st, round, n);
         } else if (n > 1) {
             note_launch(), k_karras<<<blocks_for(n - 1, T), T, 0, stream>>>(keys[cur], n, inodes, iparent, lparent);
             cudaMemsetAsync(flags, 0, (size_t)(n - 1) * 4, stream);
@@ -1911,11 +1744,10 @@ cudaError_t build_common(uint32_t n, bool top, uint32_t build_flags, uint32_t ge
         cc.sboxes = sboxes;
         cc.counts = counts;
         cc.perm = perm;
-        cc.dec = dec;
         cc.nodes = fp32_nodes;
         cc.parents = top ? reinterpret_cast<uint32_t*>(dst + al.parents) : nullptr;
         cc.st = st;
-        cc.leaf_max = top ? kTlasLeafMax : (dec ? kDpBlasLeafMax : kBlasLeafMax);
+        cc.leaf_max = top ? kTlasLeafMax : kBlasLeafMax;
         cc.width = node_width(build_flags);
         cc.max_nodes = al.max_nodes;
         cc.n = n;
@@ -1961,7 +1793,7 @@ cudaError_t build_common(uint32_t n, bool top, uint32_t build_flags, uint32_t ge
     hs.prim_count = n;
     hs.max_nodes = al.max_nodes;
     hs.geometry_count = geometry_count;
-    hs.leaf_max = leaf_max_of(n, top, build_flags);
+    hs.leaf_max = top ? kTlasLeafMax : kBlasLeafMax;
     hs.total_size = al.total;
     hs.nodes_offset = al.nodes;
     hs.prims_offset = al.prims;

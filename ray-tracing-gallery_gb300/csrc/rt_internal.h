@@ -48,7 +48,6 @@ struct ScratchLayout {
     // buffers), neighbours, survivor flags and their scan, block totals,
     // primitives per internal node
     uint64_t ploc_ref0, ploc_ref1, ploc_box0, ploc_box1, ploc_nn, ploc_keep, ploc_scan, ploc_blk, counts;
-    uint64_t dpc, dec;         // SAH-optimal collapse: costs C(n, 1..7) and decisions per internal node
     bool ploc;
     uint64_t build_total;
     uint64_t update_total;
