@@ -58,7 +58,12 @@ struct BuildState {
     uint32_t ploc_count[2];  // PLOC clusters entering the round (double-buffered by round parity)
     uint32_t merge_counter;  // PLOC merges so far (internal node ids count down from n - 2)
     uint32_t radius_bits;    // BLAS: largest vertex distance from the bounds centre (float bits, rounded up)
+    uint32_t dop_hi[7], dop_lo[7];  // BLAS: largest / smallest vertex projection on each 14-DOP axis (ordered uint)
 };
+
+// The seven 14-DOP axes (unnormalised): x, y, z and the four diagonals.
+__device__ __constant__ const int8_t kDopAxis[7][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}, {1, 1, 1},
+                                                       {1, 1, -1}, {1, -1, 1}, {-1, 1, 1}};
 
 __device__ __forceinline__ uint32_t f2o(float f) {
     uint32_t u = __float_as_uint(f);
@@ -139,6 +144,10 @@ __global__ void k_init_state(BuildState* st) {
         st->ploc_count[0] = st->ploc_count[1] = 0;
         st->merge_counter = 0;
         st->radius_bits = 0;
+        for (int k = 0; k < 7; k++) {
+            st->dop_hi[k] = 0u;
+            st->dop_lo[k] = 0xFFFFFFFFu;
+        }
     }
 }
 
@@ -290,6 +299,21 @@ __device__ bool fill_instance(const RtAccelerationStructureInstance& r, uint32_t
                     const float e = __fadd_ru(__fmul_ru(rad, row), __fmul_ru(mc, 4.8e-7f));  // + 4 ulps of |M c| + |t|
                     lo[k] = fmaxf(lo[k], __fsub_rd(cwv[k], e));
                     hi[k] = fminf(hi[k], __fadd_ru(cwv[k], e));
+                }
+            }
+            // and to the box of the transformed 14-DOP vertices
+            const uint32_t nd = bh->dop_count;
+            if (nd >= 4u && nd <= kDopMaxVertices) {
+                float dlo[3] = {INFINITY, INFINITY, INFINITY}, dhi[3] = {-INFINITY, -INFINITY, -INFINITY};
+                for (uint32_t v = 0; v < nd; v++) {
+                    const V3 q = xform_point(rec->o2w, mk3(bh->dop_vertex[v][0], bh->dop_vertex[v][1],
+                                                          bh->dop_vertex[v][2]));
+                    dlo[0] = fminf(dlo[0], q.x); dlo[1] = fminf(dlo[1], q.y); dlo[2] = fminf(dlo[2], q.z);
+                    dhi[0] = fmaxf(dhi[0], q.x); dhi[1] = fmaxf(dhi[1], q.y); dhi[2] = fmaxf(dhi[2], q.z);
+                }
+                for (int k = 0; k < 3; k++) {
+                    lo[k] = fmaxf(lo[k], dlo[k]);
+                    hi[k] = fminf(hi[k], dhi[k]);
                 }
             }
             float ext = fmaxf(fmaxf(hi[0] - lo[0], hi[1] - lo[1]), hi[2] - lo[2]);
@@ -1237,13 +1261,123 @@ __global__ void k_write_tris(const __grid_constant__ BlasInput in, const uint32_
     }
     const unsigned active = __activemask();
     rb = __reduce_max_sync(active, rb);
-    if ((threadIdx.x & 31u) == (uint32_t)(__ffs(active) - 1) && rb) atomicMax(&st->radius_bits, rb);
+    const bool leader = (threadIdx.x & 31u) == (uint32_t)(__ffs(active) - 1);
+    if (leader && rb) atomicMax(&st->radius_bits, rb);
+    // 14-DOP: extreme projections on the seven axes (sums of +-coordinates,
+    // rounded up for the maxima and down for the minima)
+    const bool valid = ok && finite3(v[0]) && finite3(v[1]) && finite3(v[2]);
+#pragma unroll
+    for (int k = 0; k < 7; k++) {
+        uint32_t hi = 0u, lo = 0xFFFFFFFFu;
+        if (valid) {
+            float ph = -INFINITY, pl = INFINITY;
+            for (int c = 0; c < 3; c++) {
+                float u = 0.0f, d = 0.0f;
+                for (int a = 0; a < 3; a++) {
+                    const float x = kDopAxis[k][a] > 0 ? v[c][a] : (kDopAxis[k][a] < 0 ? -v[c][a] : 0.0f);
+                    u = __fadd_ru(u, x);
+                    d = __fadd_rd(d, x);
+                }
+                ph = fmaxf(ph, u);
+                pl = fminf(pl, d);
+            }
+            hi = f2o(ph);
+            lo = f2o(pl);
+        }
+        hi = __reduce_max_sync(active, hi);
+        lo = __reduce_min_sync(active, lo);
+        if (leader && hi != 0u) {  // some lane of the warp had a valid triangle
+            atomicMax(&st->dop_hi[k], hi);
+            atomicMin(&st->dop_lo[k], lo);
+        }
+    }
     uint32_t flags = (in.g[g].flags & RT_GEOMETRY_OPAQUE) ? 1u : 0u;
     TriRecord r;
     r.v0 = make_float4(v[0][0], v[0][1], v[0][2], __uint_as_float(prim));
     r.v1 = make_float4(v[1][0], v[1][1], v[1][2], __uint_as_float((uint32_t)g));
     r.v2 = make_float4(v[2][0], v[2][1], v[2][2], __uint_as_float(flags));
     tris[i] = r;
+}
+
+// The 14-DOP's vertices (one block of kDopThreads): every triple of its 14
+// planes solved in double, kept when it satisfies all 14 (with a relative
+// tolerance), duplicates merged.  More than kDopMaxVertices distinct points
+// (only through rounding) or a non-finite projection leave the header's
+// dop_count at 0.  The vertices' float rounding (a few 1e-8 relative) is
+// covered by the instance box padding (1e-5 relative).
+constexpr int kDopThreads = 128;
+constexpr int kDopCandidates = 128;
+
+__global__ void __launch_bounds__(kDopThreads) k_dop_vertices(AsHeader* h, const BuildState* st) {
+    __shared__ double pn[14][3], ph[14];
+    __shared__ double cand[kDopCandidates][3];
+    __shared__ uint32_t ncand;
+    __shared__ bool ok;
+    const int t = threadIdx.x;
+    if (t == 0) {
+        ncand = 0;
+        ok = true;
+        h->dop_count = 0;
+        for (int k = 0; k < 7; k++) {
+            const float hi = o2f(st->dop_hi[k]), lo = o2f(st->dop_lo[k]);
+            if (!(lo <= hi) || !(fabsf(hi) <= FLT_MAX) || !(fabsf(lo) <= FLT_MAX)) ok = false;
+            for (int a = 0; a < 3; a++) {
+                pn[2 * k][a] = (double)kDopAxis[k][a];
+                pn[2 * k + 1][a] = -(double)kDopAxis[k][a];
+            }
+            ph[2 * k] = (double)hi;
+            ph[2 * k + 1] = -(double)lo;
+        }
+    }
+    __syncthreads();
+    if (!ok) return;
+    double scale = 1e-30;
+    for (int j = 0; j < 14; j++) scale = fmax(scale, fabs(ph[j]));
+    int idx = 0;
+    for (int a = 0; a < 14; a++)
+        for (int b = a + 1; b < 14; b++)
+            for (int c = b + 1; c < 14; c++, idx++) {
+                if (idx % kDopThreads != t) continue;
+                // Cramer's rule on the rows pn[a], pn[b], pn[c]
+                const double* A = pn[a];
+                const double* B = pn[b];
+                const double* C = pn[c];
+                const double det = A[0] * (B[1] * C[2] - B[2] * C[1]) - A[1] * (B[0] * C[2] - B[2] * C[0]) +
+                                   A[2] * (B[0] * C[1] - B[1] * C[0]);
+                if (fabs(det) < 1e-9) continue;
+                const double x = (ph[a] * (B[1] * C[2] - B[2] * C[1]) - A[1] * (ph[b] * C[2] - B[2] * ph[c]) +
+                                  A[2] * (ph[b] * C[1] - B[1] * ph[c])) / det;
+                const double y = (A[0] * (ph[b] * C[2] - B[2] * ph[c]) - ph[a] * (B[0] * C[2] - B[2] * C[0]) +
+                                  A[2] * (B[0] * ph[c] - ph[b] * C[0])) / det;
+                const double z = (A[0] * (B[1] * ph[c] - ph[b] * C[1]) - A[1] * (B[0] * ph[c] - ph[b] * C[0]) +
+                                  ph[a] * (B[0] * C[1] - B[1] * C[0])) / det;
+                bool inside = true;
+                for (int j = 0; j < 14 && inside; j++)
+                    inside = pn[j][0] * x + pn[j][1] * y + pn[j][2] * z <= ph[j] + 1e-9 * scale;
+                if (!inside) continue;
+                const uint32_t s = atomicAdd(&ncand, 1u);
+                if (s < (uint32_t)kDopCandidates) {
+                    cand[s][0] = x;
+                    cand[s][1] = y;
+                    cand[s][2] = z;
+                }
+            }
+    __syncthreads();
+    if (t != 0) return;
+    const uint32_t nc = min(ncand, (uint32_t)kDopCandidates);
+    if (ncand > (uint32_t)kDopCandidates || nc < 4u) return;
+    uint32_t nv = 0;
+    for (uint32_t i = 0; i < nc; i++) {
+        bool dup = false;
+        for (uint32_t j = 0; j < i && !dup; j++)
+            dup = fabs(cand[i][0] - cand[j][0]) <= 1e-7 * scale && fabs(cand[i][1] - cand[j][1]) <= 1e-7 * scale &&
+                  fabs(cand[i][2] - cand[j][2]) <= 1e-7 * scale;
+        if (dup) continue;
+        if (nv == kDopMaxVertices) return;  // more points than a 14-DOP has: leave it off
+        for (int a = 0; a < 3; a++) h->dop_vertex[nv][a] = (float)cand[i][a];
+        nv++;
+    }
+    h->dop_count = nv;
 }
 
 __global__ void k_write_insts(const InstRecord* temp, const uint32_t* vals, const uint32_t* perm, uint32_t n,
@@ -1769,6 +1903,7 @@ cudaError_t build_common(uint32_t n, bool top, uint32_t build_flags, uint32_t ge
             note_launch(), k_write_tris<<<blocks_for(n, T), T, 0, stream>>>(*blas, vals[cur], perm,
                                                                              reinterpret_cast<TriRecord*>(dst + al.prims),
                                                                              st);
+            note_launch(), k_dop_vertices<<<1, kDopThreads, 0, stream>>>(reinterpret_cast<AsHeader*>(dst), st);
         }
     } else {
         CollapseCtx cc{};

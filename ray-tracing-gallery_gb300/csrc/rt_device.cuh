@@ -31,6 +31,7 @@ constexpr uint32_t kInstBytes = 128;
 // 3 -> 995 / 2182 / 2567, 4 -> 922 / 2043 / 2670, 8 -> 832 / 1748 / 2528.
 constexpr uint32_t kBlasLeafMax = 2;
 constexpr uint32_t kTlasLeafMax = 1;   // instances per leaf child
+constexpr uint32_t kDopMaxVertices = 24;  // a 14-DOP (cube with cut corners) has at most 24
 constexpr uint32_t kWide = 8;
 
 struct AsHeader {
@@ -58,7 +59,14 @@ struct AsHeader {
     // transformed bounds box cut to the transformed sphere's box.
     float sphere_center[3];
     float sphere_radius;
-    uint8_t _pad[kHeaderBytes - 128];
+    // BLAS: the vertices of a 14-DOP holding every triangle (the 6 axis and
+    // 8 diagonal (+-1, +-1, +-1) planes at the triangles' extreme
+    // projections); 0 = none.  The instance box is also cut to the box of
+    // these vertices transformed.
+    uint32_t dop_count;
+    uint32_t _dop_pad[3];
+    float dop_vertex[kDopMaxVertices][3];
+    uint8_t _pad[kHeaderBytes - 144 - 12 * kDopMaxVertices];
 };
 static_assert(sizeof(AsHeader) == kHeaderBytes, "header size");
 
