@@ -651,29 +651,35 @@ def bench_precision(args):
                                    s["triangles_tested"] * TRI_BYTES + s["instances_visited"] * INST_BYTES)
         arm["gbs"] = arm["bytes_per_launch"] / (arm["total_ms"] / args.steps / 1e3) / 1e9
 
-    # end to end through the C ABI with host buffers: rt_trace_ray_buffer_host copies the rays in and
-    # the hits out from pinned host memory, chunk by chunk, overlapped with the traversal
+    # end to end through the C ABI with host buffers (pinned): rt_trace_ray_buffer_host with chunk_rays 0
+    # traces straight from / into the mapped host memory in one launch; with chunk_rays > 0 it stages
+    # copies chunk by chunk on two streams, overlapped with the traversal (both measured)
     q = arms["quantized"]["scene"]
     rays_pinned = torch.from_numpy(rays.view(np.uint8).reshape(-1).copy()).pin_memory()
     hits_pinned = torch.empty(n * RAY_HIT_BYTES, dtype=torch.uint8).pin_memory()
     push0 = abi.RtPushConstantBufferAddresses()
 
-    def host_query():
+    def host_query(chunk):
         dev.check(lib.rt_trace_ray_buffer_host(dev.ctx, q.tlas.device_address(), C.byref(push0), None, 0, 0xFF, 0,
-                                               rays_pinned.data_ptr(), n, hits_pinned.data_ptr(), E2E_CHUNK, sh))
+                                               rays_pinned.data_ptr(), n, hits_pinned.data_ptr(), chunk, sh))
 
-    host_query()
-    torch.cuda.synchronize()
-    e2e_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    for i in range(args.steps):
-        flush.fill_(i & 0xFF)
-        e2e_ev[i][0].record(stream)
-        host_query()
-        e2e_ev[i][1].record(stream)
-    torch.cuda.synchronize()
-    e2e_equal = bool(np.array_equal(hits_pinned.numpy(), hits_dev.cpu().numpy()))
-    e2e_ms = sum(a.elapsed_time(b) for a, b in e2e_ev)
-    e2e_value = n * world * args.steps / (e2e_ms / 1e3) / 1e6
+    e2e_modes = {}
+    for mode, chunk in (("direct", 0), ("staged", E2E_CHUNK)):
+        hits_pinned.zero_()
+        host_query(chunk)
+        torch.cuda.synchronize()
+        e2e_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+                  for _ in range(args.steps)]
+        for i in range(args.steps):
+            flush.fill_(i & 0xFF)
+            e2e_ev[i][0].record(stream)
+            host_query(chunk)
+            e2e_ev[i][1].record(stream)
+        torch.cuda.synchronize()
+        e2e_ms = sum(a.elapsed_time(b) for a, b in e2e_ev)
+        e2e_modes[mode] = {"value": n * world * args.steps / (e2e_ms / 1e3) / 1e6, "chunk_rays": chunk,
+                           "hits_equal_device_query": bool(np.array_equal(hits_pinned.numpy(), hits_dev.cpu().numpy()))}
+    e2e_value = e2e_modes["direct"]["value"]
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -701,7 +707,9 @@ def bench_precision(args):
                        "speedup_quantized_over_fp32": qa["value"] / fa["value"]},
             "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": n * RAY_BYTES,
                     "d2h_bytes_per_step": n * RAY_HIT_BYTES, "api": "rt_trace_ray_buffer_host",
-                    "chunk_rays": E2E_CHUNK, "hits_equal_device_query": e2e_equal},
+                    "mode": "direct (pinned host rays / hits read and written by the traversal)",
+                    "hits_equal_device_query": e2e_modes["direct"]["hits_equal_device_query"],
+                    "staged_copies": e2e_modes["staged"]},
             "roofline": {"bound": "hbm", "achieved": qa["gbs"], "peak": peak, "unit": "GB/s", "frac": qa["gbs"] / peak,
                          "traffic": profiled_traffic("k_trace_ray_buffer_precision.md"),
                          "kernel": "k_trace_ray_buffer (quantised BLAS)",

@@ -527,14 +527,17 @@ RTCORE_API int32_t rt_cmd_trace_ray_buffer(rt_ctx* ctx, uint64_t tlas, const RtP
                                            uint32_t cull_mask, uint32_t sbt_offset, uint64_t rays,
                                            uint32_t ray_count, uint64_t hits, void* stream);
 
-/* rt_cmd_trace_ray_buffer from host memory: the rays are copied in, traced
- * and their hits copied out in chunks of `chunk_rays` (0 = 1M), alternating
- * two internal streams so that one chunk's copies overlap another chunk's
- * traversal.  Ordered after the work already queued on `stream`; on return
- * everything is queued and `stream` waits for it (synchronise `stream`
- * before reading host_hits).  host_rays / host_hits should be pinned (page-
- * locked) or the copies do not overlap.  No counterpart in the reference,
- * whose rays never leave the GPU. */
+/* rt_cmd_trace_ray_buffer from host memory.  With chunk_rays = 0 and both
+ * buffers page-locked (cudaHostAlloc / cudaHostRegister), one traversal
+ * launch reads the rays from and writes the hits to host memory directly
+ * (mapped host memory; NVLink-C2C on Grace systems).  Otherwise the rays are
+ * copied in, traced and their hits copied out in chunks of `chunk_rays`
+ * (0 = 1M), alternating two internal streams so that one chunk's copies
+ * overlap another chunk's traversal.  Ordered after the work already queued
+ * on `stream`; on return everything is queued and `stream` waits for it
+ * (synchronise `stream` before reading host_hits).  Pageable buffers take
+ * the copy path and their copies do not overlap.  No counterpart in the
+ * reference, whose rays never leave the GPU. */
 RTCORE_API int32_t rt_trace_ray_buffer_host(rt_ctx* ctx, uint64_t tlas, const RtPushConstantBufferAddresses* push,
                                             const RtShaderBindingTable* sbt, uint32_t ray_flags,
                                             uint32_t cull_mask, uint32_t sbt_offset, const RtRay* host_rays,

@@ -782,6 +782,20 @@ RTCORE_API int32_t rt_trace_ray_buffer_host(rt_ctx* ctx, uint64_t tlas, const Rt
     if (!host_rays || !host_hits) return fail(RT_ERR_INVALID, "host_rays / host_hits is NULL");
     cudaStream_t caller = reinterpret_cast<cudaStream_t>(stream);
     if (stream_capturing(caller)) return fail(RT_ERR_INVALID, "rt_trace_ray_buffer_host cannot run in a capture");
+    if (chunk_rays == 0) {
+        // Page-locked host buffers are mapped into the GPU's address space
+        // (over NVLink-C2C on Grace systems): the traversal reads each ray
+        // from and writes each hit to host memory itself, in one launch,
+        // with no staging copies to overlap.
+        cudaPointerAttributes ra{}, ha{};
+        if (cudaPointerGetAttributes(&ra, host_rays) == cudaSuccess && ra.type == cudaMemoryTypeHost &&
+            ra.devicePointer && cudaPointerGetAttributes(&ha, host_hits) == cudaSuccess &&
+            ha.type == cudaMemoryTypeHost && ha.devicePointer)
+            return rt_cmd_trace_ray_buffer(ctx, tlas, push, sbt, ray_flags, cull_mask, sbt_offset,
+                                           reinterpret_cast<uint64_t>(ra.devicePointer), ray_count,
+                                           reinterpret_cast<uint64_t>(ha.devicePointer), stream);
+        cudaGetLastError();  // a pageable pointer is not an error here
+    }
     const uint64_t chunk = std::min<uint64_t>(chunk_rays ? chunk_rays : (1u << 20), ray_count);
     auto& hq = ctx->hq;
     std::lock_guard<std::mutex> lk(hq.mu);

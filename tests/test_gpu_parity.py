@@ -330,8 +330,10 @@ def test_mid_size_mesh_bit_exact(device):
 
 
 def test_host_buffer_query_matches_device_query(device):
-    """rt_trace_ray_buffer_host (chunked, two streams, ragged last chunk)
-    returns the same hits as rt_cmd_trace_ray_buffer."""
+    """rt_trace_ray_buffer_host returns the same hits as
+    rt_cmd_trace_ray_buffer: pinned buffers traced in place (chunk_rays 0),
+    staged chunks on two streams with a ragged last chunk, and pageable
+    buffers (chunk_rays 0 falls back to the staged copies)."""
     import torch
 
     host = _host()
@@ -341,14 +343,22 @@ def test_host_buffer_query_matches_device_query(device):
     rays["tmax"] = 1e4
     ref = host.trace_ray_buffer(device, gs, rays)
     rays_h = torch.from_numpy(rays.view(np.uint8).copy()).pin_memory()
+    push = gs.push_constants(0)
+
+    def query(rays_ptr, hits_ptr, chunk):
+        device.check(device.lib.rt_trace_ray_buffer_host(device.ctx, gs.tlas.device_address(), C.byref(push), None,
+                                                         0, 0xFF, 0, rays_ptr, len(rays), hits_ptr, chunk,
+                                                         host.Device.stream_handle()))
+        torch.cuda.synchronize()
+
     for chunk in (3000, 0, 20011):
         hits_h = torch.zeros(len(rays) * abi.HIT_DTYPE.itemsize, dtype=torch.uint8).pin_memory()
-        push = gs.push_constants(0)
-        device.check(device.lib.rt_trace_ray_buffer_host(device.ctx, gs.tlas.device_address(), C.byref(push), None,
-                                                         0, 0xFF, 0, rays_h.data_ptr(), len(rays), hits_h.data_ptr(),
-                                                         chunk, host.Device.stream_handle()))
-        torch.cuda.synchronize()
+        query(rays_h.data_ptr(), hits_h.data_ptr(), chunk)
         _assert_hits_equal(hits_h.numpy().view(abi.HIT_DTYPE), ref, f"host query, chunk {chunk}")
+    rays_p = np.ascontiguousarray(rays)
+    hits_p = np.zeros(len(rays), abi.HIT_DTYPE)
+    query(rays_p.ctypes.data, hits_p.ctypes.data, 0)
+    _assert_hits_equal(hits_p, ref, "pageable host query")
 
 
 def test_double_buffered_frame_loop_matches_serial_frames(device):
