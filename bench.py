@@ -15,7 +15,8 @@ launching stream, both frame streams joined at the end) with the frames'
 instance records already resident and the L2 flushed before every frame by a
 256 MiB write on its stream (inside the span); `e2e` times the same loop
 through the C ABI with host buffers: each frame's instance records copied in
-from pinned host memory and its RGBA8 image copied back, inside the span.
+from pinned host memory and its RGBA8 image written by the output kernel into
+pinned host memory (through the buffer's mapping), inside the span.
 Per-kernel times and the roofline come from serial frames outside the span.
 --workload scene runs the same loop on the reference's default scene built
 from GLB / PNG files (DefaultSceneFrames: 1280x720, TLAS refit per frame).
@@ -432,7 +433,7 @@ def bench_ours(args):
     e_begin.record(stream)
     loop.begin()
     for k in range(args.steps):
-        frame(k, instances_host=pinned_frames[k % FRAMES], image_host=images_host[k & 1])
+        frame(k, instances_host=pinned_frames[k % FRAMES], image_host=images_host[k & 1], image_direct=True)
     loop.end()
     e_end.record(stream)
     torch.cuda.synchronize()

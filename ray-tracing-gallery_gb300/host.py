@@ -328,15 +328,17 @@ class PerFrameResources:
         self.uniforms_buffer.copy_(host, non_blocking=False)
 
     def record(self, max_trace_depth: int, shadow_ray_count: int, flags: int = 0,
-               sbt: abi.RtShaderBindingTable | None = None, stream=None) -> None:
-        """cmd_trace_rays(raygen, miss, hit, {}, W, H, 1)."""
+               sbt: abi.RtShaderBindingTable | None = None, stream=None, image_address: int | None = None) -> None:
+        """cmd_trace_rays(raygen, miss, hit, {}, W, H, 1).  image_address:
+        where the RGBA8 image goes instead of this frame's device image (e.g.
+        a page-locked host buffer, which the GPU writes through its mapping)."""
         push = self.gpu_scene.push_constants(self.uniforms_buffer.data_ptr(), self.tlas)
         d = abi.RtTraceRaysDesc()
         d.width, d.height = self.width, self.height
         d.max_trace_depth = max_trace_depth
         d.shadow_ray_count = shadow_ray_count
         d.flags = flags
-        d.image_address = self.image.data_ptr()
+        d.image_address = image_address if image_address is not None else self.image.data_ptr()
         d.radiance_address = self.radiance.data_ptr() if self.radiance is not None else 0
         sbt_p = C.byref(sbt) if sbt is not None else None
         self.device.check(self.device.lib.rt_cmd_trace_rays(self.device.ctx, C.byref(push), sbt_p, C.byref(d),
@@ -369,12 +371,14 @@ class FrameLoop:
 
     def record(self, k: int, max_trace_depth: int, shadow_ray_count: int, instances=None, instances_host=None,
                uniforms_dev=None, image_host=None, flags: int = 0, before=None,
-               refit: bool = False) -> PerFrameResources:
+               refit: bool = False, image_direct: bool = False) -> PerFrameResources:
         """Frame k: new instance records (a device tensor, or pinned host bytes
         copied in on the slot's stream), TLAS rebuild (or, with refit, the
         in-place update of DefaultScene::write_resources, scene.rs:167-204),
-        uniforms (a device copy), the trace, and optionally the image copied
-        to pinned host memory."""
+        uniforms (a device copy), the trace, and optionally the image in
+        pinned host memory: copied there after the frame, or with
+        image_direct written there by the output kernel itself (through the
+        buffer's mapping into the GPU's address space)."""
         i = k % len(self.slots)
         fr, st = self.slots[i], self.streams[i]
         with torch.cuda.stream(st):
@@ -389,8 +393,10 @@ class FrameLoop:
                 fr.tlas.rebuild_tlas(self.device, instances, fr.num_instances, self.scratch[i], st)
             if uniforms_dev is not None:
                 fr.uniforms_buffer.copy_(uniforms_dev, non_blocking=True)
-            fr.record(max_trace_depth, shadow_ray_count, flags, stream=st)
-            if image_host is not None:
+            direct = image_host is not None and image_direct
+            fr.record(max_trace_depth, shadow_ray_count, flags, stream=st,
+                      image_address=image_host.data_ptr() if direct else None)
+            if image_host is not None and not direct:
                 image_host.copy_(fr.image, non_blocking=True)
         return fr
 

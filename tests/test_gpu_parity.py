@@ -384,12 +384,13 @@ def test_double_buffered_frame_loop_matches_serial_frames(device):
         torch.cuda.synchronize()
         ref.append(serial.image.clone())
     loop = host.FrameLoop(device, gs, W, H, frames_in_flight=2)
-    got = [torch.empty_like(r, device="cpu").pin_memory() for r in ref]
-    loop.begin()
-    for k in range(6):
-        loop.record(k, 2, 4, instances=frames[k], uniforms_dev=unis[k], image_host=got[k])
-    loop.end()
-    torch.cuda.synchronize()
-    for k in range(6):
-        assert torch.equal(got[k], ref[k].cpu()), f"frame {k}"
+    for direct in (False, True):  # image copied after the frame, or written into the pinned buffer
+        got = [torch.zeros_like(r, device="cpu").pin_memory() for r in ref]
+        loop.begin()
+        for k in range(6):
+            loop.record(k, 2, 4, instances=frames[k], uniforms_dev=unis[k], image_host=got[k], image_direct=direct)
+        loop.end()
+        torch.cuda.synchronize()
+        for k in range(6):
+            assert torch.equal(got[k], ref[k].cpu()), f"frame {k}, direct {direct}"
     assert len({int(r.float().sum()) for r in ref}) > 1  # the frames differ
