@@ -410,10 +410,15 @@ class FrameLoop:
 
 
 def batch_scene(frame: PerFrameResources, max_trace_depth: int, shadow_ray_count: int,
-                flags: int = 0) -> abi.RtBatchScene:
-    """The RtBatchScene of one frame (its scene's own texture table, if any)."""
+                flags: int = 0, uniforms_address: int | None = None,
+                image_address: int | None = None) -> abi.RtBatchScene:
+    """The RtBatchScene of one frame (its scene's own texture table, if any).
+    uniforms_address / image_address replace the frame's own uniform buffer
+    and image: any device address, or a pinned host pointer, which the output
+    kernel then writes over the mapped host path."""
     b = abi.RtBatchScene()
-    b.push = frame.gpu_scene.push_constants(frame.uniforms_buffer.data_ptr(), frame.tlas)
+    uni = uniforms_address if uniforms_address is not None else frame.uniforms_buffer.data_ptr()
+    b.push = frame.gpu_scene.push_constants(uni, frame.tlas)
     gs = frame.gpu_scene
     if gs.texture_table is not None:
         b.texture_table = gs.texture_table.data_ptr()
@@ -423,7 +428,7 @@ def batch_scene(frame: PerFrameResources, max_trace_depth: int, shadow_ray_count
     d.max_trace_depth = max_trace_depth
     d.shadow_ray_count = shadow_ray_count
     d.flags = flags
-    d.image_address = frame.image.data_ptr()
+    d.image_address = image_address if image_address is not None else frame.image.data_ptr()
     d.radiance_address = frame.radiance.data_ptr() if frame.radiance is not None else 0
     return b
 

@@ -128,6 +128,44 @@ def test_batch_graph_replay(device):
             assert torch.equal(fr.image, direct[k]), f"scene {k} differs after graph replay"
 
 
+def test_batch_into_pinned_host_images(device):
+    """Uniform blocks read from one shared device array and images written by
+    the output kernel straight into pinned host buffers: the same bytes as the
+    device images, for a direct call and a graph replay."""
+    import ctypes as C
+
+    import torch
+
+    host = _host()
+    frames = _frames(device, _specs()[:4])
+    host.trace_batch(device, [host.batch_scene(fr, d, s) for fr, d, s in frames])
+    torch.cuda.synchronize()
+    want = [fr.image.cpu() for fr, _, _ in frames]
+    usz = C.sizeof(abi.RtUniforms)
+    uni = torch.from_numpy(np.concatenate(
+        [np.frombuffer(bytes(fr.gpu_scene.scene.uniforms), np.uint8) for fr, _, _ in frames])).cuda()
+    out = [torch.zeros_like(fr.image, device="cpu").pin_memory() for fr, _, _ in frames]
+    batch = [host.batch_scene(fr, d, s, uniforms_address=uni.data_ptr() + k * usz, image_address=out[k].data_ptr())
+             for k, (fr, d, s) in enumerate(frames)]
+    host.trace_batch(device, batch)
+    torch.cuda.synchronize()
+    for k in range(len(frames)):
+        assert torch.equal(out[k], want[k]), f"scene {k}: pinned host image differs"
+    stream = torch.cuda.Stream()
+    with torch.cuda.stream(stream):
+        host.trace_batch(device, batch, stream=stream)
+    stream.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=stream):
+        host.trace_batch(device, batch, stream=stream)
+    for t in out:
+        t.zero_()
+    g.replay()
+    torch.cuda.synchronize()
+    for k in range(len(frames)):
+        assert torch.equal(out[k], want[k]), f"scene {k}: pinned host image differs after graph replay"
+
+
 def test_batch_rejects_bad_scenes(device):
     host = _host()
     frames = _frames(device, _specs()[:2])
