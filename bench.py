@@ -379,6 +379,25 @@ def bench_ours(args):
         frame(k, instances=frames_dev[k % FRAMES])
     loop.end()
     torch.cuda.synchronize()
+
+    # ---- the autotuner picks the traversal configuration on one frame of this workload (a batch of
+    # one: the first slot's TLAS and frame 0's uniforms), untimed; the loop then runs with it ----
+    t_tune = time.perf_counter()
+    tune_item = host.batch_scene(loop.slots[0], DEPTH, SHADOWS, uniforms_address=uni_dev[0].data_ptr())
+    tune_arr = (abi.RtBatchScene * 1)(tune_item)
+    report = abi.RtAutotuneReport()
+    dev.check(lib.rt_ctx_autotune(dev.ctx, tune_arr, 1, None, 3, host.Device.stream_handle(stream),
+                                  C.byref(report)))
+    tuned = report.configs[report.best]
+    tune_s = time.perf_counter() - t_tune
+    default_cfg = (128, 0, 20, abi.RT_TRAVERSAL_PACKET_PRIMARY)
+    tune_default_ms = [report.median_ms[i] for i in range(report.count)
+                       if report.configs[i].as_tuple() == default_cfg][0]
+    loop.begin()
+    for k in range(args.warmup):
+        frame(k, instances=frames_dev[k % FRAMES])
+    loop.end()
+    torch.cuda.synchronize()
     dev.read_stats(reset=True)
 
     # ---- device-resident timing (value): one span over all frames, both streams ----
@@ -478,7 +497,16 @@ def bench_ours(args):
                        "trace_pipeline_ms_per_step": sum(trace_ms) / len(trace_ms),
                        "traversal_ms_per_step": sum(traversal_ms) / len(traversal_ms),
                        "shade_ms_per_step": sum(kt["shade_ms"] for kt in kernel_times) / len(kernel_times),
-                       "tlas_build_and_flush_ms_per_step": (sum(serial_ms) - sum(trace_ms)) / len(serial_ms)},
+                       "tlas_build_and_flush_ms_per_step": (sum(serial_ms) - sum(trace_ms)) / len(serial_ms),
+                       "traversal_config": {"block_size": tuned.block_size,
+                                            "shared_stack_depth": tuned.shared_stack_depth,
+                                            "leaf_wait": tuned.leaf_wait, "packet_lists": tuned.packet_lists,
+                                            "chosen_by": f"rt_ctx_autotune on frame 0 ({report.count} configs, "
+                                                         f"{tune_s:.1f} s, untimed)",
+                                            "tuned_ms": report.median_ms[report.best],
+                                            "default_config_ms": tune_default_ms},
+                       "work_counts": "nodes / triangles per ray from a statistics frame of the per-lane "
+                                      "traversal (what each ray needs)"},
             "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": n_inst * 64,
                     "d2h_bytes_per_step": W * H * 4},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -868,9 +896,9 @@ def bench_batch(args):
     report = abi.RtAutotuneReport()
     t_tune = time.perf_counter()
     dev.check(lib.rt_ctx_autotune(dev.ctx, arr, len(items), None, 3, sh, C.byref(report)))
-    best8 = (report.median_ms[report.best], abi.RtTraversalConfig(*report.configs[report.best].as_tuple(), 0))
+    best8 = (report.median_ms[report.best], abi.RtTraversalConfig(*report.configs[report.best].as_tuple()))
     default_ms = [report.median_ms[i] for i in range(report.count)
-                  if report.configs[i].as_tuple() == (128, 0, 20)][0]
+                  if report.configs[i].as_tuple() == (128, 0, 20, abi.RT_TRAVERSAL_PACKET_PRIMARY)][0]
     _, frames4 = batch_setup(dev, args.batch_scenes, width4=True)
     items4 = [host.batch_scene(fr, sc.max_trace_depth, sc.shadow_ray_count) for fr, sc in zip(frames4, scs)]
     arr4 = (abi.RtBatchScene * len(items4))(*items4)
@@ -879,7 +907,7 @@ def bench_batch(args):
     torch.cuda.synchronize()
     report4 = abi.RtAutotuneReport()
     dev.check(lib.rt_ctx_autotune(dev.ctx, arr4, len(items4), None, 3, sh, C.byref(report4)))
-    best4 = (report4.median_ms[report4.best], abi.RtTraversalConfig(*report4.configs[report4.best].as_tuple(), 0))
+    best4 = (report4.median_ms[report4.best], abi.RtTraversalConfig(*report4.configs[report4.best].as_tuple()))
     tune_s = time.perf_counter() - t_tune
     width = 4 if best4[0] < best8[0] else 8
     tuned = best4[1] if width == 4 else best8[1]
@@ -984,7 +1012,7 @@ def bench_batch(args):
                        "batched_graph_mrays_s": value,
                        "autotuned_config": {"node_width": width, "block_size": tuned.block_size,
                                             "shared_stack_depth": tuned.shared_stack_depth,
-                                            "leaf_wait": tuned.leaf_wait},
+                                            "leaf_wait": tuned.leaf_wait, "packet_lists": tuned.packet_lists},
                        "autotune_configs": int(report.count + report4.count), "autotune_s": tune_s,
                        "autotune_best_ms_width8": best8[0], "autotune_best_ms_width4": best4[0],
                        "autotune_best_config_width8": best8[1].as_tuple(),

@@ -428,12 +428,19 @@ RTCORE_API int32_t rt_cmd_trace_rays_batched(rt_ctx* ctx, const RtBatchScene* sc
  *                       24 or 32 (the rest of the 64 live in local memory)
  *   leaf_wait           0..32: a warp runs leaf steps once leaf_wait/32 of its
  *                       lanes wait on one, else node steps
- * Default {128, 0, 20}. */
+ *   packet_lists        RT_TRAVERSAL_PACKET_* bits: the ray lists a warp
+ *                       traverses as one packet of 32 neighbouring rays (one
+ *                       node sequence for the union of their box hits, stack
+ *                       in shared memory); the other lists run one ray per
+ *                       lane with the three fields above
+ * Default {128, 0, 20, RT_TRAVERSAL_PACKET_PRIMARY}. */
+#define RT_TRAVERSAL_PACKET_PRIMARY 0x1u /* camera rays (8x4 pixel tiles) and their mirror / portal bounces */
+#define RT_TRAVERSAL_PACKET_SHADOW 0x2u  /* the shadow rays of each shaded pixel, appended per shading warp */
 typedef struct RtTraversalConfig {
     uint32_t block_size;
     uint32_t shared_stack_depth;
     uint32_t leaf_wait;
-    uint32_t _padding;
+    uint32_t packet_lists;
 } RtTraversalConfig;
 RTCORE_API int32_t rt_ctx_set_traversal_config(rt_ctx* ctx, const RtTraversalConfig* config);
 RTCORE_API int32_t rt_ctx_get_traversal_config(rt_ctx* ctx, RtTraversalConfig* out);

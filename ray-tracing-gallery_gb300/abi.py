@@ -33,10 +33,12 @@ RT_INSTANCE_TRIANGLE_FLIP_FACING = 0x2
 RT_INSTANCE_FORCE_OPAQUE = 0x4
 RT_INSTANCE_FORCE_NO_OPAQUE = 0x8
 RT_GEOMETRY_OPAQUE = 0x1
+RT_GEOMETRY_NO_DUPLICATE_ANY_HIT_INVOCATION = 0x2
 RT_BUILD_ALLOW_UPDATE = 0x1
 RT_BUILD_ALLOW_COMPACTION = 0x2
 RT_BUILD_PREFER_FAST_TRACE = 0x4
 RT_BUILD_PREFER_FAST_BUILD = 0x8
+RT_BUILD_LOW_MEMORY = 0x10
 RT_BUILD_QUANTIZED_NODES = 0x100
 RT_BUILD_EXT_NODE_WIDTH_4 = 0x200
 RT_RAY_FLAG_NONE = 0x0
@@ -213,12 +215,16 @@ class RtBatchScene(C.Structure):
 RT_MAX_BATCH_SCENES = 65536
 
 
+RT_TRAVERSAL_PACKET_PRIMARY = 0x1
+RT_TRAVERSAL_PACKET_SHADOW = 0x2
+
+
 class RtTraversalConfig(C.Structure):
     _fields_ = [("block_size", C.c_uint32), ("shared_stack_depth", C.c_uint32), ("leaf_wait", C.c_uint32),
-                ("_padding", C.c_uint32)]
+                ("packet_lists", C.c_uint32)]
 
     def as_tuple(self) -> tuple:
-        return (self.block_size, self.shared_stack_depth, self.leaf_wait)
+        return (self.block_size, self.shared_stack_depth, self.leaf_wait, self.packet_lists)
 
 
 RT_AUTOTUNE_MAX_CONFIGS = 64

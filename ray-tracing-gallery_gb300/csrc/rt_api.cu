@@ -111,7 +111,7 @@ struct rt_ctx {
     std::mutex mu;
     std::vector<Workspace> workspaces;
     KernelTimer timer;
-    RtTraversalConfig traversal{128, 0, 20, 0};
+    RtTraversalConfig traversal{128, 0, 20, RT_TRAVERSAL_PACKET_PRIMARY};
     // rt_trace_ray_buffer_host: two streams and their device staging (rays, then hits)
     struct HostQuery {
         std::mutex mu;
@@ -661,12 +661,11 @@ RTCORE_API int32_t rt_cmd_trace_rays_batched(rt_ctx* ctx, const RtBatchScene* sc
 RTCORE_API int32_t rt_ctx_set_traversal_config(rt_ctx* ctx, const RtTraversalConfig* config) {
     if (!ctx || !config) return fail(RT_ERR_INVALID, "ctx or config is NULL");
     if (!traversal_config_supported(*config))
-        return fail(RT_ERR_UNSUPPORTED, "traversal config {%u, %u, %u} is not built (block 64/128/256, shared stack "
-                    "depth 0/16/24/32, leaf_wait <= 32)", config->block_size, config->shared_stack_depth,
-                    config->leaf_wait);
+        return fail(RT_ERR_UNSUPPORTED, "traversal config {%u, %u, %u, 0x%x} is not built (block 64/128/256, shared "
+                    "stack depth 0/16/24/32, leaf_wait <= 32, packet_lists <= 3)", config->block_size,
+                    config->shared_stack_depth, config->leaf_wait, config->packet_lists);
     MaybeLock l(ctx);
     ctx->traversal = *config;
-    ctx->traversal._padding = 0;
     return RT_OK;
 }
 
@@ -684,35 +683,53 @@ RTCORE_API int32_t rt_ctx_autotune(rt_ctx* ctx, const RtBatchScene* scenes, uint
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     if (stream_capturing(s)) return fail(RT_ERR_INVALID, "rt_ctx_autotune cannot run inside a stream capture");
     reps = std::max(1u, std::min(reps, 64u));
+    // stage 1: the per-lane launch shapes, camera rays in packets; stage 2:
+    // the other packet_lists choices on the fastest shape
     static const uint32_t kBlocks[] = {64, 128, 256}, kDepths[] = {0, 16, 24, 32}, kWaits[] = {16, 20, 24};
     std::vector<RtTraversalConfig> cands;
     for (uint32_t b : kBlocks)
         for (uint32_t d : kDepths)
-            for (uint32_t w : kWaits) cands.push_back(RtTraversalConfig{b, d, w, 0});
+            for (uint32_t w : kWaits) cands.push_back(RtTraversalConfig{b, d, w, RT_TRAVERSAL_PACKET_PRIMARY});
     const RtTraversalConfig saved = ctx->traversal;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     cudaError_t ce = cudaEventCreate(&e0);
     if (ce == cudaSuccess) ce = cudaEventCreate(&e1);
     if (ce != cudaSuccess) return cuda_fail(ce, "rt_ctx_autotune (events)");
-    std::vector<float> med(cands.size(), 0.0f);
+    std::vector<float> med;
     int32_t r = RT_OK;
-    for (size_t i = 0; i < cands.size() && r == RT_OK; i++) {
-        ctx->traversal = cands[i];
-        std::vector<float> t;
-        for (uint32_t k = 0; k <= reps && r == RT_OK; k++) {
-            ce = cudaEventRecord(e0, s);
-            if (ce == cudaSuccess) r = rt_cmd_trace_rays_batched(ctx, scenes, scene_count, sbt, 0, stream);
-            if (r == RT_OK && ce == cudaSuccess) ce = cudaEventRecord(e1, s);
-            if (r == RT_OK && ce == cudaSuccess) ce = cudaEventSynchronize(e1);
-            float ms = 0.0f;
-            if (r == RT_OK && ce == cudaSuccess) ce = cudaEventElapsedTime(&ms, e0, e1);
-            if (ce != cudaSuccess) r = cuda_fail(ce, "rt_ctx_autotune");
-            if (k > 0) t.push_back(ms);  // the first run is the warm-up
+    auto time_cands = [&](size_t from) {
+        for (size_t i = from; i < cands.size() && r == RT_OK; i++) {
+            ctx->traversal = cands[i];
+            std::vector<float> t;
+            for (uint32_t k = 0; k <= reps && r == RT_OK; k++) {
+                ce = cudaEventRecord(e0, s);
+                if (ce == cudaSuccess) r = rt_cmd_trace_rays_batched(ctx, scenes, scene_count, sbt, 0, stream);
+                if (r == RT_OK && ce == cudaSuccess) ce = cudaEventRecord(e1, s);
+                if (r == RT_OK && ce == cudaSuccess) ce = cudaEventSynchronize(e1);
+                float ms = 0.0f;
+                if (r == RT_OK && ce == cudaSuccess) ce = cudaEventElapsedTime(&ms, e0, e1);
+                if (ce != cudaSuccess) r = cuda_fail(ce, "rt_ctx_autotune");
+                if (k > 0) t.push_back(ms);  // the first run is the warm-up
+            }
+            if (r == RT_OK) {
+                std::sort(t.begin(), t.end());
+                med.push_back(t[t.size() / 2]);
+            }
         }
-        if (r == RT_OK) {
-            std::sort(t.begin(), t.end());
-            med[i] = t[t.size() / 2];
-        }
+    };
+    auto fastest = [&] {
+        size_t best = 0;
+        for (size_t i = 1; i < med.size(); i++)
+            if (med[i] < med[best]) best = i;
+        return best;
+    };
+    time_cands(0);
+    if (r == RT_OK) {
+        const RtTraversalConfig shape = cands[fastest()];
+        const size_t n1 = cands.size();
+        for (uint32_t pl : {0u, RT_TRAVERSAL_PACKET_SHADOW, RT_TRAVERSAL_PACKET_PRIMARY | RT_TRAVERSAL_PACKET_SHADOW})
+            cands.push_back(RtTraversalConfig{shape.block_size, shape.shared_stack_depth, shape.leaf_wait, pl});
+        time_cands(n1);
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
@@ -720,9 +737,7 @@ RTCORE_API int32_t rt_ctx_autotune(rt_ctx* ctx, const RtBatchScene* scenes, uint
         ctx->traversal = saved;
         return r;
     }
-    size_t best = 0;
-    for (size_t i = 1; i < cands.size(); i++)
-        if (med[i] < med[best]) best = i;
+    const size_t best = fastest();
     ctx->traversal = cands[best];
     if (report) {
         memset(report, 0, sizeof *report);

@@ -379,6 +379,80 @@ __device__ __noinline__ bool ids_below_best(const InstRecord* insts, uint32_t c_
     return prim < hit_prim;
 }
 
+// Moves the lane's ray into the object space of TLAS instance `first` (its
+// record's BLAS fields q0 = blas lo, blas hi, instance_id, custom_mask and
+// q1 = sbt_flags, tri_count, node_count, prims_off256).
+__device__ __forceinline__ void enter_instance(Trav& s, const InstRecord* ir, uint4 q0, uint4 q1, uint32_t first) {
+    const float4* wp = reinterpret_cast<const float4*>(ir->w2o);
+    float4 w0 = __ldg(wp), w1 = __ldg(wp + 1), w2 = __ldg(wp + 2);
+    const float w[12] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w, w2.x, w2.y, w2.z, w2.w};
+    s.o = xform_point(w, s.wo);
+    s.d = xform_dir(w, s.wd);
+    s.inv = safe_inv(s.d);
+    s.oct = octant_offsets(s.inv);
+    s.wt = wt_setup(s.d);
+    const uint8_t* blas = reinterpret_cast<const uint8_t*>(((uint64_t)q0.y << 32) | q0.x);
+    s.nodes = reinterpret_cast<const WideNode*>(blas + kHeaderBytes);
+    s.tris = reinterpret_cast<const TriRecord*>(blas + (uint64_t)q1.w * 256u);
+    s.node_count = q1.z & ~kQuantizedBlasBit;
+    s.quant = (q1.z & kQuantizedBlasBit) != 0u;
+    s.tri_count = q1.y;
+    s.c_inst = first;
+    s.c_sbt_flags = q1.x;
+    s.in_blas = true;
+}
+
+// Triangle `idx` of the current BLAS against the lane's ray: the opacity and
+// facing flags of the ray and the instance, the watertight test, the
+// total-order tie break and the alpha-clip any-hit.  An accepted triangle
+// becomes the best hit and the call returns true.
+template <bool STATS, class SV>
+__device__ __forceinline__ bool try_triangle(Trav& s, const SV& sv, const RtShaderBindingTable* sbt,
+                                             uint32_t ray_flags, uint32_t ray_sbt_offset, uint32_t idx,
+                                             Counters& cnt) {
+    const uint32_t iflags = s.c_sbt_flags >> 24;
+    if (STATS) cnt.tris++;
+    const float4* tp = reinterpret_cast<const float4*>(s.tris + idx);
+    float4 p0 = __ldg(tp), p1 = __ldg(tp + 1), p2 = __ldg(tp + 2);
+    uint32_t prim = __float_as_uint(p0.w), geom = __float_as_uint(p1.w), tfl = __float_as_uint(p2.w);
+    bool opaque = (tfl & 1u) != 0u;
+    if (iflags & RT_INSTANCE_FORCE_OPAQUE) opaque = true;
+    if (iflags & RT_INSTANCE_FORCE_NO_OPAQUE) opaque = false;
+    if (ray_flags & RT_RAY_FLAG_OPAQUE) opaque = true;
+    if (ray_flags & RT_RAY_FLAG_NO_OPAQUE) opaque = false;
+    if ((ray_flags & RT_RAY_FLAG_CULL_OPAQUE) && opaque) return false;
+    if ((ray_flags & RT_RAY_FLAG_CULL_NO_OPAQUE) && !opaque) return false;
+    float t, u, v;
+    bool front;
+    if (!tri_intersect(s.o, s.wt, mk3(p0.x, p0.y, p0.z), mk3(p1.x, p1.y, p1.z), mk3(p2.x, p2.y, p2.z), s.tmin, s.t,
+                       &t, &u, &v, &front))
+        return false;
+    if (iflags & RT_INSTANCE_TRIANGLE_FLIP_FACING) front = !front;
+    if (!(iflags & RT_INSTANCE_TRIANGLE_FACING_CULL_DISABLE)) {
+        if ((ray_flags & RT_RAY_FLAG_CULL_BACK_FACING) && !front) return false;
+        if ((ray_flags & RT_RAY_FLAG_CULL_FRONT_FACING) && front) return false;
+    }
+    if (t == s.t && s.hit_inst != kNoHit &&
+        !ids_below_best(sv(s.scene).insts, s.c_inst, s.hit_inst, geom, prim, s.hit_geom, s.hit_prim))
+        return false;
+    if (!opaque) {
+        const Env e = sv(s.scene);
+        const RtHitGroup* g = e.models ? hit_group(sbt, s.c_sbt_flags, ray_sbt_offset) : nullptr;
+        if (g && g->any_hit == RT_PROGRAM_ANY_HIT_ALPHA_CLIP &&
+            !alpha_clip_accepts(e.models, e.textures, e.texture_count, e.insts[s.c_inst].custom_mask & 0xFFFFFFu,
+                                geom, prim, u, v))
+            return false;
+    }
+    s.t = t;
+    s.u = u;
+    s.v = v;
+    s.hit_inst = s.c_inst;
+    s.hit_geom = geom;
+    s.hit_prim = prim;
+    s.front = front;
+    return true;
+}
+
 // One traversal step.  Returns true when the ray is finished (s.t/hit_* hold
 // the result; with terminate-on-first-hit, any accepted hit finishes it).
 // KINDS (kBlasKind* bits) are the BLAS node formats this instantiation
@@ -505,23 +579,7 @@ __device__ __forceinline__ bool trav_step(Trav& s, STK& stack, const SV& sv, con
             }
             if (enter) {
                 if (STATS) cnt.insts++;
-                const float4* wp = reinterpret_cast<const float4*>(ir->w2o);
-                float4 w0 = __ldg(wp), w1 = __ldg(wp + 1), w2 = __ldg(wp + 2);
-                const float w[12] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w, w2.x, w2.y, w2.z, w2.w};
-                s.o = xform_point(w, s.wo);
-                s.d = xform_dir(w, s.wd);
-                s.inv = safe_inv(s.d);
-                s.oct = octant_offsets(s.inv);
-                s.wt = wt_setup(s.d);
-                const uint8_t* blas = reinterpret_cast<const uint8_t*>(((uint64_t)q0.y << 32) | q0.x);
-                s.nodes = reinterpret_cast<const WideNode*>(blas + kHeaderBytes);
-                s.tris = reinterpret_cast<const TriRecord*>(blas + (uint64_t)q1.w * 256u);
-                s.node_count = q1.z & ~kQuantizedBlasBit;
-                s.quant = (q1.z & kQuantizedBlasBit) != 0u;
-                s.tri_count = q1.y;
-                s.c_inst = first;
-                s.c_sbt_flags = q1.x;
-                s.in_blas = true;
+                enter_instance(s, ir, q0, q1, first);
                 if (s.sp < (int)kStackSize) {
                     stack.put(s.sp++, make_uint2(kMarker, 0u));
                     s.entry = 0;  // BLAS root
@@ -531,48 +589,9 @@ __device__ __forceinline__ bool trav_step(Trav& s, STK& stack, const SV& sv, con
                 trav_restore_world(s, sv(s.scene));
             }
         } else {
-            const uint32_t iflags = s.c_sbt_flags >> 24;
             for (uint32_t q = 0; q < count; q++) {
-                if (STATS) cnt.tris++;
-                const float4* tp = reinterpret_cast<const float4*>(s.tris + first + q);
-                float4 p0 = __ldg(tp), p1 = __ldg(tp + 1), p2 = __ldg(tp + 2);
-                uint32_t prim = __float_as_uint(p0.w), geom = __float_as_uint(p1.w), tfl = __float_as_uint(p2.w);
-                bool opaque = (tfl & 1u) != 0u;
-                if (iflags & RT_INSTANCE_FORCE_OPAQUE) opaque = true;
-                if (iflags & RT_INSTANCE_FORCE_NO_OPAQUE) opaque = false;
-                if (ray_flags & RT_RAY_FLAG_OPAQUE) opaque = true;
-                if (ray_flags & RT_RAY_FLAG_NO_OPAQUE) opaque = false;
-                if ((ray_flags & RT_RAY_FLAG_CULL_OPAQUE) && opaque) continue;
-                if ((ray_flags & RT_RAY_FLAG_CULL_NO_OPAQUE) && !opaque) continue;
-                float t, u, v;
-                bool front;
-                if (!tri_intersect(s.o, s.wt, mk3(p0.x, p0.y, p0.z), mk3(p1.x, p1.y, p1.z), mk3(p2.x, p2.y, p2.z),
-                                   s.tmin, s.t, &t, &u, &v, &front))
-                    continue;
-                if (iflags & RT_INSTANCE_TRIANGLE_FLIP_FACING) front = !front;
-                if (!(iflags & RT_INSTANCE_TRIANGLE_FACING_CULL_DISABLE)) {
-                    if ((ray_flags & RT_RAY_FLAG_CULL_BACK_FACING) && !front) continue;
-                    if ((ray_flags & RT_RAY_FLAG_CULL_FRONT_FACING) && front) continue;
-                }
-                if (t == s.t && s.hit_inst != kNoHit &&
-                    !ids_below_best(sv(s.scene).insts, s.c_inst, s.hit_inst, geom, prim, s.hit_geom, s.hit_prim))
-                    continue;
-                if (!opaque) {
-                    const Env e = sv(s.scene);
-                    const RtHitGroup* g = e.models ? hit_group(sbt, s.c_sbt_flags, ray_sbt_offset) : nullptr;
-                    if (g && g->any_hit == RT_PROGRAM_ANY_HIT_ALPHA_CLIP &&
-                        !alpha_clip_accepts(e.models, e.textures, e.texture_count,
-                                            e.insts[s.c_inst].custom_mask & 0xFFFFFFu, geom, prim, u, v))
-                        continue;
-                }
-                s.t = t;
-                s.u = u;
-                s.v = v;
-                s.hit_inst = s.c_inst;
-                s.hit_geom = geom;
-                s.hit_prim = prim;
-                s.front = front;
-                if (ray_flags & RT_RAY_FLAG_TERMINATE_ON_FIRST_HIT) {
+                if (try_triangle<STATS>(s, sv, sbt, ray_flags, ray_sbt_offset, first + q, cnt) &&
+                    (ray_flags & RT_RAY_FLAG_TERMINATE_ON_FIRST_HIT)) {
                     s.entry = kNoEntry;
                     return true;
                 }
@@ -907,6 +926,246 @@ __global__ void __launch_bounds__(BLOCK, trace_warps_per_sm(KINDS) * 32 / BLOCK)
     if (kinds_selected(P.kinds_built, P.B.ctr->kinds, KINDS)) trace_wavefront<MODE, STATS, KINDS, SD, BLOCK>(P);
 }
 
+// ---------------------------------------------------------------------------
+// Packet traversal of the wavefront lists.  Neighbouring entries of a list
+// are neighbouring rays: the primary list holds the 32 rays of one 8x4 pixel
+// tile per warp-sized chunk, and a shading warp appends the shadow rays of
+// its pixels contiguously.  A warp takes a chunk of 32 entries and walks one
+// node sequence for its rays of one scene (a sub-packet): every lane tests
+// the node's eight children against its own ray, each child's key is reduced
+// to its minimum over the lanes (REDUX), and the union of the hit children,
+// ordered by those keys, goes on one stack per warp in shared memory.
+// Leaves and instance entries run once for the sub-packet, each lane testing
+// its own ray.  A lane tests every triangle of every box its ray hits (and
+// some more), so the closest hit under the total order is the per-lane
+// traversal's, bit for bit; every lane runs the same steps, so the SIMD
+// lanes stay full while the rays agree.
+// ---------------------------------------------------------------------------
+
+// Traverses the sub-packet `act` (the calling lanes, converged, one scene,
+// each at the TLAS root).  ws: the warp's stack (kStackSize entries).
+template <bool STATS, uint32_t KINDS>
+__device__ __forceinline__ void packet_traverse(Trav& s, uint2* ws, const unsigned act, const SceneTable& sv,
+                                                const RtShaderBindingTable* sbt, uint32_t* status,
+                                                uint32_t ray_flags, uint32_t ray_sbt_offset, Counters& cnt) {
+    const bool any_hit = (ray_flags & RT_RAY_FLAG_TERMINATE_ON_FIRST_HIT) != 0u;
+    const bool leader = (threadIdx.x & 31u) == (uint32_t)(__ffs(act) - 1);
+    bool done = false;  // any-hit rays: an accepted hit ends the lane's part
+    uint32_t entry = s.entry;
+    int sp = 0;
+    uint32_t steps = 0;
+    while (entry != kNoEntry) {
+        if (++steps > kMaxTraversalSteps) {
+            if (leader) atomicOr(status, 1u << RT_ERR_TIMEOUT);
+            break;
+        }
+        bool pop = true;
+        if (entry == kMarker) {
+            trav_restore_world(s, sv(s.scene));
+        } else if ((entry & kLeafEntry) == 0u) {
+            if (entry >= s.node_count) {
+                if (leader) atomicOr(status, 1u << RT_ERR_BAD_AS);
+            } else {
+                if (STATS) cnt.nodes++;
+                uint32_t keys[8], refs[8];
+                if ((KINDS & kBlasKindQ8) && s.in_blas && (KINDS == kBlasKindQ8 || s.quant))
+                    qnode_keys(s, entry, keys, refs);
+                else
+                    fnode_keys(s, entry, keys, refs);
+                // the nearest lane's key of each child; every lane has read its
+                // last popped entry before this point, so the pushes below
+                // cannot overwrite an entry a lane has yet to read
+#pragma unroll
+                for (int k = 0; k < 8; k++) keys[k] = __reduce_min_sync(act, done ? 0xFFFFFFFFu : keys[k]);
+                if (any_hit) {
+                    uint32_t mask = 0;
+#pragma unroll
+                    for (int k = 0; k < 8; k++) mask |= (keys[k] != 0xFFFFFFFFu ? 1u : 0u) << k;
+                    if (mask) {
+                        entry = pick8(refs, (uint32_t)(__ffs(mask) - 1));
+                        mask &= mask - 1u;
+                        while (mask) {
+                            const uint32_t k = (uint32_t)(__ffs(mask) - 1);
+                            mask &= mask - 1u;
+                            if (sp < (int)kStackSize) ws[sp++] = make_uint2(pick8(refs, k), 0u);
+                            else if (leader) atomicOr(status, 1u << RT_ERR_STACK_OVERFLOW);
+                        }
+                        pop = false;
+                    }
+                } else {
+                    sort8(keys);
+                    if (keys[0] != 0xFFFFFFFFu) {
+#pragma unroll
+                        for (int q = 7; q >= 1; q--) {
+                            const uint32_t key = keys[q];
+                            if (key == 0xFFFFFFFFu) continue;
+                            if (sp < (int)kStackSize) ws[sp++] = make_uint2(pick8(refs, key & 7u), key & ~7u);
+                            else if (leader) atomicOr(status, 1u << RT_ERR_STACK_OVERFLOW);
+                        }
+                        entry = pick8(refs, keys[0] & 7u);
+                        pop = false;
+                    }
+                }
+            }
+        } else {
+            const uint32_t first = entry & 0x0FFFFFFFu;
+            const uint32_t count = ((entry >> 28) & 7u) + 1u;
+            if (first + count > (s.in_blas ? s.tri_count : sv(s.scene).inst_count)) {
+                if (leader) atomicOr(status, 1u << RT_ERR_BAD_AS);
+            } else if (!s.in_blas) {
+                const InstRecord* ir = &sv(s.scene).insts[first];
+                const uint4* tail = reinterpret_cast<const uint4*>(&ir->blas);
+                const uint4 q0 = __ldg(tail), q1 = __ldg(tail + 1);
+                bool enter = q1.y != 0u && (q0.w >> 24) != 0u;  // cull mask 0xFF
+                if (enter && (blas_kind(q1.z) & KINDS) == 0u) {
+                    if (leader) atomicOr(status, 1u << RT_ERR_BAD_AS);
+                    enter = false;
+                }
+                if (enter) {
+                    if (sp < (int)kStackSize) {
+                        if (STATS) cnt.insts++;
+                        enter_instance(s, ir, q0, q1, first);
+                        __syncwarp(act);  // every lane has read the entry this push replaces
+                        ws[sp++] = make_uint2(kMarker, 0u);
+                        entry = 0;  // BLAS root
+                        pop = false;
+                    } else if (leader) {
+                        atomicOr(status, 1u << RT_ERR_STACK_OVERFLOW);
+                    }
+                }
+            } else {
+                if (!done) {
+                    for (uint32_t q = 0; q < count; q++) {
+                        if (try_triangle<STATS>(s, sv, sbt, ray_flags, ray_sbt_offset, first + q, cnt) && any_hit) {
+                            done = true;
+                            break;
+                        }
+                    }
+                }
+                if (any_hit && __all_sync(act, done)) break;
+            }
+        }
+        if (pop) {
+            // the next entry some lane still needs (markers always)
+            entry = kNoEntry;
+            const float cull = s.t * kBoxFarScale;
+            while (sp > 0) {
+                const uint2 en = ws[--sp];
+                if (en.x == kMarker) {
+                    entry = kMarker;
+                    break;
+                }
+                if (__any_sync(act, !done && !(__uint_as_float(en.y) > cull))) {
+                    entry = en.x;
+                    break;
+                }
+            }
+        }
+    }
+}
+
+template <int MODE, bool STATS, uint32_t KINDS, int BLOCK>
+__device__ __forceinline__ void trace_packets(const WfParams& P) {
+    __shared__ uint2 stacks[BLOCK / 32][kStackSize];
+    uint2* ws = stacks[threadIdx.x >> 5];
+    const SceneTable sv{P.B.scenes};
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t b = P.bounce;
+    uint32_t total;
+    uint32_t* work;
+    if (MODE == kModeBounce) {
+        total = P.B.ctr->ray_count[b];
+        work = &P.B.ctr->work[b];
+    } else {
+        total = P.B.ctr->shadow_count;
+        work = &P.B.ctr->work[kMaxDepth + 1];
+    }
+    const uint32_t ray_flags = MODE == kModeShadow
+                                   ? (RT_RAY_FLAG_TERMINATE_ON_FIRST_HIT | RT_RAY_FLAG_SKIP_CLOSEST_HIT_SHADER)
+                                   : RT_RAY_FLAG_NONE;
+    const uint32_t sbt_offset = MODE == kModeShadow ? 1u : 0u;
+    Counters cnt = {0, 0, 0};
+    for (;;) {
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(work, 32u);
+        base = __shfl_sync(0xFFFFFFFFu, base, 0);
+        if (base >= total) break;
+        const uint32_t item = base + lane;
+        const bool valid = item < total;
+        Trav s;
+        s.scene = 0;
+        s.entry = kNoEntry;
+        uint32_t depth = 0, depth0 = 0, pix = kNoPixel;  // depth of the ray traced / of the slot's ray
+        if (valid) {
+            uint32_t sc;
+            if (MODE == kModeBounce) {
+                const float4 a = P.B.rays[b & 1][2 * (size_t)item], c = P.B.rays[b & 1][2 * (size_t)item + 1];
+                pix = P.B.ray_pixel[b & 1][item];
+                const uint32_t rs = P.B.ray_scene[b & 1][item];
+                sc = rs & kSceneMask;
+                depth = depth0 = rs >> kSceneBits;
+                trav_begin(s, sv(sc), mk3(a.x, a.y, a.z), mk3(c.x, c.y, c.z), a.w, c.w);
+            } else {
+                const float4 a = P.B.shadow_rays[2 * (size_t)item], c = P.B.shadow_rays[2 * (size_t)item + 1];
+                pix = P.B.shadow_pixel[item];
+                sc = P.B.shadow_scene[item];
+                trav_begin(s, sv(sc), mk3(a.x, a.y, a.z), mk3(c.x, c.y, c.z), a.w, c.w);
+            }
+            s.scene = sc;
+        }
+        const bool heat = pix != kNoPixel && P.B.scenes[s.scene].uniforms->show_heatmap != 0;
+        const uint32_t t0 = heat ? (uint32_t)clock() : 0u;
+        unsigned pending = __ballot_sync(0xFFFFFFFFu, s.entry != kNoEntry);
+        while (pending) {
+            const uint32_t lead = (uint32_t)(__ffs(pending) - 1);
+            const uint32_t sc = __shfl_sync(0xFFFFFFFFu, s.scene, lead);
+            const unsigned act = __ballot_sync(0xFFFFFFFFu, ((pending >> lane) & 1u) != 0u && s.scene == sc);
+            pending &= ~act;
+            bool cont = false;
+            if ((act >> lane) & 1u) {
+                packet_traverse<STATS, KINDS>(s, ws, act, sv, &P.sbt, P.status, ray_flags, sbt_offset, cnt);
+                // a mirror / portal hit with depth left: the lane's next ray joins
+                // the chunk's next sub-packet (the closest-hit program's arithmetic)
+                if (MODE == kModeBounce && s.hit_inst != kNoHit && depth + 1 < P.B.scenes[s.scene].max_depth) {
+                    const NextRay nr = next_bounce_ray(P.B.scenes[s.scene].env, &P.sbt, s.hit_inst, s.hit_geom,
+                                                       s.hit_prim, s.t, s.u, s.v, s.wo, s.wd);
+                    if (nr.d.x != 0.0f || nr.d.y != 0.0f || nr.d.z != 0.0f) {
+                        trav_begin(s, sv(s.scene), nr.o, nr.d, 0.01f, 10000.0f);
+                        depth++;
+                        atomicAdd(reinterpret_cast<unsigned long long*>(&P.stats->traversals), 1ull);
+                        atomicAdd(reinterpret_cast<unsigned long long*>(&P.stats->secondary_rays), 1ull);
+                        cont = s.entry != kNoEntry;
+                    }
+                }
+            }
+            __syncwarp();
+            pending |= __ballot_sync(0xFFFFFFFFu, cont);
+        }
+        if (valid) {
+            if (MODE == kModeBounce) {
+                P.B.hits[2 * (size_t)item] = make_uint4(__float_as_uint(s.t), __float_as_uint(s.u),
+                                                        __float_as_uint(s.v), s.hit_inst);
+                P.B.hits[2 * (size_t)item + 1] = make_uint4(s.hit_geom, s.hit_prim, s.front ? 1u : 0u, 0u);
+                if (depth != depth0) {  // the slot's ray, for the shading kernel, is the last one traced
+                    P.B.rays[b & 1][2 * (size_t)item] = make_float4(s.wo.x, s.wo.y, s.wo.z, 0.01f);
+                    P.B.rays[b & 1][2 * (size_t)item + 1] = make_float4(s.wd.x, s.wd.y, s.wd.z, 10000.0f);
+                    P.B.ray_scene[b & 1][item] = s.scene | (depth << kSceneBits);
+                }
+            } else if (s.hit_inst == kNoHit) {
+                atomicAdd(&P.B.lit[pix], 1u);
+            }
+        }
+        if (heat) atomicAdd(&P.B.heat[pix], (unsigned long long)((uint32_t)clock() - t0));
+    }
+    flush_counters(P.stats, cnt);
+}
+
+template <int MODE, bool STATS, uint32_t KINDS, int BLOCK>
+__global__ void __launch_bounds__(BLOCK, trace_warps_per_sm(KINDS) * 32 / BLOCK)
+    k_trace_packet(const __grid_constant__ WfParams P) {
+    if (kinds_selected(P.kinds_built, P.B.ctr->kinds, KINDS)) trace_packets<MODE, STATS, KINDS, BLOCK>(P);
+}
+
 // The closest-hit and miss programs for the last ray of every slot of bounce
 // list b (its depth is in the slot's scene word).  Mirror and portal hits
 // that reach it end their pixel's bounce loop (no depth left, or a zero
@@ -1215,6 +1474,14 @@ void launch_trace_kernel(const WfParams& P, int num_sms, cudaStream_t stream) {
     note_launch(), kern<<<blocks, BLOCK, smem, stream>>>(P);
 }
 
+template <int MODE, bool STATS, uint32_t KINDS, int BLOCK>
+void launch_packet_kernel(const WfParams& P, int num_sms, cudaStream_t stream) {
+    const auto kern = k_trace_packet<MODE, STATS, KINDS, BLOCK>;
+    static int blocks = 0;
+    if (!blocks) blocks = persistent_blocks(kern, BLOCK, num_sms);
+    note_launch(), kern<<<blocks, BLOCK, 0, stream>>>(P);
+}
+
 // The traversal variants the autotuner chooses among: block size x depth of
 // the shared-memory part of the stack (kTraversalConfigs in the same order).
 #define RT_FOR_EACH_TRAVERSAL_VARIANT(X) \
@@ -1224,8 +1491,14 @@ void launch_trace_kernel(const WfParams& P, int num_sms, cudaStream_t stream) {
 template <int MODE, uint32_t K>
 void launch_trace_config(const WfParams& P, const RtTraversalConfig& c, bool stats, int num_sms,
                          cudaStream_t stream) {
-    if (stats) {  // statistics runs use the default variant
+    if (stats) {  // statistics runs use the default per-lane variant: work counted per ray
         launch_trace_kernel<MODE, true, K, 0, kTraceThreads>(P, num_sms, stream);
+        return;
+    }
+    if (c.packet_lists & (MODE == kModeBounce ? RT_TRAVERSAL_PACKET_PRIMARY : RT_TRAVERSAL_PACKET_SHADOW)) {
+        if (c.block_size == 64) launch_packet_kernel<MODE, false, K, 64>(P, num_sms, stream);
+        else if (c.block_size == 256) launch_packet_kernel<MODE, false, K, 256>(P, num_sms, stream);
+        else launch_packet_kernel<MODE, false, K, 128>(P, num_sms, stream);
         return;
     }
 #define RT_TRACE_CASE(B, D)                                                  \
@@ -1311,6 +1584,7 @@ struct BatchLayout {
 
 bool traversal_config_supported(const RtTraversalConfig& c) {
     if (c.leaf_wait > 32) return false;
+    if (c.packet_lists & ~(RT_TRAVERSAL_PACKET_PRIMARY | RT_TRAVERSAL_PACKET_SHADOW)) return false;
 #define RT_TRACE_SUPPORTED(B, D) \
     if (c.block_size == B && c.shared_stack_depth == D) return true;
     RT_FOR_EACH_TRAVERSAL_VARIANT(RT_TRACE_SUPPORTED)

@@ -24,6 +24,24 @@ def test_layouts_match_reference():
     abi.check_layouts()
 
 
+def test_header_constants_match_the_python_binding():
+    """Every integer #define RT_* of the headers (a literal or `(a << b)`)
+    exists in the ctypes binding with the same value."""
+    seen = 0
+    for h in HEADERS:
+        for m in re.finditer(r"^#define\s+(RT_[A-Z0-9_]+)\s+(.+?)\s*(?:/\*.*)?$", h.read_text(), re.M):
+            name, body = m.group(1), m.group(2)
+            lit = re.fullmatch(r"\(?(0x[0-9a-fA-F]+|\d+)u?l{0,2}\)?", body)
+            shl = re.fullmatch(r"\((\d+)u?l{0,2}\s*<<\s*(\d+)\)", body)
+            if not (lit or shl):
+                continue
+            value = int(lit.group(1), 0) if lit else int(shl.group(1)) << int(shl.group(2))
+            assert hasattr(abi, name), f"{h.name}: {name} missing from abi.py"
+            assert getattr(abi, name) == value, (h.name, name, getattr(abi, name), value)
+            seen += 1
+    assert seen >= 60
+
+
 def test_header_static_asserts_compile(tmp_path):
     src = tmp_path / "t.c"
     src.write_text("".join(f'#include "{h.name}"\n' for h in HEADERS) + "int main(void){return 0;}\n")

@@ -199,24 +199,25 @@ def test_every_traversal_config_gives_identical_images(device):
     ref = _images(frames)
     default = abi.RtTraversalConfig()
     device.check(device.lib.rt_ctx_get_traversal_config(device.ctx, C.byref(default)))
-    assert default.as_tuple() == (128, 0, 20)
+    assert default.as_tuple() == (128, 0, 20, abi.RT_TRAVERSAL_PACKET_PRIMARY)
+    # every per-lane launch shape (both lists per lane), then every packet choice on each block size
+    configs = [(block, depth, wait, 0) for block in (64, 128, 256) for depth in (0, 16, 24, 32) for wait in (0, 20, 32)]
+    configs += [(block, 16, 20, pl) for block in (64, 128, 256) for pl in (1, 2, 3)]
     try:
-        for block in (64, 128, 256):
-            for depth in (0, 16, 24, 32):
-                for wait in (0, 20, 32):
-                    c = abi.RtTraversalConfig(block, depth, wait, 0)
-                    device.check(device.lib.rt_ctx_set_traversal_config(device.ctx, C.byref(c)))
-                    for fr, _, _ in frames:
-                        fr.image.zero_()
-                    host.trace_batch(device, batch)
-                    torch.cuda.synchronize()
-                    for k, (fr, _, _) in enumerate(frames):
-                        assert torch.equal(fr.image, ref[k]), (block, depth, wait, k)
+        for cfg in configs:
+            c = abi.RtTraversalConfig(*cfg)
+            device.check(device.lib.rt_ctx_set_traversal_config(device.ctx, C.byref(c)))
+            for fr, _, _ in frames:
+                fr.image.zero_()
+            host.trace_batch(device, batch)
+            torch.cuda.synchronize()
+            for k, (fr, _, _) in enumerate(frames):
+                assert torch.equal(fr.image, ref[k]), (cfg, k)
     finally:
         device.check(device.lib.rt_ctx_set_traversal_config(device.ctx, C.byref(default)))
-    for bad in ((96, 0, 20), (128, 8, 20), (128, 0, 33)):
+    for bad in ((96, 0, 20, 0), (128, 8, 20, 0), (128, 0, 33, 0), (128, 0, 20, 4)):
         with pytest.raises(abi.RtError) as e:
-            device.check(device.lib.rt_ctx_set_traversal_config(device.ctx, C.byref(abi.RtTraversalConfig(*bad, 0))))
+            device.check(device.lib.rt_ctx_set_traversal_config(device.ctx, C.byref(abi.RtTraversalConfig(*bad))))
         assert e.value.status == abi.RT_ERR_UNSUPPORTED
 
 
@@ -238,7 +239,11 @@ def test_autotune_picks_a_built_config(device):
     try:
         device.check(device.lib.rt_ctx_autotune(device.ctx, arr, len(batch), None, 1, host.Device.stream_handle(),
                                                 C.byref(rep)))
-        assert rep.count == 36 and rep.best < rep.count
+        # 36 launch shapes with camera-ray packets, then the other 3 packet choices on the fastest shape
+        assert rep.count == 39 and rep.best < rep.count
+        cfgs = [rep.configs[i].as_tuple() for i in range(rep.count)]
+        assert all(c[3] == abi.RT_TRAVERSAL_PACKET_PRIMARY for c in cfgs[:36])
+        assert sorted(c[3] for c in cfgs[36:]) == [0, 2, 3] and len({c[:3] for c in cfgs[36:]}) == 1
         ms = [rep.median_ms[i] for i in range(rep.count)]
         assert all(m > 0 for m in ms) and ms[rep.best] == min(ms)
         chosen = abi.RtTraversalConfig()
