@@ -79,6 +79,9 @@ def parse_args():
                         "GLB / PNG files at 1280x720 with a TLAS refit per frame; precision: 10,485,760-triangle "
                         "icosphere, 4M random rays, quantised vs FP32 nodes; batch: 64 scenes in one batched "
                         "launch; serve: Poisson request stream over 32 resident scenes")
+    p.add_argument("--traversal", default=None, metavar="B,D,W,P",
+                   help="frame / scene: set this RtTraversalConfig (block_size, shared_stack_depth, leaf_wait, "
+                        "packet_lists) instead of running rt_ctx_autotune on the workload's frame")
     p.add_argument("--batch-scenes", type=int, default=64, help=argparse.SUPPRESS)
     p.add_argument("--serve-seconds", type=float, default=120.0, help="serve: length of the request stream")
     p.add_argument("--serve-rate", type=float, default=400.0, help=argparse.SUPPRESS)
@@ -382,17 +385,24 @@ def bench_ours(args):
 
     # ---- the autotuner picks the traversal configuration on one frame of this workload (a batch of
     # one: the first slot's TLAS and frame 0's uniforms), untimed; the loop then runs with it ----
-    t_tune = time.perf_counter()
-    tune_item = host.batch_scene(loop.slots[0], DEPTH, SHADOWS, uniforms_address=uni_dev[0].data_ptr())
-    tune_arr = (abi.RtBatchScene * 1)(tune_item)
-    report = abi.RtAutotuneReport()
-    dev.check(lib.rt_ctx_autotune(dev.ctx, tune_arr, 1, None, 3, host.Device.stream_handle(stream),
-                                  C.byref(report)))
-    tuned = report.configs[report.best]
-    tune_s = time.perf_counter() - t_tune
-    default_cfg = (128, 0, 20, abi.RT_TRAVERSAL_PACKET_PRIMARY)
-    tune_default_ms = [report.median_ms[i] for i in range(report.count)
-                       if report.configs[i].as_tuple() == default_cfg][0]
+    if args.traversal:
+        tuned = abi.RtTraversalConfig(*(int(v) for v in args.traversal.split(",")))
+        dev.check(lib.rt_ctx_set_traversal_config(dev.ctx, C.byref(tuned)))
+        tune_note = {"chosen_by": "--traversal"}
+    else:
+        t_tune = time.perf_counter()
+        tune_item = host.batch_scene(loop.slots[0], DEPTH, SHADOWS, uniforms_address=uni_dev[0].data_ptr())
+        tune_arr = (abi.RtBatchScene * 1)(tune_item)
+        report = abi.RtAutotuneReport()
+        dev.check(lib.rt_ctx_autotune(dev.ctx, tune_arr, 1, None, 3, host.Device.stream_handle(stream),
+                                      C.byref(report)))
+        tuned = report.configs[report.best]
+        default_cfg = (128, 0, 20, abi.RT_TRAVERSAL_PACKET_PRIMARY)
+        tune_note = {"chosen_by": f"rt_ctx_autotune on frame 0 ({report.count} configs, "
+                                  f"{time.perf_counter() - t_tune:.1f} s, untimed)",
+                     "tuned_ms": report.median_ms[report.best],
+                     "default_config_ms": [report.median_ms[i] for i in range(report.count)
+                                           if report.configs[i].as_tuple() == default_cfg][0]}
     loop.begin()
     for k in range(args.warmup):
         frame(k, instances=frames_dev[k % FRAMES])
@@ -501,10 +511,7 @@ def bench_ours(args):
                        "traversal_config": {"block_size": tuned.block_size,
                                             "shared_stack_depth": tuned.shared_stack_depth,
                                             "leaf_wait": tuned.leaf_wait, "packet_lists": tuned.packet_lists,
-                                            "chosen_by": f"rt_ctx_autotune on frame 0 ({report.count} configs, "
-                                                         f"{tune_s:.1f} s, untimed)",
-                                            "tuned_ms": report.median_ms[report.best],
-                                            "default_config_ms": tune_default_ms},
+                                            **tune_note},
                        "work_counts": "nodes / triangles per ray from a statistics frame of the per-lane "
                                       "traversal (what each ray needs)"},
             "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": n_inst * 64,

@@ -13,17 +13,20 @@
 // triangle test; non-opaque candidates run the alpha-clip any-hit inline.
 // The closest hit is the minimum under (t, instance index, geometry index,
 // primitive index), so the result does not depend on the BVH or visit order.
+// Coherent wavefront lists (camera rays in 8x4 pixel tiles) can instead be
+// traversed as warp packets (k_trace_packet): one node sequence for the
+// union of 32 neighbouring rays, the same hits.
 //
 // Pipeline (replaces cmd_trace_rays, src/command_buffer_recording.rs:116-126,
 // with the programs of src/main.rs:289-305), one frame:
-//   raygen -> [trace closest (bounce b) -> shade (b)] x max_trace_depth
-//          -> trace shadow rays (any hit, terminate on first) -> resolve -> output
-// `shade` runs the closest-hit / miss programs for every ray of bounce b:
-// misses and terminal hits write the pixel's colour; mirror / portal hits
-// append the next bounce ray; textured hits store their BRDF terms and
-// shadow origin and append the pixel to the shadow list.  Appends are
-// block-aggregated (one atomic per list per block), which compacts the
-// wavefronts.
+//   setup -> raygen -> trace closest (every mirror / portal bounce followed
+//   in the traversal) -> shade -> trace shadow rays (any hit, terminate on
+//   first) -> resolve -> output
+// `shade` runs the closest-hit / miss programs for the last ray of every
+// slot: misses and terminal hits write the pixel's colour; textured hits
+// store their BRDF terms and shadow origin and append the pixel's shadow
+// rays.  Appends are warp-aggregated (one atomic per list per warp), which
+// compacts the wavefronts.
 #include <algorithm>
 #include <cstring>
 #include <mutex>
