@@ -397,7 +397,7 @@ def bench_ours(args):
         dev.check(lib.rt_ctx_autotune(dev.ctx, tune_arr, 1, None, 3, host.Device.stream_handle(stream),
                                       C.byref(report)))
         tuned = report.configs[report.best]
-        default_cfg = (128, 0, 20, abi.RT_TRAVERSAL_PACKET_PRIMARY)
+        default_cfg = (128, 0, 20, 0)
         tune_note = {"chosen_by": f"rt_ctx_autotune on frame 0 ({report.count} configs, "
                                   f"{time.perf_counter() - t_tune:.1f} s, untimed)",
                      "tuned_ms": report.median_ms[report.best],
@@ -905,7 +905,7 @@ def bench_batch(args):
     dev.check(lib.rt_ctx_autotune(dev.ctx, arr, len(items), None, 3, sh, C.byref(report)))
     best8 = (report.median_ms[report.best], abi.RtTraversalConfig(*report.configs[report.best].as_tuple()))
     default_ms = [report.median_ms[i] for i in range(report.count)
-                  if report.configs[i].as_tuple() == (128, 0, 20, abi.RT_TRAVERSAL_PACKET_PRIMARY)][0]
+                  if report.configs[i].as_tuple() == (128, 0, 20, 0)][0]
     _, frames4 = batch_setup(dev, args.batch_scenes, width4=True)
     items4 = [host.batch_scene(fr, sc.max_trace_depth, sc.shadow_ray_count) for fr, sc in zip(frames4, scs)]
     arr4 = (abi.RtBatchScene * len(items4))(*items4)

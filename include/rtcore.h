@@ -432,8 +432,11 @@ RTCORE_API int32_t rt_cmd_trace_rays_batched(rt_ctx* ctx, const RtBatchScene* sc
  *                       traverses as one packet of 32 neighbouring rays (one
  *                       node sequence for the union of their box hits, stack
  *                       in shared memory); the other lists run one ray per
- *                       lane with the three fields above
- * Default {128, 0, 20, RT_TRAVERSAL_PACKET_PRIMARY}. */
+ *                       lane with the three fields above.  Packets pay on
+ *                       large coherent frames; for small images a request
+ *                       lasts as long as its slowest tile, so they are
+ *                       opt-in (rt_ctx_autotune tries them)
+ * Default {128, 0, 20, 0}. */
 #define RT_TRAVERSAL_PACKET_PRIMARY 0x1u /* camera rays (8x4 pixel tiles) and their mirror / portal bounces */
 #define RT_TRAVERSAL_PACKET_SHADOW 0x2u  /* the shadow rays of each shaded pixel, appended per shading warp */
 typedef struct RtTraversalConfig {

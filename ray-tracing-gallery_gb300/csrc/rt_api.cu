@@ -111,7 +111,7 @@ struct rt_ctx {
     std::mutex mu;
     std::vector<Workspace> workspaces;
     KernelTimer timer;
-    RtTraversalConfig traversal{128, 0, 20, RT_TRAVERSAL_PACKET_PRIMARY};
+    RtTraversalConfig traversal{128, 0, 20, 0};
     // rt_trace_ray_buffer_host: two streams and their device staging (rays, then hits)
     struct HostQuery {
         std::mutex mu;
@@ -683,13 +683,13 @@ RTCORE_API int32_t rt_ctx_autotune(rt_ctx* ctx, const RtBatchScene* scenes, uint
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     if (stream_capturing(s)) return fail(RT_ERR_INVALID, "rt_ctx_autotune cannot run inside a stream capture");
     reps = std::max(1u, std::min(reps, 64u));
-    // stage 1: the per-lane launch shapes, camera rays in packets; stage 2:
-    // the other packet_lists choices on the fastest shape
+    // stage 1: the per-lane launch shapes (the default among them); stage 2:
+    // the packet_lists choices on the fastest shape
     static const uint32_t kBlocks[] = {64, 128, 256}, kDepths[] = {0, 16, 24, 32}, kWaits[] = {16, 20, 24};
     std::vector<RtTraversalConfig> cands;
     for (uint32_t b : kBlocks)
         for (uint32_t d : kDepths)
-            for (uint32_t w : kWaits) cands.push_back(RtTraversalConfig{b, d, w, RT_TRAVERSAL_PACKET_PRIMARY});
+            for (uint32_t w : kWaits) cands.push_back(RtTraversalConfig{b, d, w, 0});
     const RtTraversalConfig saved = ctx->traversal;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     cudaError_t ce = cudaEventCreate(&e0);
@@ -727,7 +727,8 @@ RTCORE_API int32_t rt_ctx_autotune(rt_ctx* ctx, const RtBatchScene* scenes, uint
     if (r == RT_OK) {
         const RtTraversalConfig shape = cands[fastest()];
         const size_t n1 = cands.size();
-        for (uint32_t pl : {0u, RT_TRAVERSAL_PACKET_SHADOW, RT_TRAVERSAL_PACKET_PRIMARY | RT_TRAVERSAL_PACKET_SHADOW})
+        for (uint32_t pl : {RT_TRAVERSAL_PACKET_PRIMARY, RT_TRAVERSAL_PACKET_SHADOW,
+                            RT_TRAVERSAL_PACKET_PRIMARY | RT_TRAVERSAL_PACKET_SHADOW})
             cands.push_back(RtTraversalConfig{shape.block_size, shape.shared_stack_depth, shape.leaf_wait, pl});
         time_cands(n1);
     }

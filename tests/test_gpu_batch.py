@@ -199,7 +199,7 @@ def test_every_traversal_config_gives_identical_images(device):
     ref = _images(frames)
     default = abi.RtTraversalConfig()
     device.check(device.lib.rt_ctx_get_traversal_config(device.ctx, C.byref(default)))
-    assert default.as_tuple() == (128, 0, 20, abi.RT_TRAVERSAL_PACKET_PRIMARY)
+    assert default.as_tuple() == (128, 0, 20, 0)
     # every per-lane launch shape (both lists per lane), then every packet choice on each block size
     configs = [(block, depth, wait, 0) for block in (64, 128, 256) for depth in (0, 16, 24, 32) for wait in (0, 20, 32)]
     configs += [(block, 16, 20, pl) for block in (64, 128, 256) for pl in (1, 2, 3)]
@@ -239,11 +239,11 @@ def test_autotune_picks_a_built_config(device):
     try:
         device.check(device.lib.rt_ctx_autotune(device.ctx, arr, len(batch), None, 1, host.Device.stream_handle(),
                                                 C.byref(rep)))
-        # 36 launch shapes with camera-ray packets, then the other 3 packet choices on the fastest shape
+        # 36 per-lane launch shapes, then the 3 packet choices on the fastest shape
         assert rep.count == 39 and rep.best < rep.count
         cfgs = [rep.configs[i].as_tuple() for i in range(rep.count)]
-        assert all(c[3] == abi.RT_TRAVERSAL_PACKET_PRIMARY for c in cfgs[:36])
-        assert sorted(c[3] for c in cfgs[36:]) == [0, 2, 3] and len({c[:3] for c in cfgs[36:]}) == 1
+        assert all(c[3] == 0 for c in cfgs[:36]) and (128, 0, 20, 0) in cfgs[:36]
+        assert sorted(c[3] for c in cfgs[36:]) == [1, 2, 3] and len({c[:3] for c in cfgs[36:]}) == 1
         ms = [rep.median_ms[i] for i in range(rep.count)]
         assert all(m > 0 for m in ms) and ms[rep.best] == min(ms)
         chosen = abi.RtTraversalConfig()
