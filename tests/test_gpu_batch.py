@@ -86,6 +86,42 @@ def test_batch_matches_individual_frames(device):
     assert st["traversals"] == want
 
 
+def test_packet_traversal_matches_per_lane(device):
+    """Both ray lists as warp packets over a batch of five scenes (mirrors,
+    a portal, alpha-clipped geometry, 0 to 8 shadow rays; shadow-list
+    chunks that straddle two scenes split into sub-packets): every image and
+    radiance is bit-identical to the per-lane render of the scene alone, and
+    the traversal count is the oracle's."""
+    import ctypes as C
+
+    import torch
+
+    host = _host()
+    frames = _frames(device, _specs())
+    alone = _alone(device, frames)
+    cfg = abi.RtTraversalConfig(128, 0, 20, abi.RT_TRAVERSAL_PACKET_PRIMARY | abi.RT_TRAVERSAL_PACKET_SHADOW)
+    default = abi.RtTraversalConfig()
+    device.check(device.lib.rt_ctx_get_traversal_config(device.ctx, C.byref(default)))
+    try:
+        device.check(device.lib.rt_ctx_set_traversal_config(device.ctx, C.byref(cfg)))
+        for fr, _, _ in frames:
+            fr.image.zero_()
+            fr.radiance.zero_()
+        device.read_stats(reset=True)
+        host.trace_batch(device, [host.batch_scene(fr, d, s) for fr, d, s in frames])
+        torch.cuda.synchronize()
+        st = device.read_stats(reset=True)
+    finally:
+        device.check(device.lib.rt_ctx_set_traversal_config(device.ctx, C.byref(default)))
+    assert st["status"] == 0
+    for k, ((fr, d, s), (img, rad)) in enumerate(zip(frames, alone)):
+        assert torch.equal(fr.image, img), f"scene {k}: packet image differs"
+        assert torch.equal(fr.radiance, rad), f"scene {k}: packet radiance differs"
+    want = sum(O.OracleScene(fr.gpu_scene.scene).render(max_trace_depth=d, shadow_ray_count=s)[2]["traversals"]
+               for fr, d, s in frames)
+    assert st["traversals"] == want
+
+
 def test_batch_scene_matches_oracle(device):
     import torch
 
@@ -197,6 +233,7 @@ def test_every_traversal_config_gives_identical_images(device):
     host.trace_batch(device, batch)
     torch.cuda.synchronize()
     ref = _images(frames)
+    ref_rad = [fr.radiance.clone() for fr, _, _ in frames]
     default = abi.RtTraversalConfig()
     device.check(device.lib.rt_ctx_get_traversal_config(device.ctx, C.byref(default)))
     assert default.as_tuple() == (128, 0, 20, 0)
@@ -209,10 +246,12 @@ def test_every_traversal_config_gives_identical_images(device):
             device.check(device.lib.rt_ctx_set_traversal_config(device.ctx, C.byref(c)))
             for fr, _, _ in frames:
                 fr.image.zero_()
+                fr.radiance.zero_()
             host.trace_batch(device, batch)
             torch.cuda.synchronize()
             for k, (fr, _, _) in enumerate(frames):
                 assert torch.equal(fr.image, ref[k]), (cfg, k)
+                assert torch.equal(fr.radiance, ref_rad[k]), (cfg, k)  # bit-identical radiance: same hits
     finally:
         device.check(device.lib.rt_ctx_set_traversal_config(device.ctx, C.byref(default)))
     for bad in ((96, 0, 20, 0), (128, 8, 20, 0), (128, 0, 33, 0), (128, 0, 20, 4)):
