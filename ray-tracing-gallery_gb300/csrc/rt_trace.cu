@@ -1163,8 +1163,16 @@ __device__ __forceinline__ void trace_packets(const WfParams& P) {
     flush_counters(P.stats, cnt);
 }
 
+// Packets hold the per-lane keys, the reduced keys and the child references
+// at once: the FP32 kernels run at 20 warps per SM (96 registers, 68-byte
+// spills instead of 288 at 80 registers; 1080p frame +0.8 %, 16 warps -1 %).
+// A 256-thread block cannot make 20 warps and keeps 24.
+constexpr int packet_warps_per_sm(uint32_t kinds, int block) {
+    return kinds == kBlasKindQ8 ? 32 : (block == 256 ? 24 : 20);
+}
+
 template <int MODE, bool STATS, uint32_t KINDS, int BLOCK>
-__global__ void __launch_bounds__(BLOCK, trace_warps_per_sm(KINDS) * 32 / BLOCK)
+__global__ void __launch_bounds__(BLOCK, packet_warps_per_sm(KINDS, BLOCK) * 32 / BLOCK)
     k_trace_packet(const __grid_constant__ WfParams P) {
     if (kinds_selected(P.kinds_built, P.B.ctr->kinds, KINDS)) trace_packets<MODE, STATS, KINDS, BLOCK>(P);
 }
