@@ -263,14 +263,16 @@ class GpuScene:
 
     def __init__(self, device: Device, scene: Scene, scratch: ScratchBuffer | None = None,
                  tlas_flags: int = abi.RT_BUILD_PREFER_FAST_TRACE | abi.RT_BUILD_ALLOW_UPDATE, stream=None,
-                 blas_flags: int = abi.RT_BUILD_PREFER_FAST_TRACE, own_textures: bool = False):
+                 blas_flags: int | list[int] = abi.RT_BUILD_PREFER_FAST_TRACE, own_textures: bool = False):
         """own_textures: keep the scene's bindless table in its own device array
         (for batched rendering of scenes with different textures) instead of
-        binding the textures into the context's table."""
+        binding the textures into the context's table.  blas_flags: one value
+        for every model, or one per model (e.g. some quantised, some FP32)."""
         self.device = device
         self.scene = scene
         self.scratch = scratch or ScratchBuffer("scene scratch")
-        self.models = [GpuModel(device, m, self.scratch, i, build_flags=blas_flags, stream=stream)
+        per_model = blas_flags if isinstance(blas_flags, (list, tuple)) else [blas_flags] * len(scene.models)
+        self.models = [GpuModel(device, m, self.scratch, i, build_flags=per_model[i], stream=stream)
                        for i, m in enumerate(scene.models)]
         infos = np.array([m.model_info() for m in self.models], abi.MODEL_INFO_DTYPE)
         self.model_info_buffer = Device.upload(infos)

@@ -98,7 +98,42 @@ def test_quantized_render_matches_oracle(device):
     assert np.abs(img.astype(int) - o_img.astype(int)).max() <= 1
 
 
-@pytest.mark.parametrize("distance", [30.0, 3.0e5])
+@pytest.mark.parametrize("formats", ["quantised", "mixed"])
+def test_quantized_scenes_render_identically_per_lane_and_as_packets(device, formats):
+    """A scene of quantised BLASes (the quantised-only kernels) and one mixing
+    quantised and FP32 BLASes in one TLAS (the kernels decoding both): the
+    per-lane traversal and both lists as warp packets give bit-identical
+    images and radiance, equal to the oracle's within its tolerance."""
+    import torch
+
+    host = _host()
+    sc = scenes.scene_full(0, 96, 54)
+    flags = Q if formats == "quantised" else [Q if i % 2 == 0 else abi.RT_BUILD_PREFER_FAST_TRACE
+                                              for i in range(len(sc.models))]
+    g = host.GpuScene(device, sc, blas_flags=flags)
+    sizes = {m.blas.info(device).node_bytes for m in g.models}
+    assert sizes == ({96} if formats == "quantised" else {96, 256})
+    out = []
+    default = abi.RtTraversalConfig()
+    device.check(device.lib.rt_ctx_get_traversal_config(device.ctx, C.byref(default)))
+    try:
+        for packets in (0, abi.RT_TRAVERSAL_PACKET_PRIMARY | abi.RT_TRAVERSAL_PACKET_SHADOW):
+            cfg = abi.RtTraversalConfig(128, 0, 20, packets)
+            device.check(device.lib.rt_ctx_set_traversal_config(device.ctx, C.byref(cfg)))
+            img, rad, st = host.render(device, sc, radiance=True, gpu_scene=g)
+            assert st["status"] == 0
+            out.append((img, rad, st["traversals"]))
+    finally:
+        device.check(device.lib.rt_ctx_set_traversal_config(device.ctx, C.byref(default)))
+    (img0, rad0, n0), (img1, rad1, n1) = out
+    assert np.array_equal(img0, img1) and np.array_equal(rad0.view(np.uint32), rad1.view(np.uint32)) and n0 == n1
+    o_img, o_rad, o_st = O.OracleScene(sc).render()
+    assert n0 == o_st["traversals"]
+    assert np.abs(rad0 - o_rad).max() <= 1e-3
+    torch.cuda.synchronize()
+
+
+@pytest.mark.parametrize("distance",[30.0, 3.0e5])
 def test_quantized_mesh_near_and_far_rays(device, distance):
     """655,360 triangles; rays from 30 units use the fast plane decode, rays
     from 3e5 units the exact one (the origin is over 2^19 grid steps away)."""
