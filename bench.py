@@ -396,13 +396,37 @@ def bench_ours(args):
         report = abi.RtAutotuneReport()
         dev.check(lib.rt_ctx_autotune(dev.ctx, tune_arr, 1, None, 3, host.Device.stream_handle(stream),
                                       C.byref(report)))
-        tuned = report.configs[report.best]
+        best = report.configs[report.best].as_tuple()
         default_cfg = (128, 0, 20, 0)
         tune_note = {"chosen_by": f"rt_ctx_autotune on frame 0 ({report.count} configs, "
-                                  f"{time.perf_counter() - t_tune:.1f} s, untimed)",
+                                  f"{time.perf_counter() - t_tune:.1f} s, untimed), then 10 untimed frames "
+                                  "of this loop for its pick and its launch shape with packet_lists 0 / 1 / 5",
                      "tuned_ms": report.median_ms[report.best],
                      "default_config_ms": [report.median_ms[i] for i in range(report.count)
                                            if report.configs[i].as_tuple() == default_cfg][0]}
+        # the tuner times one warm frame; the loop rebuilds / refits and flushes L2 every frame, so
+        # the pick is confirmed on 10 frames of the loop itself
+        cands = list(dict.fromkeys([best] + [best[:3] + (pl,) for pl in
+                                             (0, abi.RT_TRAVERSAL_PACKET_PRIMARY,
+                                              abi.RT_TRAVERSAL_PACKET_PRIMARY | abi.RT_TRAVERSAL_PACKET_LANE_BOUNCES)]))
+        loop_ms = {}
+        for cfg in cands:
+            dev.check(lib.rt_ctx_set_traversal_config(dev.ctx, C.byref(abi.RtTraversalConfig(*cfg))))
+            for rep in range(2):  # the first pass warms the configuration's kernels
+                torch.cuda.synchronize()
+                ea, eb = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                ea.record(stream)
+                loop.begin()
+                for k in range(10):
+                    frame(k, instances=frames_dev[k % FRAMES])
+                loop.end()
+                eb.record(stream)
+                torch.cuda.synchronize()
+            loop_ms[cfg] = ea.elapsed_time(eb) / 10
+        pick = min(loop_ms, key=loop_ms.get)
+        tuned = abi.RtTraversalConfig(*pick)
+        dev.check(lib.rt_ctx_set_traversal_config(dev.ctx, C.byref(tuned)))
+        tune_note["loop_ms_per_frame"] = {",".join(map(str, k)): v for k, v in loop_ms.items()}
     loop.begin()
     for k in range(args.warmup):
         frame(k, instances=frames_dev[k % FRAMES])

@@ -439,6 +439,10 @@ RTCORE_API int32_t rt_cmd_trace_rays_batched(rt_ctx* ctx, const RtBatchScene* sc
  * Default {128, 0, 20, 0}. */
 #define RT_TRAVERSAL_PACKET_PRIMARY 0x1u /* camera rays (8x4 pixel tiles) and their mirror / portal bounces */
 #define RT_TRAVERSAL_PACKET_SHADOW 0x2u  /* the shadow rays of each shaded pixel, appended per shading warp */
+/* with PACKET_PRIMARY: the mirror / portal continuation rays of a packet are
+ * traced one per lane inside the packet launch instead of as further
+ * sub-packets (pays when many pixels see curved mirrors) */
+#define RT_TRAVERSAL_PACKET_LANE_BOUNCES 0x4u
 typedef struct RtTraversalConfig {
     uint32_t block_size;
     uint32_t shared_stack_depth;

@@ -217,6 +217,7 @@ RT_MAX_BATCH_SCENES = 65536
 
 RT_TRAVERSAL_PACKET_PRIMARY = 0x1
 RT_TRAVERSAL_PACKET_SHADOW = 0x2
+RT_TRAVERSAL_PACKET_LANE_BOUNCES = 0x4
 
 
 class RtTraversalConfig(C.Structure):

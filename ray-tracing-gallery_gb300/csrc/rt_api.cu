@@ -727,8 +727,9 @@ RTCORE_API int32_t rt_ctx_autotune(rt_ctx* ctx, const RtBatchScene* scenes, uint
     if (r == RT_OK) {
         const RtTraversalConfig shape = cands[fastest()];
         const size_t n1 = cands.size();
-        for (uint32_t pl : {RT_TRAVERSAL_PACKET_PRIMARY, RT_TRAVERSAL_PACKET_SHADOW,
-                            RT_TRAVERSAL_PACKET_PRIMARY | RT_TRAVERSAL_PACKET_SHADOW})
+        const uint32_t P1 = RT_TRAVERSAL_PACKET_PRIMARY, P2 = RT_TRAVERSAL_PACKET_SHADOW,
+                       LB = RT_TRAVERSAL_PACKET_LANE_BOUNCES;
+        for (uint32_t pl : {P1, P2, P1 | P2, P1 | LB, P1 | P2 | LB})
             cands.push_back(RtTraversalConfig{shape.block_size, shape.shared_stack_depth, shape.leaf_wait, pl});
         time_cands(n1);
     }

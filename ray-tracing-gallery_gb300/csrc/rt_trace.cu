@@ -1067,7 +1067,9 @@ __device__ __forceinline__ void packet_traverse(Trav& s, uint2* ws, const unsign
     }
 }
 
-template <int MODE, bool STATS, uint32_t KINDS, int BLOCK>
+// LANE_BOUNCES: mirror / portal continuations traced one per lane inside the
+// launch (RT_TRAVERSAL_PACKET_LANE_BOUNCES), else as further sub-packets.
+template <int MODE, bool STATS, uint32_t KINDS, int BLOCK, bool LANE_BOUNCES>
 __device__ __forceinline__ void trace_packets(const WfParams& P) {
     __shared__ uint2 stacks[BLOCK / 32][kStackSize];
     uint2* ws = stacks[threadIdx.x >> 5];
@@ -1127,9 +1129,26 @@ __device__ __forceinline__ void trace_packets(const WfParams& P) {
             bool cont = false;
             if ((act >> lane) & 1u) {
                 packet_traverse<STATS, KINDS>(s, ws, act, sv, &P.sbt, P.status, ray_flags, sbt_offset, cnt);
-                // a mirror / portal hit with depth left: the lane's next ray joins
-                // the chunk's next sub-packet (the closest-hit program's arithmetic)
-                if (MODE == kModeBounce && s.hit_inst != kNoHit && depth + 1 < P.B.scenes[s.scene].max_depth) {
+                if (MODE == kModeBounce && LANE_BOUNCES) {
+                    // every further bounce of the lane's ray, traced by the lane
+                    // alone (the closest-hit program's arithmetic, bit for bit)
+                    TravStack<0, BLOCK> stk;
+                    while (s.hit_inst != kNoHit && depth + 1 < P.B.scenes[s.scene].max_depth) {
+                        const NextRay nr = next_bounce_ray(P.B.scenes[s.scene].env, &P.sbt, s.hit_inst, s.hit_geom,
+                                                           s.hit_prim, s.t, s.u, s.v, s.wo, s.wd);
+                        if (nr.d.x == 0.0f && nr.d.y == 0.0f && nr.d.z == 0.0f) break;
+                        trav_begin(s, sv(s.scene), nr.o, nr.d, 0.01f, 10000.0f);
+                        depth++;
+                        atomicAdd(reinterpret_cast<unsigned long long*>(&P.stats->traversals), 1ull);
+                        atomicAdd(reinterpret_cast<unsigned long long*>(&P.stats->secondary_rays), 1ull);
+                        while (!trav_step<STATS, KINDS>(s, stk, sv, &P.sbt, P.status, ray_flags, 0xFFu, sbt_offset,
+                                                        cnt, -1)) {
+                        }
+                    }
+                } else if (MODE == kModeBounce && s.hit_inst != kNoHit &&
+                           depth + 1 < P.B.scenes[s.scene].max_depth) {
+                    // a mirror / portal hit with depth left: the lane's next ray
+                    // joins the chunk's next sub-packet
                     const NextRay nr = next_bounce_ray(P.B.scenes[s.scene].env, &P.sbt, s.hit_inst, s.hit_geom,
                                                        s.hit_prim, s.t, s.u, s.v, s.wo, s.wd);
                     if (nr.d.x != 0.0f || nr.d.y != 0.0f || nr.d.z != 0.0f) {
@@ -1171,10 +1190,11 @@ constexpr int packet_warps_per_sm(uint32_t kinds, int block) {
     return kinds == kBlasKindQ8 ? 32 : (block == 256 ? 24 : 20);
 }
 
-template <int MODE, bool STATS, uint32_t KINDS, int BLOCK>
+template <int MODE, bool STATS, uint32_t KINDS, int BLOCK, bool LANE_BOUNCES>
 __global__ void __launch_bounds__(BLOCK, packet_warps_per_sm(KINDS, BLOCK) * 32 / BLOCK)
     k_trace_packet(const __grid_constant__ WfParams P) {
-    if (kinds_selected(P.kinds_built, P.B.ctr->kinds, KINDS)) trace_packets<MODE, STATS, KINDS, BLOCK>(P);
+    if (kinds_selected(P.kinds_built, P.B.ctr->kinds, KINDS))
+        trace_packets<MODE, STATS, KINDS, BLOCK, LANE_BOUNCES>(P);
 }
 
 // The closest-hit and miss programs for the last ray of every slot of bounce
@@ -1485,9 +1505,9 @@ void launch_trace_kernel(const WfParams& P, int num_sms, cudaStream_t stream) {
     note_launch(), kern<<<blocks, BLOCK, smem, stream>>>(P);
 }
 
-template <int MODE, bool STATS, uint32_t KINDS, int BLOCK>
+template <int MODE, bool STATS, uint32_t KINDS, int BLOCK, bool LANE_BOUNCES = false>
 void launch_packet_kernel(const WfParams& P, int num_sms, cudaStream_t stream) {
-    const auto kern = k_trace_packet<MODE, STATS, KINDS, BLOCK>;
+    const auto kern = k_trace_packet<MODE, STATS, KINDS, BLOCK, LANE_BOUNCES>;
     static int blocks = 0;
     if (!blocks) blocks = persistent_blocks(kern, BLOCK, num_sms);
     note_launch(), kern<<<blocks, BLOCK, 0, stream>>>(P);
@@ -1507,9 +1527,21 @@ void launch_trace_config(const WfParams& P, const RtTraversalConfig& c, bool sta
         return;
     }
     if (c.packet_lists & (MODE == kModeBounce ? RT_TRAVERSAL_PACKET_PRIMARY : RT_TRAVERSAL_PACKET_SHADOW)) {
-        if (c.block_size == 64) launch_packet_kernel<MODE, false, K, 64>(P, num_sms, stream);
-        else if (c.block_size == 256) launch_packet_kernel<MODE, false, K, 256>(P, num_sms, stream);
-        else launch_packet_kernel<MODE, false, K, 128>(P, num_sms, stream);
+        if constexpr (MODE == kModeBounce) {
+            if (c.packet_lists & RT_TRAVERSAL_PACKET_LANE_BOUNCES) {
+                if (c.block_size == 64) launch_packet_kernel<MODE, false, K, 64, true>(P, num_sms, stream);
+                else if (c.block_size == 256) launch_packet_kernel<MODE, false, K, 256, true>(P, num_sms, stream);
+                else launch_packet_kernel<MODE, false, K, 128, true>(P, num_sms, stream);
+                return;
+            }
+        }
+        if (c.block_size == 64) {
+            launch_packet_kernel<MODE, false, K, 64>(P, num_sms, stream);
+        } else if (c.block_size == 256) {
+            launch_packet_kernel<MODE, false, K, 256>(P, num_sms, stream);
+        } else {
+            launch_packet_kernel<MODE, false, K, 128>(P, num_sms, stream);
+        }
         return;
     }
 #define RT_TRACE_CASE(B, D)                                                  \
@@ -1595,7 +1627,9 @@ struct BatchLayout {
 
 bool traversal_config_supported(const RtTraversalConfig& c) {
     if (c.leaf_wait > 32) return false;
-    if (c.packet_lists & ~(RT_TRAVERSAL_PACKET_PRIMARY | RT_TRAVERSAL_PACKET_SHADOW)) return false;
+    if (c.packet_lists &
+        ~(RT_TRAVERSAL_PACKET_PRIMARY | RT_TRAVERSAL_PACKET_SHADOW | RT_TRAVERSAL_PACKET_LANE_BOUNCES))
+        return false;
 #define RT_TRACE_SUPPORTED(B, D) \
     if (c.block_size == B && c.shared_stack_depth == D) return true;
     RT_FOR_EACH_TRAVERSAL_VARIANT(RT_TRACE_SUPPORTED)

@@ -86,12 +86,14 @@ def test_batch_matches_individual_frames(device):
     assert st["traversals"] == want
 
 
-def test_packet_traversal_matches_per_lane(device):
+@pytest.mark.parametrize("lane_bounces", [False, True])
+def test_packet_traversal_matches_per_lane(device, lane_bounces):
     """Both ray lists as warp packets over a batch of five scenes (mirrors,
     a portal, alpha-clipped geometry, 0 to 8 shadow rays; shadow-list
-    chunks that straddle two scenes split into sub-packets): every image and
-    radiance is bit-identical to the per-lane render of the scene alone, and
-    the traversal count is the oracle's."""
+    chunks that straddle two scenes split into sub-packets; mirror / portal
+    continuations as sub-packets or one per lane): every image and radiance
+    is bit-identical to the per-lane render of the scene alone, and the
+    traversal count is the oracle's."""
     import ctypes as C
 
     import torch
@@ -99,7 +101,8 @@ def test_packet_traversal_matches_per_lane(device):
     host = _host()
     frames = _frames(device, _specs())
     alone = _alone(device, frames)
-    cfg = abi.RtTraversalConfig(128, 0, 20, abi.RT_TRAVERSAL_PACKET_PRIMARY | abi.RT_TRAVERSAL_PACKET_SHADOW)
+    pl = abi.RT_TRAVERSAL_PACKET_PRIMARY | abi.RT_TRAVERSAL_PACKET_SHADOW
+    cfg = abi.RtTraversalConfig(128, 0, 20, pl | (abi.RT_TRAVERSAL_PACKET_LANE_BOUNCES if lane_bounces else 0))
     default = abi.RtTraversalConfig()
     device.check(device.lib.rt_ctx_get_traversal_config(device.ctx, C.byref(default)))
     try:
@@ -239,7 +242,7 @@ def test_every_traversal_config_gives_identical_images(device):
     assert default.as_tuple() == (128, 0, 20, 0)
     # every per-lane launch shape (both lists per lane), then every packet choice on each block size
     configs = [(block, depth, wait, 0) for block in (64, 128, 256) for depth in (0, 16, 24, 32) for wait in (0, 20, 32)]
-    configs += [(block, 16, 20, pl) for block in (64, 128, 256) for pl in (1, 2, 3)]
+    configs += [(block, 16, 20, pl) for block in (64, 128, 256) for pl in (1, 2, 3, 5, 7)]
     try:
         for cfg in configs:
             c = abi.RtTraversalConfig(*cfg)
@@ -254,7 +257,7 @@ def test_every_traversal_config_gives_identical_images(device):
                 assert torch.equal(fr.radiance, ref_rad[k]), (cfg, k)  # bit-identical radiance: same hits
     finally:
         device.check(device.lib.rt_ctx_set_traversal_config(device.ctx, C.byref(default)))
-    for bad in ((96, 0, 20, 0), (128, 8, 20, 0), (128, 0, 33, 0), (128, 0, 20, 4)):
+    for bad in ((96, 0, 20, 0), (128, 8, 20, 0), (128, 0, 33, 0), (128, 0, 20, 8)):
         with pytest.raises(abi.RtError) as e:
             device.check(device.lib.rt_ctx_set_traversal_config(device.ctx, C.byref(abi.RtTraversalConfig(*bad))))
         assert e.value.status == abi.RT_ERR_UNSUPPORTED
@@ -278,11 +281,11 @@ def test_autotune_picks_a_built_config(device):
     try:
         device.check(device.lib.rt_ctx_autotune(device.ctx, arr, len(batch), None, 1, host.Device.stream_handle(),
                                                 C.byref(rep)))
-        # 36 per-lane launch shapes, then the 3 packet choices on the fastest shape
-        assert rep.count == 39 and rep.best < rep.count
+        # 36 per-lane launch shapes, then the 5 packet choices on the fastest shape
+        assert rep.count == 41 and rep.best < rep.count
         cfgs = [rep.configs[i].as_tuple() for i in range(rep.count)]
         assert all(c[3] == 0 for c in cfgs[:36]) and (128, 0, 20, 0) in cfgs[:36]
-        assert sorted(c[3] for c in cfgs[36:]) == [1, 2, 3] and len({c[:3] for c in cfgs[36:]}) == 1
+        assert sorted(c[3] for c in cfgs[36:]) == [1, 2, 3, 5, 7] and len({c[:3] for c in cfgs[36:]}) == 1
         ms = [rep.median_ms[i] for i in range(rep.count)]
         assert all(m > 0 for m in ms) and ms[rep.best] == min(ms)
         chosen = abi.RtTraversalConfig()
