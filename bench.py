@@ -137,7 +137,7 @@ class DefaultSceneFrames:
                    "soft shadows (radius 0.05), TLAS refitted in place every frame")
     path = "plain FP32 8-wide BVH, TLAS refit"
     depth, shadows, refit = 3, 2, True
-    profile = None
+    profile = "k_trace_default_scene_720p.md"
     data = "synthetic stand-in asset files (GLB / PNG written from seeds), decoded by librtcore"
 
     def __init__(self, width: int, height: int):
