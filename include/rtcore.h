@@ -423,7 +423,8 @@ RTCORE_API int32_t rt_cmd_trace_rays_batched(rt_ctx* ctx, const RtBatchScene* sc
  * rt_cmd_trace_rays_batched).  Every configuration gives identical results;
  * they differ only in speed.  No counterpart in the reference (the driver
  * schedules its own traversal).
- *   block_size          threads per block: 64, 128 or 256 (24 warps per SM each)
+ *   block_size          threads per block: 64, 128 or 256 (24 warps per SM each;
+ *                       packet kernels 20 for 64 / 128)
  *   shared_stack_depth  traversal-stack entries kept in shared memory: 0, 16,
  *                       24 or 32 (the rest of the 64 live in local memory)
  *   leaf_wait           0..32: a warp runs leaf steps once leaf_wait/32 of its
@@ -459,10 +460,11 @@ typedef struct RtAutotuneReport {
     RtTraversalConfig configs[RT_AUTOTUNE_MAX_CONFIGS];
     float median_ms[RT_AUTOTUNE_MAX_CONFIGS];        /* of `reps` batched launches each */
 } RtAutotuneReport;
-/* Times rt_cmd_trace_rays_batched(scenes) under every traversal
- * configuration (block size x shared stack depth x leaf_wait in {16, 20,
- * 24}), `reps` timed launches each after one warm-up, and makes the fastest
- * the context's configuration.  Synchronises `stream`; not allowed while it
+/* Times rt_cmd_trace_rays_batched(scenes) under the traversal configurations
+ * and makes the fastest the context's configuration: first the 36 per-lane
+ * launch shapes (block size x shared stack depth x leaf_wait in {16, 20,
+ * 24}), then packet_lists 1, 2, 3, 5 and 7 on the fastest shape (41 in all),
+ * `reps` timed launches each after one warm-up.  Synchronises `stream`; not allowed while it
  * is being captured.  The scenes' output buffers are overwritten.  `report`
  * may be NULL. */
 RTCORE_API int32_t rt_ctx_autotune(rt_ctx* ctx, const RtBatchScene* scenes, uint32_t scene_count,
