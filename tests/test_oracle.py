@@ -1,5 +1,5 @@
 """CPU tests of the oracle: the reference's own known-answer test, published
-vectors, and properties the oracle must have before it can judge the GPU."""
+vectors, and properties the oracle must have before it can check the GPU."""
 import json
 import math
 from pathlib import Path
