@@ -1,30 +1,34 @@
 """Benchmark of the ray-tracing hot path on one GB300 (or N replicas).
 
-Workload (one step = one frame): the full plain feature set at 1920x1080 —
-256 instances of {torus, displaced UV sphere, alpha-clipped fence} with
-per-frame random rigid transforms (60 precomputed frames), a TLAS rebuild
-from that frame's instance records, then the reference's pipeline
-(raygen, textured / mirror / portal closest-hits, alpha-clip any-hit, misses)
-with 4 blue-noise soft-shadow rays per textured hit and 1 reflection bounce.
+Default workload (--workload batch; one step = 64 scenes): 64 independent
+procedural scenes (unique triangles log-uniform in [10k, 2M], resolutions
+from 128^2 to 1920x1080, primary + 2 blue-noise soft shadows + 1 reflection
+bounce).  `value` is the quantised + batched path: BLASes with 8-bit
+quantised child boxes, all 64 scenes in one batched launch sequence replayed
+from a CUDA graph, launch shape and node width chosen by rt_ctx_autotune.
+Beside it stands the plain FP32 path (FP32 child boxes, one rt_cmd_trace_rays
+per scene, the default launch shape) and their ratio; every image of the two
+paths and the hits of a camera-ray sample are compared bit for bit; the
+radiance error against the FP32 and FP64 oracles is reported per image; then
+the serving stream (Poisson arrivals over 32 resident scenes) gives its
+p50 / p99 / p99.9 latencies.
 
 Metric: Mrays/s = traversals (primary + shadow + reflection, each traceRay
-counted once) / time.  Frames run as the reference runs them, two in flight
-(host.FrameLoop: each with its own instance buffer, TLAS, uniforms, image and
-stream).  `value` times all K frames as one span of CUDA events (start on the
-launching stream, both frame streams joined at the end) with the frames'
-instance records already resident and the L2 flushed before every frame by a
-256 MiB write on its stream (inside the span); `e2e` times the same loop
-through the C ABI with host buffers: each frame's instance records copied in
-from pinned host memory and its RGBA8 image written by the output kernel into
-pinned host memory (through the buffer's mapping), inside the span.
-Per-kernel times and the roofline come from serial frames outside the span.
---workload scene runs the same loop on the reference's default scene built
-from GLB / PNG files (DefaultSceneFrames: 1280x720, TLAS refit per frame).
-Other workloads: --workload precision / batch / serve (see their functions).
+counted once) / time, time from CUDA events on the launching stream with the
+L2 flushed (a 256 MiB write) before every step, outside the events.  `e2e`
+runs the same graph through the C ABI with host buffers: the uniforms come
+in from pinned host memory and every image is written into pinned host
+memory, inside the timed span.
+
+Other workloads: --workload frame (the full plain feature set at 1920x1080:
+256 instances, TLAS rebuild per frame, two frames in flight), scene (the
+reference's default scene from GLB / PNG files, 1280x720, TLAS refit per
+frame), precision (10,485,760 triangles, 4M random rays, quantised vs FP32
+nodes) and serve (the request stream alone, batched and plain in full).
 
 --impl reference runs the CPU oracle (the restatement of the reference's
 shader logic; the reference itself needs a Vulkan ray-tracing driver, which
-does not exist on this machine) over bounded bands of the same frames.
+does not exist on this machine) over bounded samples of the same work.
 """
 from __future__ import annotations
 
@@ -74,16 +78,20 @@ def parse_args():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--width", type=int, default=None, help="frame: 1920, scene: 1280")
     p.add_argument("--height", type=int, default=None, help="frame: 1080, scene: 720")
-    p.add_argument("--workload", default="frame", choices=["frame", "scene", "precision", "batch", "serve"],
-                   help="frame: the full 1080p frame (default); scene: the reference's default scene from "
-                        "GLB / PNG files at 1280x720 with a TLAS refit per frame; precision: 10,485,760-triangle "
-                        "icosphere, 4M random rays, quantised vs FP32 nodes; batch: 64 scenes in one batched "
-                        "launch; serve: Poisson request stream over 32 resident scenes")
+    p.add_argument("--workload", default="batch", choices=["batch", "frame", "scene", "precision", "serve"],
+                   help="batch (default): 64 scenes, the quantised + batched path against the plain FP32 path, "
+                        "then the serving stream's latency percentiles; frame: the full 1080p frame; scene: the "
+                        "reference's default scene from GLB / PNG files at 1280x720 with a TLAS refit per frame; "
+                        "precision: 10,485,760-triangle icosphere, 4M random rays, quantised vs FP32 nodes; "
+                        "serve: the Poisson request stream over 32 resident scenes alone")
     p.add_argument("--traversal", default=None, metavar="B,D,W,P",
                    help="frame / scene: set this RtTraversalConfig (block_size, shared_stack_depth, leaf_wait, "
                         "packet_lists) instead of running rt_ctx_autotune on the workload's frame")
     p.add_argument("--batch-scenes", type=int, default=64, help=argparse.SUPPRESS)
-    p.add_argument("--serve-seconds", type=float, default=120.0, help="serve: length of the request stream")
+    p.add_argument("--serve-seconds", type=float, default=120.0,
+                   help="batch / serve: length of the request stream (0: batch skips the stream)")
+    p.add_argument("--serve-plain-seconds", type=float, default=30.0,
+                   help="batch: the plain per-request server replays the stream's first this many seconds")
     p.add_argument("--serve-rate", type=float, default=400.0, help=argparse.SUPPRESS)
     p.add_argument("--serve-scenes", type=int, default=32, help=argparse.SUPPRESS)
     p.add_argument("--serve-budget-gb", type=float, default=150.0, help=argparse.SUPPRESS)
@@ -191,19 +199,37 @@ def reduce_over_ranks(dist, total_ms: float, rays: float, device: str = "cuda") 
     return float(t.item()), float(r.item())
 
 
+def profiled_figures(name: str) -> dict:
+    """Figures of the committed ncu summary profiles/<name>: the lines
+    `dram_bytes_per_launch: N` (DRAM read + write bytes of one launch of the
+    kernel, used as roofline.traffic), `dram_frac: F` (DRAM throughput as a
+    fraction of peak) and `l2_pct: P` (L2 throughput, % of peak)."""
+    p = ROOT / "profiles" / name
+    out = {}
+    if not p.exists():
+        return out
+    for line in p.read_text().splitlines():
+        key, _, rest = line.strip().partition(":")
+        if key in ("dram_bytes_per_launch", "dram_frac", "l2_pct") and rest.strip():
+            try:
+                out[key] = float(rest.strip().split()[0])
+            except ValueError:
+                pass
+    return out
+
+
 def profiled_traffic(name: str = "k_trace_full_1080p.md"):
     """DRAM bytes per traversal launch from the committed ncu summary of this
     workload (profiles/<name>, line `dram_bytes_per_launch: N`)."""
-    p = ROOT / "profiles" / name
-    if not p.exists():
-        return None
-    for line in p.read_text().splitlines():
-        if line.strip().startswith("dram_bytes_per_launch:"):
-            try:
-                return float(line.split(":", 1)[1].strip().split()[0])
-            except ValueError:
-                return None
-    return None
+    return profiled_figures(name).get("dram_bytes_per_launch")
+
+
+_T0 = time.perf_counter()
+
+
+def note(msg: str) -> None:
+    """Progress on stderr (the JSON line alone goes to stdout)."""
+    print(f"[bench {time.perf_counter() - _T0:7.1f} s] {msg}", file=sys.stderr, flush=True)
 
 
 def measured_peaks() -> tuple[float, str]:
@@ -785,60 +811,118 @@ def bench_precision(args):
         dist.destroy_process_group()
 
 
+BATCH_METRIC = "Mrays/s quantized+batched vs plain FP32 (exact hit IDs); serve p50/p99 ms"
 BATCH_WORKLOAD = ("batch: 64 independent scenes (procedural torus + displaced UV sphere + ground grid, unique "
                   "triangles log-uniform in [10k, 2M], resolutions from {128^2, 256^2, 512^2, 1024^2, 1920x1080}), "
                   "primary + 2 blue-noise soft shadows + 1 reflection bounce each, one batched launch sequence "
                   "replayed from a CUDA graph")
 
 
-def batch_setup(dev, count, width4: bool = False):
+def batch_setup(dev, scs, quantized: bool = False, width4: bool = False, radiance: bool = False):
+    """GPU scenes and frames of the batch: BLASes with FP32 boxes or 8-bit
+    quantised child boxes, 8 or at most 4 children per node."""
     from rtgallery import host
 
     w = abi.RT_BUILD_EXT_NODE_WIDTH_4 if width4 else 0
-    scs = scenes.batch_scenes(count)
+    q = abi.RT_BUILD_QUANTIZED_NODES if quantized else 0
     frames = []
     for sc in scs:
-        gs = host.GpuScene(dev, sc, own_textures=True, blas_flags=abi.RT_BUILD_PREFER_FAST_TRACE | w,
+        gs = host.GpuScene(dev, sc, own_textures=True, blas_flags=abi.RT_BUILD_PREFER_FAST_TRACE | q | w,
                            tlas_flags=abi.RT_BUILD_PREFER_FAST_TRACE | abi.RT_BUILD_ALLOW_UPDATE | w)
-        fr = host.PerFrameResources(dev, gs, sc.width, sc.height)
+        fr = host.PerFrameResources(dev, gs, sc.width, sc.height, radiance=radiance)
         fr.write_uniforms(sc.uniforms)
         frames.append(fr)
-    return scs, frames
+    return frames
 
 
-def batch_cpu(scs, budget_s: float = 12.0) -> dict:
-    """The oracle (FP32, all host threads) rendering row bands of the batch's
-    scenes in turn until about `budget_s` seconds of CPU work."""
+def build_oracles(scs, threads: int | None = None):
+    """One oracle per scene, built on a thread pool (the oracle's BVH build
+    runs in C with the interpreter lock released)."""
+    from concurrent.futures import ThreadPoolExecutor
+
     from oracle.oracle import OracleScene, default_threads
+
+    with ThreadPoolExecutor(max_workers=threads or default_threads()) as ex:
+        return list(ex.map(OracleScene, scs))
+
+
+def batch_cpu(scs, oracles, budget_s: float = 12.0) -> dict:
+    """The oracle (FP32, all host threads) rendering row bands of the batch's
+    scenes in turn until about `budget_s` seconds of CPU work (the oracles'
+    BVH builds are not timed)."""
+    from oracle.oracle import default_threads
 
     threads = default_threads()
     rays, t_total, done = 0, 0.0, 0
-    for sc in scs:
-        o = OracleScene(sc)
+    for k in range(len(scs) * 16):
+        sc, o = scs[k % len(scs)], oracles[k % len(scs)]
         band = max(4, sc.height // 16)
+        y0 = ((k // len(scs)) * band) % max(1, sc.height - band)
         t = time.perf_counter()
-        _, _, st = o.render(rows=(0, band), threads=threads)
+        _, _, st = o.render(rows=(y0, y0 + band), threads=threads)
         t_total += time.perf_counter() - t
         rays += st["traversals"]
         done += 1
         if t_total >= budget_s:
             break
     return {"value": rays / t_total / 1e6, "unit": "Mrays/s", "cores": threads, "kind": "port",
-            "sample": f"first 1/16 of the rows of {done} of the {len(scs)} scenes ({rays} traversals, {t_total:.1f} s)"}
+            "sample": f"{done} row bands of 1/16 of a scene's rows, the 64 scenes in turn ({rays} traversals, "
+                      f"{t_total:.1f} s)"}
+
+
+def radiance_error_bands(scs, oracles, radiance_host) -> dict:
+    """Per image: max-abs linear radiance error of the GPU against the FP32
+    oracle (the <= 1e-3 tolerance) and against the FP64 oracle (reported), on
+    the central 1/16 of its rows."""
+    from oracle.oracle import default_threads
+
+    err32, err64 = [], []
+    for sc, o, rad in zip(scs, oracles, radiance_host):
+        band = max(4, sc.height // 16)
+        y0 = (sc.height - band) // 2
+        _, r32, _ = o.render(rows=(y0, y0 + band), threads=default_threads())
+        _, r64, _ = o.render(rows=(y0, y0 + band), double=True, threads=default_threads())
+        g = rad[y0:y0 + band, :, :3]
+        err32.append(float(np.abs(g - r32[y0:y0 + band, :, :3]).max()))
+        err64.append(float(np.abs(g - r64[y0:y0 + band, :, :3]).max()))
+    return {"rows": "central 1/16 of each image's rows", "tolerance_vs_fp32_oracle": 1e-3,
+            "max_abs_vs_fp32_oracle": max(err32), "max_abs_vs_fp64_oracle": max(err64),
+            "per_image_max_abs_vs_fp64_oracle": err64, "per_image_max_abs_vs_fp32_oracle": err32}
+
+
+def camera_ray_sample(sc, step: int) -> np.ndarray:
+    """The camera rays (ray_generation's formula, in float32) of every
+    `step`-th pixel in x and y of scene `sc`."""
+    u = sc.uniforms
+    vi = np.array(u.view_inverse, np.float32).reshape(4, 4).T  # column-major -> [row, col]
+    pi = np.array(u.proj_inverse, np.float32).reshape(4, 4).T
+    ys, xs = np.mgrid[0:sc.height:step, 0:sc.width:step]
+    xs, ys = xs.ravel().astype(np.float32), ys.ravel().astype(np.float32)
+    ndc = np.stack([(xs + 0.5) / sc.width * 2 - 1, (ys + 0.5) / sc.height * 2 - 1,
+                    np.ones_like(xs), np.ones_like(xs)], 1).astype(np.float32)
+    tgt = (ndc @ pi.T)[:, :3]
+    loc = tgt / np.linalg.norm(tgt, axis=1, keepdims=True)
+    d = loc @ vi[:3, :3].T
+    rays = np.zeros(len(xs), abi.RAY_DTYPE)
+    rays["origin"] = vi[:3, 3]
+    rays["direction"] = d.astype(np.float32)
+    rays["tmin"] = 0.01
+    rays["tmax"] = 10000.0
+    return rays
 
 
 def bench_batch_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    from oracle.oracle import OracleScene, default_threads
+    from oracle.oracle import default_threads
 
     threads = default_threads()
     scs = scenes.batch_scenes(args.batch_scenes)
+    oracles = build_oracles(scs)
     times, rays = [], 0
     for k in range(args.warmup + args.steps):
-        sc = scs[k % len(scs)]
-        o = OracleScene(sc)
+        sc, o = scs[k % len(scs)], oracles[k % len(scs)]
         band = max(4, sc.height // 32)
         y0 = (k * band) % max(1, sc.height - band)
         t = time.perf_counter()
@@ -850,18 +934,23 @@ def bench_batch_reference(args):
     total = sum(times)
     value = rays / total / 1e6
     print(json.dumps({
-        "impl": "reference", "metric": "Mrays/s", "value": value, "unit": "Mrays/s", "n_gpus": world,
+        "impl": "reference", "metric": BATCH_METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": BATCH_WORKLOAD, "sample": "a 1/32 row band of one scene per step"},
+        "config": {"workload": BATCH_WORKLOAD, "sample": "a 1/32 row band of one scene per step",
+                   "path": "the reference's shader logic on the host (oracle port), FP32, one scene at a time"},
         "cpu_baseline": {"value": value, "unit": "Mrays/s", "cores": threads, "kind": "port",
                          "sample": f"1/32 row band of one scene per step, {args.steps} steps"},
         "e2e": {"value": value, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
 
 
 def bench_batch(args):
-    """64 scenes per step: per-scene launches vs one batched launch sequence,
-    direct and replayed from a CUDA graph."""
+    """The headline: 64 scenes rendered by the quantised + batched path (8-bit
+    child boxes, one batched launch sequence replayed from a CUDA graph, the
+    launch shape and node width from rt_ctx_autotune) against the plain FP32
+    path (FP32 boxes, one rt_cmd_trace_rays per scene, the library's default
+    launch shape), with every image and a sample of hits compared between the
+    two; then the serving stream's latency percentiles."""
     import torch
 
     rank, world, local = dist_env()
@@ -875,23 +964,32 @@ def bench_batch(args):
 
     dev = host.Device()
     lib = dev.lib
+    scs = scenes.batch_scenes(args.batch_scenes)
     t0 = time.perf_counter()
-    scs, frames = batch_setup(dev, args.batch_scenes)
+    fr32 = batch_setup(dev, scs)
+    frq8 = batch_setup(dev, scs, quantized=True)
     torch.cuda.synchronize()
     setup_s = time.perf_counter() - t0
+    note(f"batch: 64 scenes built twice (FP32, quantised) in {setup_s:.1f} s")
     stream = torch.cuda.Stream()
     sh = host.Device.stream_handle(stream)
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
-    items = [host.batch_scene(fr, sc.max_trace_depth, sc.shadow_ray_count) for fr, sc in zip(frames, scs)]
-    arr = (abi.RtBatchScene * len(items))(*items)
-    singles = [(abi.RtBatchScene * 1)(it) for it in items]
+    default_cfg = abi.RtTraversalConfig(128, 0, 20, 0)
 
-    def batched(flags=0):
-        dev.check(lib.rt_cmd_trace_rays_batched(dev.ctx, arr, len(items), None, flags, sh))
+    def items_of(frames, **kw):
+        its = [host.batch_scene(fr, sc.max_trace_depth, sc.shadow_ray_count, **kw) for fr, sc in zip(frames, scs)]
+        return (abi.RtBatchScene * len(its))(*its)
 
-    def per_scene():
-        for one in singles:
-            dev.check(lib.rt_cmd_trace_rays_batched(dev.ctx, one, 1, None, 0, sh))
+    arr32, arrq8 = items_of(fr32), items_of(frq8)
+
+    def batched(arr, flags=0):
+        dev.check(lib.rt_cmd_trace_rays_batched(dev.ctx, arr, len(scs), None, flags, sh))
+
+    def plain():
+        # the drop-in: one rt_cmd_trace_rays per scene (PerFrameResources::record), FP32 nodes
+        for fr, sc in zip(fr32, scs):
+            fr.gpu_scene.bind_textures()
+            fr.record(sc.max_trace_depth, sc.shadow_ray_count, stream=stream)
 
     def timed(fn, steps):
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
@@ -904,63 +1002,81 @@ def bench_batch(args):
         torch.cuda.synchronize()
         return sum(a.elapsed_time(b) for a, b in ev)
 
+    def set_cfg(cfg):
+        dev.check(lib.rt_ctx_set_traversal_config(dev.ctx, C.byref(cfg)))
+
+    def autotune(arr):
+        rep = abi.RtAutotuneReport()
+        dev.check(lib.rt_ctx_autotune(dev.ctx, arr, len(scs), None, 3, sh, C.byref(rep)))
+        return rep.median_ms[rep.best], abi.RtTraversalConfig(*rep.configs[rep.best].as_tuple()), rep
+
+    set_cfg(default_cfg)
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
-            per_scene()
-            batched()
+            plain()
+            batched(arr32)
+            batched(arrq8)
     torch.cuda.synchronize()
     dev.read_stats(reset=True)
     with torch.cuda.stream(stream):
-        batched()
+        batched(arrq8)
     torch.cuda.synchronize()
     rays_per_step = dev.read_stats(reset=True)["traversals"]
 
-    # untuned: per-scene launches and one batched launch, the default traversal configuration
+    # ---- the plain FP32 path: per-scene calls, default launch shape ----
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
-    ms_single = timed(per_scene, args.steps)
-    ms_batch = timed(batched, args.steps)
+    ms_plain = timed(plain, args.steps)
+    note(f"plain FP32 per-scene: {ms_plain / args.steps:.2f} ms per step")
+    plain_images = [fr.image.clone() for fr in fr32]
 
-    # the autotuner picks the traversal launch shape on this batch, for 8-wide and for 4-wide BVHs of
-    # the same scenes (rebuilt); the graph is captured with the fastest width and launch shape
-    report = abi.RtAutotuneReport()
+    # ---- the autotuner: launch shape for the FP32 batch (decomposition only), and launch shape x node
+    # width {8, 4} for the quantised batch; the graph is captured with the quantised winner ----
     t_tune = time.perf_counter()
-    dev.check(lib.rt_ctx_autotune(dev.ctx, arr, len(items), None, 3, sh, C.byref(report)))
-    best8 = (report.median_ms[report.best], abi.RtTraversalConfig(*report.configs[report.best].as_tuple()))
-    default_ms = [report.median_ms[i] for i in range(report.count)
-                  if report.configs[i].as_tuple() == (128, 0, 20, 0)][0]
-    _, frames4 = batch_setup(dev, args.batch_scenes, width4=True)
-    items4 = [host.batch_scene(fr, sc.max_trace_depth, sc.shadow_ray_count) for fr, sc in zip(frames4, scs)]
-    arr4 = (abi.RtBatchScene * len(items4))(*items4)
+    best32 = autotune(arr32)
+    best_q8 = autotune(arrq8)
+    frq4 = batch_setup(dev, scs, quantized=True, width4=True)
+    arrq4 = items_of(frq4)
     with torch.cuda.stream(stream):
-        dev.check(lib.rt_cmd_trace_rays_batched(dev.ctx, arr4, len(items4), None, 0, sh))  # sizes, warm-up
+        batched(arrq4)  # sizes the workspace outside the tuner
     torch.cuda.synchronize()
-    report4 = abi.RtAutotuneReport()
-    dev.check(lib.rt_ctx_autotune(dev.ctx, arr4, len(items4), None, 3, sh, C.byref(report4)))
-    best4 = (report4.median_ms[report4.best], abi.RtTraversalConfig(*report4.configs[report4.best].as_tuple()))
+    best_q4 = autotune(arrq4)
     tune_s = time.perf_counter() - t_tune
-    width = 4 if best4[0] < best8[0] else 8
-    tuned = best4[1] if width == 4 else best8[1]
-    dev.check(lib.rt_ctx_set_traversal_config(dev.ctx, C.byref(tuned)))
-    if width == 4:
-        arr, frames = arr4, frames4  # the same scenes and images, 4-wide BVHs
-    else:
-        del frames4
+    width = 4 if best_q4[0] < best_q8[0] else 8
+    tuned = best_q4[1] if width == 4 else best_q8[1]
+    frq, arrq = (frq4, arrq4) if width == 4 else (frq8, arrq8)
+    note(f"autotune {tune_s:.1f} s: quantised width {width} {tuned.as_tuple()}, "
+         f"best ms q8 {best_q8[0]:.2f} q4 {best_q4[0]:.2f} fp32 {best32[0]:.2f}")
+
+    # FP32 batched (the batching gain alone), its own tuned launch shape
+    set_cfg(best32[1])
+    g32 = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g32, stream=stream):
+        batched(arr32)
+    for _ in range(args.warmup):
+        g32.replay()
+    torch.cuda.synchronize()
+    ms_batch32 = timed(g32.replay, args.steps)
+    del g32
+
+    # ---- the quantised + batched path (value) ----
+    set_cfg(tuned)
     graph = torch.cuda.CUDAGraph()
     with torch.cuda.graph(graph, stream=stream):
-        batched()
+        batched(arrq)
     for _ in range(args.warmup):
         graph.replay()
     torch.cuda.synchronize()
-
     clocks = ClockSampler(local)
     clocks.start()
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
     l0 = lib.rt_kernel_launch_count()
-    batched()
+    with torch.cuda.stream(stream):
+        batched(arrq)
+    torch.cuda.synchronize()
     launches_per_step = lib.rt_kernel_launch_count() - l0
     ms_graph = timed(graph.replay, args.steps)
     torch.cuda.synchronize()
@@ -969,101 +1085,152 @@ def bench_batch(args):
     clk = clocks.stop()
     ms_graph, _ = reduce_over_ranks(dist, ms_graph, 0.0)
     value = rays_per_step * world * args.steps / (ms_graph / 1e3) / 1e6
+    plain_value = rays_per_step * args.steps / (ms_plain / 1e3) / 1e6
+    batch32_value = rays_per_step * args.steps / (ms_batch32 / 1e3) / 1e6
+    note(f"quantised+batched {value:.0f} Mrays/s, plain FP32 {plain_value:.0f}, batched FP32 {batch32_value:.0f}")
 
-    # kernel split and roofline of the traversal (a direct call with per-kernel events)
+    # ---- exact hits: every image of the quantised batch equals the plain path's, byte for byte, and
+    # the camera rays of every 4th pixel (each axis) hit the same (t, u, v, instance, geometry,
+    # primitive, facing) through FP32 and quantised structures ----
+    images_identical = all(torch.equal(a, fr.image) for a, fr in zip(plain_images, frq))
+    hit_rays, hits_identical = 0, True
+    for gs32, gsq, sc in zip([f.gpu_scene for f in fr32], [f.gpu_scene for f in frq], scs):
+        rays = camera_ray_sample(sc, 4)
+        a = host.trace_ray_buffer(dev, gs32, rays)
+        b = host.trace_ray_buffer(dev, gsq, rays)
+        hit_rays += len(rays)
+        hits_identical = hits_identical and bool(np.array_equal(a.view(np.uint8), b.view(np.uint8)))
+
+    # ---- kernel split and roofline of the traversal (a direct call with per-kernel events; work counts
+    # from a statistics run of the per-lane traversal) ----
     with torch.cuda.stream(stream):
-        batched(abi.RT_TRACE_FLAG_KERNEL_TIMINGS)
+        batched(arrq, abi.RT_TRACE_FLAG_KERNEL_TIMINGS)
     tt = abi.RtTraceTimings()
     dev.check(lib.rt_ctx_read_trace_timings(dev.ctx, C.byref(tt)))
     kt = tt.as_dict()
     torch.cuda.synchronize()
     dev.read_stats(reset=True)
     with torch.cuda.stream(stream):
-        batched(abi.RT_TRACE_FLAG_COLLECT_STATS)
+        batched(arrq, abi.RT_TRACE_FLAG_COLLECT_STATS)
     torch.cuda.synchronize()
     s = dev.read_stats(reset=True)
-    bytes_step = (s["traversals"] * (RAY_BYTES + HIT_BYTES) + s["nodes_visited"] * NODE_BYTES +
-                  s["triangles_tested"] * TRI_BYTES + s["instances_visited"] * INST_BYTES)
+    fp32_nodes = s["nodes_visited"] - s["quantized_nodes_visited"]
+    bytes_step = (s["traversals"] * (RAY_BYTES + HIT_BYTES) + fp32_nodes * NODE_BYTES +
+                  s["quantized_nodes_visited"] * QNODE_BYTES + s["triangles_tested"] * TRI_BYTES +
+                  s["instances_visited"] * INST_BYTES)
     achieved = bytes_step / (kt["trace_ms"] / 1e3) / 1e9
+    note(f"hits identical {hits_identical}, images identical {images_identical}; traversal {kt['trace_ms']:.2f} ms")
     peak, peak_kind = measured_peaks()
+    prof = profiled_figures("k_trace_batch_quantized.md")
 
-    # end to end: every scene's uniforms in from pinned host memory, every image out to pinned host memory.
-    # "direct": one copy of all uniform blocks into one device array, and a graph whose output kernel writes
-    # each image straight into its pinned host buffer (mapped host memory); "staged": one copy per uniform
-    # block into each frame's buffer, the device-image graph, then one copy per image back
-    uni_host = torch.from_numpy(np.concatenate([np.frombuffer(bytes(sc.uniforms), np.uint8) for sc in scs])).pin_memory()
-    img_host = [torch.empty_like(fr.image, device="cpu").pin_memory() for fr in frames]
+    # ---- end to end: every scene's uniforms in from pinned host memory (one copy into one device array),
+    # every image written into its pinned host buffer by the output kernel, inside the timed span ----
+    uni_host = torch.from_numpy(np.concatenate([np.frombuffer(bytes(sc.uniforms), np.uint8)
+                                                for sc in scs])).pin_memory()
+    img_host = [torch.empty_like(fr.image, device="cpu").pin_memory() for fr in frq]
     usz = C.sizeof(abi.RtUniforms)
     uni_dev = torch.empty_like(uni_host, device="cuda")
-    items_e2e = [host.batch_scene(fr, sc.max_trace_depth, sc.shadow_ray_count,
-                                  uniforms_address=uni_dev.data_ptr() + k * usz,
-                                  image_address=img_host[k].data_ptr())
-                 for k, (fr, sc) in enumerate(zip(frames, scs))]
-    arr_e2e = (abi.RtBatchScene * len(items_e2e))(*items_e2e)
+    arr_e2e = (abi.RtBatchScene * len(scs))(*[
+        host.batch_scene(fr, sc.max_trace_depth, sc.shadow_ray_count, uniforms_address=uni_dev.data_ptr() + k * usz,
+                         image_address=img_host[k].data_ptr()) for k, (fr, sc) in enumerate(zip(frq, scs))])
     uni_dev.copy_(uni_host)
     graph_e2e = torch.cuda.CUDAGraph()
     with torch.cuda.graph(graph_e2e, stream=stream):
-        dev.check(lib.rt_cmd_trace_rays_batched(dev.ctx, arr_e2e, len(items_e2e), None, 0, sh))
+        dev.check(lib.rt_cmd_trace_rays_batched(dev.ctx, arr_e2e, len(scs), None, 0, sh))
     for _ in range(args.warmup):
         graph_e2e.replay()
     torch.cuda.synchronize()
 
-    def e2e_direct():
+    def e2e_step():
         uni_dev.copy_(uni_host, non_blocking=True)
         graph_e2e.replay()
 
-    def e2e_staged():
-        for k, fr in enumerate(frames):
-            fr.uniforms_buffer.copy_(uni_host[k * usz:(k + 1) * usz], non_blocking=True)
-        graph.replay()
-        for k, fr in enumerate(frames):
-            img_host[k].copy_(fr.image, non_blocking=True)
-
-    e2e_ms_staged = timed(e2e_staged, args.steps)
-    staged_images = [t.clone() for t in img_host]
-    e2e_ms = timed(e2e_direct, args.steps)
-    for a, b in zip(img_host, staged_images):
-        if not torch.equal(a, b):
-            raise RuntimeError("batch e2e: the directly written images differ from the copied ones")
+    e2e_ms = timed(e2e_step, args.steps)
+    e2e_images_ok = all(torch.equal(a, b.cpu()) for a, b in zip(img_host, plain_images))
     e2e_value = rays_per_step * world * args.steps / (e2e_ms / 1e3) / 1e6
-    e2e_staged_value = rays_per_step * world * args.steps / (e2e_ms_staged / 1e3) / 1e6
-    cpu = batch_cpu(scs) if rank == 0 and not args.no_cpu_baseline else None
+    del graph, graph_e2e
+
+    # ---- radiance against the FP32 and FP64 oracles, and the timed CPU baseline ----
+    err = cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        rad = [torch.zeros((sc.height, sc.width, 4), dtype=torch.float32, device="cuda") for sc in scs]
+        arr_rad = (abi.RtBatchScene * len(scs))(*[
+            host.batch_scene(fr, sc.max_trace_depth, sc.shadow_ray_count) for fr, sc in zip(frq, scs)])
+        for k in range(len(scs)):
+            arr_rad[k].desc.radiance_address = rad[k].data_ptr()
+        with torch.cuda.stream(stream):
+            batched(arr_rad)
+        torch.cuda.synchronize()
+        rad_host = [r.cpu().numpy() for r in rad]
+        del rad
+        oracles = build_oracles(scs)
+        err = radiance_error_bands(scs, oracles, rad_host)
+        cpu = batch_cpu(scs, oracles)
+        del oracles
+    pixels = sum(sc.width * sc.height for sc in scs)
+    unique_tris = int(sum(m.triangle_count for sc in scs for m in sc.models))
+    del fr32, frq8, frq4, frq, arr32, arrq8, arrq4, arrq
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+
+    note("batch part done; serving stream next")
+    serve = serve_measure(args, plain_seconds=args.serve_plain_seconds) if args.serve_seconds > 0 else None
     if rank == 0:
-        pixels = sum(sc.width * sc.height for sc in scs)
+        cfg = {"workload": BATCH_WORKLOAD, "scenes": len(scs), "pixels_per_step": pixels,
+               "unique_triangles": unique_tris, "traversals_per_step": rays_per_step,
+               "parallelism": f"replicas x{world}",
+               "l2": "flushed before every step (256 MiB write on the stream, outside the timed events)",
+               "path": "quantised + batched: BLASes with 8-bit child boxes, one batched launch sequence for the "
+                       "64 scenes replayed from a CUDA graph, launch shape and node width from rt_ctx_autotune",
+               "plain_fp32_path": "FP32 child boxes, one rt_cmd_trace_rays per scene, default launch shape "
+                                  "(128, 0, 20, 0)",
+               "plain_fp32_mrays_s": plain_value,
+               "speedup_over_plain_fp32": value / plain_value,
+               "batched_fp32_mrays_s": batch32_value,
+               "hits_identical": hits_identical and images_identical,
+               "images_identical_to_plain": images_identical,
+               "hit_sample": f"{hit_rays} camera rays (every 4th pixel in x and y of all 64 scenes) traced through "
+                             f"FP32 and quantised structures: t, u, v, instance, geometry, primitive and facing "
+                             f"bit-identical = {hits_identical}",
+               "radiance": err,
+               "autotuned_config": {"node_width": width, "block_size": tuned.block_size,
+                                    "shared_stack_depth": tuned.shared_stack_depth,
+                                    "leaf_wait": tuned.leaf_wait, "packet_lists": tuned.packet_lists},
+               "autotune_configs": int(best_q8[2].count + best_q4[2].count + best32[2].count),
+               "autotune_s": tune_s,
+               "autotune_best_ms": {"quantized_width8": best_q8[0], "quantized_width4": best_q4[0],
+                                    "fp32_width8": best32[0]},
+               "kernel_launches_per_step": launches_per_step, "scene_setup_s": setup_s,
+               "trace_ms_per_step": kt["trace_ms"], "shade_ms_per_step": kt["shade_ms"],
+               "pipeline_ms_per_step": kt["total_ms"]}
+        if serve is not None:
+            cfg["serve"] = serve
         print(json.dumps({
-            "metric": "Mrays/s", "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
+            "metric": BATCH_METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_graph / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (procedural scenes from seeds)",
-            "config": {"workload": BATCH_WORKLOAD, "scenes": len(scs), "pixels_per_step": pixels,
-                       "unique_triangles": int(sum(m.triangle_count for sc in scs for m in sc.models)),
-                       "traversals_per_step": rays_per_step, "parallelism": f"replicas x{world}",
-                       "l2": "flushed between steps (256 MiB write outside the timed events)",
-                       "per_scene_launches_mrays_s": rays_per_step * args.steps / (ms_single / 1e3) / 1e6,
-                       "batched_direct_mrays_s": rays_per_step * args.steps / (ms_batch / 1e3) / 1e6,
-                       "batched_graph_mrays_s": value,
-                       "autotuned_config": {"node_width": width, "block_size": tuned.block_size,
-                                            "shared_stack_depth": tuned.shared_stack_depth,
-                                            "leaf_wait": tuned.leaf_wait, "packet_lists": tuned.packet_lists},
-                       "autotune_configs": int(report.count + report4.count), "autotune_s": tune_s,
-                       "autotune_best_ms_width8": best8[0], "autotune_best_ms_width4": best4[0],
-                       "autotune_best_config_width8": best8[1].as_tuple(),
-                       "autotune_best_config_width4": best4[1].as_tuple(),
-                       "autotune_default_config_ms": default_ms,
-                       "speedup_graph_batch_over_per_scene": ms_single / ms_graph,
-                       "kernel_launches_per_step": launches_per_step, "scene_setup_s": setup_s,
-                       "trace_ms_per_step": kt["trace_ms"], "shade_ms_per_step": kt["shade_ms"],
-                       "pipeline_ms_per_step": kt["total_ms"]},
+            "config": cfg,
             "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": usz * len(scs),
                     "d2h_bytes_per_step": pixels * 4,
-                    "path": "one uniform copy in, images written into pinned host buffers by the output kernel",
-                    "staged_copies_mrays_s": e2e_staged_value},
+                    "path": "rt_cmd_trace_rays_batched in a CUDA graph: one copy of the 64 uniform blocks in from "
+                            "pinned host memory, every RGBA8 image written into its pinned host buffer by the "
+                            "output kernel",
+                    "images_identical_to_plain": e2e_images_ok},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                         "traffic": None, "kernel": "k_trace (all traversal launches of the batch)",
+                         "traffic": prof.get("dram_bytes_per_launch"),
+                         "kernel": "k_trace (every traversal launch of the quantised batch)",
+                         "achieved_is": "algorithmic bytes per step (rays, hits, 96-byte quantised BLAS nodes, "
+                                        "256-byte TLAS nodes, triangles, instance records, counted by a statistics "
+                                        "run) / traversal time per step; most of them are L2 hits",
                          "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
                          else "fallback 6.8 TB/s",
                          "algorithmic_bytes_per_step": bytes_step,
                          "bytes_per_ray": bytes_step / max(1, s["traversals"]),
-                         "nodes_per_ray": s["nodes_visited"] / max(1, s["traversals"])},
+                         "nodes_per_ray": s["nodes_visited"] / max(1, s["traversals"]),
+                         "quantized_nodes_per_ray": s["quantized_nodes_visited"] / max(1, s["traversals"]),
+                         "dram_frac_of_peak_from_profile": prof.get("dram_frac"),
+                         "l2_throughput_pct_from_profile": prof.get("l2_pct"),
+                         "profile": "profiles/k_trace_batch_quantized.md" if prof else None},
             "cpu_baseline": cpu,
             "clocks": clk,
             "gpu_launches": int(launches_per_step) * args.steps,
@@ -1078,6 +1245,13 @@ SERVE_WORKLOAD = ("serve: Poisson request stream (seeded) over 32 device-residen
                   "light, resolution from {256^2, 512^2, 1024^2, 1280x720, 1920x1080}, 1-8 soft-shadow rays and "
                   "1 reflection bounce; admission by an HBM budget for BVHs + textures + frame buffers; "
                   "continuous batching vs the plain one-request-per-launch path on the same stream")
+
+
+SERVE_MAX_BATCH, SERVE_IN_FLIGHT = 32, 2
+# batch limits of the batched server (ray slots, shadow rays), and of the plain server (one request of the
+# largest size: 1920x1080 with 8 shadow rays)
+SERVE_BATCH_SLOTS, SERVE_BATCH_SHADOW = 4 << 20, 16 << 20
+SERVE_REQUEST_SLOTS, SERVE_REQUEST_SHADOW = 1920 * 1080, 1920 * 1080 * 8
 
 
 def serve_requests(args, n_scenes):
@@ -1097,12 +1271,17 @@ def serve_requests(args, n_scenes):
 
 def run_stream(dev, gscenes, reqs, budget, max_batch, in_flight, ring):
     """Replays `reqs` at their arrival times against a fresh server; returns
-    (latencies ms, queue ms, batch sizes, wall s, traversals, server stats)."""
+    (latencies ms, queue ms, batch sizes, wall s, traversals, server stats).
+    Batches stay within SERVE_BATCH_SLOTS ray slots and SERVE_BATCH_SHADOW
+    shadow rays (a larger request alone), and the server sizes its workspace
+    and frame-buffer pool for that at creation."""
     import torch
 
     from rtgallery import host
 
-    srv = host.Server(dev, budget, max_batch_requests=max_batch, max_in_flight=in_flight)
+    srv = host.Server(dev, budget, max_batch_requests=max_batch, max_in_flight=in_flight,
+                      max_batch_pixels=SERVE_BATCH_SLOTS if max_batch > 1 else SERVE_REQUEST_SLOTS,
+                      max_batch_shadow_rays=SERVE_BATCH_SHADOW if max_batch > 1 else SERVE_REQUEST_SHADOW)
     ids = [srv.add_scene(g) for g in gscenes]
     tickets = [None] * len(reqs)
     results = [None] * len(reqs)
@@ -1140,6 +1319,22 @@ def run_stream(dev, gscenes, reqs, budget, max_batch, in_flight, ring):
     return lat, qms, bs, wall, rays, st
 
 
+def run_alone(dev, gscenes, reqs, budget, ring) -> np.ndarray:
+    """Each request of `reqs` submitted only after the previous one finished
+    (nothing else on the GPU): its service time alone, in ms."""
+    from rtgallery import host
+
+    srv = host.Server(dev, budget, max_batch_requests=1, max_in_flight=1, max_batch_pixels=SERVE_REQUEST_SLOTS,
+                      max_batch_shadow_rays=SERVE_REQUEST_SHADOW)
+    ids = [srv.add_scene(g) for g in gscenes]
+    out = []
+    for i, (t, sc, w, h, shadows, u) in enumerate(reqs):
+        tk = srv.submit(ids[sc], u, w, h, 2, shadows, image_host=ring[i % len(ring)].data_ptr())
+        out.append(srv.wait(tk, 600000).latency_ms)
+    srv.close()
+    return np.array(out)
+
+
 def bench_serve_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -1175,11 +1370,14 @@ def bench_serve_reference(args):
         "e2e": {"value": value, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
 
 
-def bench_serve(args):
+def serve_measure(args, plain_seconds: float | None = None) -> dict:
+    """The serving stream (args.serve_seconds of seeded Poisson arrivals at
+    args.serve_rate per second over 32 resident scenes) through the batched
+    server, then through the plain one-request-per-launch server over its
+    first `plain_seconds` (None = all of it), then a 2000-request burst
+    through both (capacity).  Returns the figures of the JSON line."""
     import torch
 
-    rank, world, local = dist_env()
-    torch.cuda.set_device(local)
     from rtgallery import host
 
     dev = host.Device(threadsafe=True)
@@ -1192,28 +1390,71 @@ def bench_serve(args):
     budget = int(args.serve_budget_gb * (1 << 30))
     max_px = max(w * h for w, h in scenes.SERVE_RESOLUTIONS)
     ring = [torch.empty(max_px * 4, dtype=torch.uint8).pin_memory() for _ in range(256)]
-    # warm-up: a short stream so kernels, pools and the workspace exist
+    # warm-up: a short stream so kernels, pools and the workspaces exist
     warm = [(0.0005 * i, *r[1:]) for i, r in enumerate(reqs[:64])]
-    run_stream(dev, gscenes, warm, budget, 32, 2, ring)
-    clocks = ClockSampler(local)
+    run_stream(dev, gscenes, warm, budget, SERVE_MAX_BATCH, SERVE_IN_FLIGHT, ring)
+    clocks = ClockSampler(torch.cuda.current_device())
     clocks.start()
-    lat, qms, bs, wall, rays, st = run_stream(dev, gscenes, reqs, budget, 32, 2, ring)
+    lat, qms, bs, wall, rays, st = run_stream(dev, gscenes, reqs, budget, SERVE_MAX_BATCH, SERVE_IN_FLIGHT, ring)
     clk = clocks.stop()
-    p_lat, p_q, p_bs, p_wall, p_rays, p_st = run_stream(dev, gscenes, reqs, budget, 1, 1, ring)
+    preqs = reqs if plain_seconds is None else [r for r in reqs if r[0] < plain_seconds]
+    p_lat, p_q, p_bs, p_wall, p_rays, p_st = run_stream(dev, gscenes, preqs, budget, 1, 1, ring)
     # capacity: the first 2000 requests all arriving at once, batched and plain
     burst = [(0.0, *r[1:]) for r in reqs[:2000]]
-    _, _, c_bs, c_wall, c_rays, _ = run_stream(dev, gscenes, burst, budget, 32, 2, ring)
+    _, _, c_bs, c_wall, c_rays, _ = run_stream(dev, gscenes, burst, budget, SERVE_MAX_BATCH, SERVE_IN_FLIGHT, ring)
     _, _, _, cp_wall, cp_rays, _ = run_stream(dev, gscenes, burst, budget, 1, 1, ring)
+    # the service time of each of the first 1000 requests alone; slowdown = latency in the stream / alone
+    alone = run_alone(dev, gscenes, reqs[:1000], budget, ring)
+    slow = lat[:len(alone)] / alone
 
     def pct(a, q):
         return float(np.percentile(a, q))
 
-    value = rays / wall / 1e6
+    out = {"workload": SERVE_WORKLOAD, "requests": len(reqs), "rate_per_s": args.serve_rate,
+           "stream_s": args.serve_seconds, "scenes": len(scs),
+           "unique_triangles": int(sum(m.triangle_count for sc in scs for m in sc.models)),
+           "hbm_budget_bytes": budget, "peak_bytes": st["peak_bytes"], "resident_bytes": st["resident_bytes"],
+           "scene_setup_s": setup_s,
+           "p50_ms": pct(lat, 50), "p99_ms": pct(lat, 99), "p999_ms": pct(lat, 99.9),
+           "p99_over_p50": pct(lat, 99) / pct(lat, 50),
+           "alone_first_1000": {"p50_ms": pct(alone, 50), "p99_ms": pct(alone, 99),
+                                "p99_over_p50": pct(alone, 99) / pct(alone, 50),
+                                "note": "each of the stream's first 1000 requests rendered with nothing else on "
+                                        "the GPU: the spread of the requests' own service times"},
+           "slowdown_first_1000": {"p50": pct(slow, 50), "p99": pct(slow, 99), "max": float(slow.max()),
+                                   "note": "latency in the batched stream / the same request's time alone"},
+           "batched": {"p50_ms": pct(lat, 50), "p99_ms": pct(lat, 99), "p999_ms": pct(lat, 99.9),
+                       "queue_p50_ms": pct(qms, 50), "mean_batch": float(bs.mean()), "batches": st["batches"],
+                       "mrays_s": rays / wall / 1e6, "wall_s": wall, "rejected": st["rejected"]},
+           "plain_per_request": {"p50_ms": pct(p_lat, 50), "p99_ms": pct(p_lat, 99), "p999_ms": pct(p_lat, 99.9),
+                                 "mrays_s": p_rays / p_wall / 1e6, "wall_s": p_wall, "requests": len(preqs),
+                                 "rejected": p_st["rejected"]},
+           "capacity_burst_2000": {"batched_mrays_s": c_rays / c_wall / 1e6, "plain_mrays_s": cp_rays / cp_wall / 1e6,
+                                   "batched_req_s": len(burst) / c_wall, "plain_req_s": len(burst) / cp_wall,
+                                   "mean_batch": float(c_bs.mean())},
+           "max_batch_requests": SERVE_MAX_BATCH, "max_in_flight": SERVE_IN_FLIGHT, "clocks": clk,
+           "traversals": rays, "wall_s": wall, "batches": int(st["batches"]),
+           "mean_d2h_bytes": float(np.mean([w * h * 4 for _, _, w, h, _, _ in reqs]))}
+    del gscenes
+    dev.close()
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+    return out
+
+
+def bench_serve(args):
+    import torch
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    sv = serve_measure(args)
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         from oracle.oracle import OracleScene, default_threads
 
         threads = default_threads()
+        scs = [scenes.scene_serve_member(i) for i in range(args.serve_scenes)]
+        reqs = serve_requests(args, len(scs))
         # requests of the four smallest scenes, one oracle BVH each (its build is untimed)
         small = sorted(range(len(scs)), key=lambda i: sum(m.triangle_count for m in scs[i].models))[:4]
         oracles = {i: OracleScene(scs[i]) for i in small}
@@ -1233,35 +1474,20 @@ def bench_serve(args):
                "sample": f"1/64 row bands of the first {k} requests on the 4 smallest scenes "
                          f"({r_cpu} traversals, {t_cpu:.1f} s)"}
     if rank == 0:
+        value = sv["batched"]["mrays_s"]
         print(json.dumps({
-            "metric": "Mrays/s", "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": len(reqs),
-            "warmup": 64, "ms_per_step": 1e3 * wall / len(reqs), "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic (procedural scenes and request stream from seeds)",
-            "config": {"workload": SERVE_WORKLOAD, "requests": len(reqs), "rate_per_s": args.serve_rate,
-                       "stream_s": args.serve_seconds, "scenes": len(scs),
-                       "unique_triangles": int(sum(m.triangle_count for sc in scs for m in sc.models)),
-                       "hbm_budget_bytes": budget, "peak_bytes": st["peak_bytes"], "resident_bytes": st["resident_bytes"],
-                       "scene_setup_s": setup_s,
-                       "batched": {"p50_ms": pct(lat, 50), "p99_ms": pct(lat, 99), "p999_ms": pct(lat, 99.9),
-                                   "queue_p50_ms": pct(qms, 50), "mean_batch": float(bs.mean()),
-                                   "batches": st["batches"], "mrays_s": value, "wall_s": wall,
-                                   "rejected": st["rejected"]},
-                       "plain_per_request": {"p50_ms": pct(p_lat, 50), "p99_ms": pct(p_lat, 99),
-                                             "p999_ms": pct(p_lat, 99.9), "mrays_s": p_rays / p_wall / 1e6,
-                                             "wall_s": p_wall, "rejected": p_st["rejected"]},
-                       "capacity_burst_2000": {"batched_mrays_s": c_rays / c_wall / 1e6,
-                                               "plain_mrays_s": cp_rays / cp_wall / 1e6,
-                                               "batched_req_s": len(burst) / c_wall, "plain_req_s": len(burst) / cp_wall,
-                                               "mean_batch": float(c_bs.mean())},
-                       "max_batch_requests": 32, "max_in_flight": 2},
+            "metric": "Mrays/s", "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": sv["requests"],
+            "warmup": 64, "ms_per_step": 1e3 * sv["wall_s"] / sv["requests"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (procedural scenes and request stream from seeds)",
+            "config": {k: v for k, v in sv.items() if k not in ("clocks", "traversals", "wall_s", "mean_d2h_bytes")},
             "e2e": {"value": value, "unit": "Mrays/s", "h2d_bytes_per_step": C.sizeof(abi.RtUniforms),
-                    "d2h_bytes_per_step": float(np.mean([w * h * 4 for _, _, w, h, _, _ in reqs]))},
+                    "d2h_bytes_per_step": sv["mean_d2h_bytes"]},
             "roofline": None,
             "cpu_baseline": cpu,
-            "clocks": clk,
-            "gpu_launches": int(st["batches"]) * 9,
+            "clocks": sv["clocks"],
+            "gpu_launches": sv["batches"] * 9,
         }))
-    dev.close()
 
 
 def main():

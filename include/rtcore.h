@@ -310,8 +310,11 @@ typedef struct RtStats {
     uint64_t nodes_visited;       /* only with RT_TRACE_FLAG_COLLECT_STATS     */
     uint64_t triangles_tested;    /* only with RT_TRACE_FLAG_COLLECT_STATS     */
     uint64_t instances_visited;   /* only with RT_TRACE_FLAG_COLLECT_STATS     */
-    uint32_t status;              /* first device-side error (RT_ERR_*)         */
+    uint32_t status;              /* bit (1 << RT_ERR_*) set for every kind of
+                                     device-side error seen; 0 = none          */
     uint32_t _padding;
+    uint64_t quantized_nodes_visited; /* of nodes_visited: 96-byte quantised BLAS
+                                     nodes (the rest are 256-byte FP32 nodes)  */
 } RtStats;
 
 /* ------------------------------------------------------------------------ */
@@ -354,9 +357,12 @@ RTCORE_API int32_t rt_cmd_build_blas(rt_ctx* ctx, const RtGeometryTriangles* geo
  * a host whose device memory belongs to another allocator that hands this
  * library only the destination buffer, or a frame loop whose memory budget
  * is fixed at start-up.
- * Limit: geometries whose rt_get_blas_build_sizes().build_scratch_size is
- * above RT_STATIC_SCRATCH_BYTES (about 400k triangles) are rejected with
- * RT_ERR_TOO_LARGE before anything is queued.  Every call uses the same
+ * FP32 nodes only: RT_BUILD_QUANTIZED_NODES returns RT_ERR_UNSUPPORTED.
+ * Limit: geometries whose rt_get_blas_build_sizes().build_scratch_size (with
+ * the same flags) is above RT_STATIC_SCRATCH_BYTES are rejected with
+ * RT_ERR_TOO_LARGE before anything is queued.  That is about 264k triangles
+ * with RT_BUILD_PREFER_FAST_TRACE (its PLOC hierarchy needs more scratch)
+ * and about 406k otherwise; the size query is the exact check.  Every call uses the same
  * array, so calls whose GPU work can overlap (different streams with no
  * ordering between them) race and corrupt each other's builds; order them.
  * The first call on each device looks the array's device address up
@@ -479,14 +485,22 @@ RTCORE_API int32_t rt_ctx_autotune(rt_ctx* ctx, const RtBatchScene* scenes, uint
  * fit the HBM budget, and the admitted ones are rendered together by
  * rt_cmd_trace_rays_batched as soon as one of `max_in_flight` batch slots is
  * free (continuous batching: requests that arrive while a batch runs join the
- * next one).  A request's image is identical to rendering it alone. */
+ * next one).  A batch also stays within max_batch_pixels ray slots and
+ * max_batch_shadow_rays shadow rays (a request beyond a limit on its own is
+ * rendered alone).  With both limits set, rt_server_create sizes the
+ * stream's wavefront workspace and the frame-buffer pool for the largest
+ * batch they allow (counted in the budget from then on), so batches within
+ * the limits allocate nothing while requests stream.  A request whose
+ * image_host is page-locked has its image written there by the output
+ * kernel; a pageable image_host gets a copy from a server frame buffer.  A
+ * request's image is identical to rendering it alone. */
 typedef struct rt_server rt_server;
 typedef struct RtServerConfig {
     uint64_t hbm_budget_bytes;    /* resident scenes + frame buffers + workspace */
     uint32_t max_batch_requests;  /* 1 = the plain per-request path */
-    uint32_t max_batch_pixels;    /* 0 = no limit */
+    uint32_t max_batch_pixels;    /* ray slots per batch (pixels padded to 8x4 tiles); 0 = no limit */
     uint32_t max_in_flight;       /* batches queued on the GPU at once, >= 1 */
-    uint32_t _padding;
+    uint32_t max_batch_shadow_rays; /* pixels x shadow rays per batch; 0 = no limit */
 } RtServerConfig;
 typedef struct RtServeScene {
     uint64_t acceleration_structure;  /* TLAS device address */
@@ -610,5 +624,6 @@ RT_STATIC_ASSERT(offsetof(RtServeRequest, image_device) == 200, "RtServeRequest.
 RT_STATIC_ASSERT(sizeof(RtServeResult) == 32, "serve result is 32 bytes");
 RT_STATIC_ASSERT(sizeof(RtServeStats) == 64, "serve stats are 64 bytes");
 RT_STATIC_ASSERT(sizeof(RtTraceTimings) == 32, "timings are 32 bytes");
+RT_STATIC_ASSERT(sizeof(RtStats) == 72, "stats are 72 bytes");
 
 #endif /* RTCORE_H */

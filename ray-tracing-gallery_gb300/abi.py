@@ -239,7 +239,8 @@ class RtAutotuneReport(C.Structure):
 
 class RtServerConfig(C.Structure):
     _fields_ = [("hbm_budget_bytes", C.c_uint64), ("max_batch_requests", C.c_uint32),
-                ("max_batch_pixels", C.c_uint32), ("max_in_flight", C.c_uint32), ("_padding", C.c_uint32)]
+                ("max_batch_pixels", C.c_uint32), ("max_in_flight", C.c_uint32),
+                ("max_batch_shadow_rays", C.c_uint32)]
 
 
 class RtServeScene(C.Structure):
@@ -330,6 +331,7 @@ class RtStats(C.Structure):
         ("instances_visited", C.c_uint64),
         ("status", C.c_uint32),
         ("_padding", C.c_uint32),
+        ("quantized_nodes_visited", C.c_uint64),
     ]
 
     def as_dict(self) -> dict:

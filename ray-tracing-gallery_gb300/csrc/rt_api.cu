@@ -168,6 +168,12 @@ struct MaybeLock {
 };
 }  // namespace
 
+cudaError_t rt::ctx_reserve_workspace(rt_ctx* ctx, cudaStream_t s, uint64_t bytes) {
+    MaybeLock l(ctx);
+    uint8_t* p = nullptr;
+    return ctx_workspace(ctx, s, bytes, &p);
+}
+
 extern "C" {
 
 RTCORE_API const char* rt_last_error_string(void) { return g_last_error.c_str(); }

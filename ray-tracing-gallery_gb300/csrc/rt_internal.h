@@ -97,6 +97,13 @@ struct TraceBatch {
 bool traversal_config_supported(const RtTraversalConfig& c);
 // Bytes of the wavefront workspace a batch needs.
 uint64_t trace_workspace_bytes(const TraceScene* scenes, uint32_t count);
+// Bytes that hold the workspace of any batch of at most `count` scenes with
+// at most `slots` ray slots (pixels padded to 8x4 tiles), `pixels` pixels
+// and `shadow_rays` shadow rays in total.
+uint64_t trace_workspace_bound(uint32_t count, uint64_t slots, uint64_t pixels, uint64_t shadow_rays);
+// Sizes the context's wavefront workspace of `stream` to at least `bytes`
+// now (stream-ordered), so that launches within that size never grow it.
+cudaError_t ctx_reserve_workspace(rt_ctx* ctx, cudaStream_t stream, uint64_t bytes);
 
 // CUDA events recorded after each kernel of a trace launch
 // (RT_TRACE_FLAG_KERNEL_TIMINGS); kind[i] names the kernel that ended at ev[i].

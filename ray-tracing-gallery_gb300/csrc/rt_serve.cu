@@ -40,6 +40,7 @@ struct Request {
     RtServeRequest req;
     Clock::time_point t_submit, t_launch, t_done;
     uint64_t frame_bytes;   // server-owned bytes: uniforms slot + image (if server-owned)
+    bool host_direct;       // image_host is page-locked: the output kernel writes it directly
     RtServeResult result;
 };
 
@@ -85,10 +86,28 @@ struct rt_server {
 
 namespace {
 
-uint64_t frame_bytes_of(const RtServeRequest& r) {
+// Whether the GPU can write `p` directly: page-locked host memory
+// (cudaHostAlloc / cudaHostRegister), which the output kernel reaches through
+// its mapping instead of a device frame buffer and a copy.
+bool page_locked(uint64_t p) {
+    if (!p) return false;
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, reinterpret_cast<void*>(p)) != cudaSuccess) {
+        cudaGetLastError();  // pageable memory may report an error on older runtimes: clear it
+        return false;
+    }
+    return a.type == cudaMemoryTypeHost;
+}
+
+uint64_t frame_bytes_of(const RtServeRequest& r, bool host_direct) {
     uint64_t b = kUniformSlot;
-    if (!r.image_device) b += align256((uint64_t)r.width * r.height * 4);
+    if (!r.image_device && !host_direct) b += align256((uint64_t)r.width * r.height * 4);
     return b;
+}
+
+// Ray slots of a request: its pixels padded to whole 8x4 tiles.
+uint64_t slots_of(const RtServeRequest& r) {
+    return (uint64_t)((r.width + 7) / 8) * 8 * (uint64_t)((r.height + 3) / 4) * 4;
 }
 
 rt::TraceScene trace_scene_of(const RtServeScene& s, const RtServeRequest& r) {
@@ -183,6 +202,8 @@ int32_t launch(rt_server* sv, Batch* b) {
         it.desc.flags = r.flags & RT_TRACE_FLAG_LAMBERT_DIFFUSE;
         if (r.image_device) {
             it.desc.image_address = r.image_device;
+        } else if (b->reqs[i]->host_direct) {
+            it.desc.image_address = r.image_host;
         } else {
             it.desc.image_address = reinterpret_cast<uint64_t>(b->device) + off;
             off += align256((uint64_t)r.width * r.height * 4);
@@ -194,7 +215,7 @@ int32_t launch(rt_server* sv, Batch* b) {
     if (st != RT_OK) return st;
     for (uint32_t i = 0; i < n; i++) {
         const RtServeRequest& r = b->reqs[i]->req;
-        if (!r.image_host) continue;
+        if (!r.image_host || b->reqs[i]->host_direct) continue;
         e = cudaMemcpyAsync(reinterpret_cast<void*>(r.image_host), reinterpret_cast<void*>(items[i].desc.image_address),
                             (size_t)r.width * r.height * 4, cudaMemcpyDeviceToHost, sv->stream);
         if (e != cudaSuccess) return RT_ERR_CUDA;
@@ -219,14 +240,18 @@ void worker_loop(rt_server* sv) {
             sv->cv.wait(lk);
             continue;
         }
-        // form a batch: arrival order, within the request / pixel limits and the budget
+        // form a batch: arrival order, within the request / ray-slot / shadow-ray limits and the budget
+        // (a request beyond a limit on its own still forms a batch alone)
         Batch* b = new Batch();
         b->server = sv;
-        uint64_t pixels = 0;
+        uint64_t slots = 0, shadow = 0;
         while (!sv->queue.empty() && b->reqs.size() < sv->cfg.max_batch_requests) {
             Request* q = sv->queue.front();
-            const uint64_t px = (uint64_t)q->req.width * q->req.height;
-            if (!b->reqs.empty() && sv->cfg.max_batch_pixels && pixels + px > sv->cfg.max_batch_pixels) break;
+            const uint64_t sl = slots_of(q->req);
+            const uint64_t sh = (uint64_t)q->req.width * q->req.height * q->req.shadow_ray_count;
+            if (!b->reqs.empty() && sv->cfg.max_batch_pixels && slots + sl > sv->cfg.max_batch_pixels) break;
+            if (!b->reqs.empty() && sv->cfg.max_batch_shadow_rays && shadow + sh > sv->cfg.max_batch_shadow_rays)
+                break;
             b->reqs.push_back(q);
             const uint64_t ws = std::max(sv->workspace, batch_workspace(sv, b->reqs));
             if (sv->resident + sv->frames + b->bytes + q->frame_bytes + ws > sv->cfg.hbm_budget_bytes) {
@@ -235,7 +260,8 @@ void worker_loop(rt_server* sv) {
             }
             sv->queue.pop_front();
             b->bytes += q->frame_bytes;
-            pixels += px;
+            slots += sl;
+            shadow += sh;
         }
         if (b->reqs.empty()) {  // the head request waits for memory to be released
             delete b;
@@ -273,10 +299,10 @@ void worker_loop(rt_server* sv) {
         if (st != RT_OK) {  // fail the batch's requests; its memory is released when the stream reaches here
             for (Request* q : b->reqs) q->result.status = (uint32_t)st;
             if (cudaLaunchHostFunc(sv->stream, batch_done, b) != cudaSuccess) {
-                for (Request* q : b->reqs) q->result.state = RT_SERVE_DONE;
-                sv->frames -= b->bytes;
-                b->done = true;
-                sv->done_cv.notify_all();
+                // no callback will come: finish the batch here, as batch_done would
+                lk.unlock();
+                batch_done(b);
+                lk.lock();
             }
         }
     }
@@ -309,11 +335,34 @@ RTCORE_API int32_t rt_server_create(rt_ctx* ctx, const RtServerConfig* config, r
     if (e == cudaSuccess)
         e = cudaMallocHost(reinterpret_cast<void**>(&sv->staging),
                            (size_t)config->max_in_flight * config->max_batch_requests * kUniformSlot);
+    if (e == cudaSuccess && config->max_batch_pixels && config->max_batch_shadow_rays) {
+        // Size the wavefront workspace of the server's stream for the largest batch the limits allow,
+        // and grow the frame-buffer pool by one full batch of images, so that steady-state batches
+        // allocate nothing new; both count against the budget from here on.
+        const uint64_t ws = rt::trace_workspace_bound(config->max_batch_requests, config->max_batch_pixels,
+                                                      config->max_batch_pixels, config->max_batch_shadow_rays);
+        const uint64_t frames = (uint64_t)config->max_batch_requests * kUniformSlot +
+                                align256((uint64_t)config->max_batch_pixels * 4);
+        if (ws + frames > config->hbm_budget_bytes) {
+            e = cudaErrorMemoryAllocation;
+        } else {
+            e = rt::ctx_reserve_workspace(ctx, sv->stream, ws);
+            void* warm = nullptr;
+            if (e == cudaSuccess) e = cudaMallocFromPoolAsync(&warm, frames, sv->pool, sv->stream);
+            if (e == cudaSuccess) e = cudaFreeAsync(warm, sv->stream);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(sv->stream);
+            if (e == cudaSuccess) {
+                sv->workspace = ws;
+                sv->note_peak();
+            }
+        }
+    }
     if (e != cudaSuccess) {
+        if (sv->staging) cudaFreeHost(sv->staging);
         if (sv->pool) cudaMemPoolDestroy(sv->pool);
         if (sv->stream) cudaStreamDestroy(sv->stream);
         delete sv;
-        return RT_ERR_CUDA;
+        return e == cudaErrorMemoryAllocation ? RT_ERR_OOM : RT_ERR_CUDA;
     }
     for (uint32_t i = 0; i < config->max_in_flight; i++) sv->free_slots.push_back(i);
     sv->stats.budget_bytes = config->hbm_budget_bytes;
@@ -361,7 +410,8 @@ RTCORE_API int32_t rt_server_submit(rt_server* sv, const RtServeRequest* r, uint
         return RT_ERR_INVALID;
     Request* q = new Request();
     q->req = *r;
-    q->frame_bytes = frame_bytes_of(*r);
+    q->host_direct = !r->image_device && page_locked(r->image_host);
+    q->frame_bytes = frame_bytes_of(*r, q->host_direct);
     q->t_submit = Clock::now();
     memset(&q->result, 0, sizeof q->result);
     {

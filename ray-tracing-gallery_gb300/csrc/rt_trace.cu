@@ -71,14 +71,17 @@ constexpr int kMaxDepth = 64;
 constexpr int kTraceWarpsPerSM = 24;
 // Kernels that decode only quantised BLAS nodes hold far fewer node registers
 // and run at 32 warps per SM (at most 64 registers a thread).
-constexpr int trace_warps_per_sm(uint32_t kinds) { return kinds == kBlasKindQ8 ? 32 : kTraceWarpsPerSM; }
+#ifndef RT_Q8_TRACE_WARPS
+#define RT_Q8_TRACE_WARPS 32
+#endif
+constexpr int trace_warps_per_sm(uint32_t kinds) { return kinds == kBlasKindQ8 ? RT_Q8_TRACE_WARPS : kTraceWarpsPerSM; }
 
 constexpr int kModeBounce = 0;   // closest hit of a bounce list -> hit records
 constexpr int kModeShadow = 1;   // any hit of generated shadow rays -> lit counters
 
 // Work counters of one lane (RT_TRACE_FLAG_COLLECT_STATS launches only).
 struct Counters {
-    uint32_t nodes, tris, insts;
+    uint32_t nodes, tris, insts, qnodes;  // qnodes: of `nodes`, the quantised ones
 };
 
 __device__ __forceinline__ uint32_t lanemask_lt() {
@@ -523,10 +526,12 @@ __device__ __forceinline__ bool trav_step(Trav& s, STK& stack, const SV& sv, con
             if (STATS) cnt.nodes++;
             uint32_t keys[8], refs[8];
             // TLAS nodes are always FP32
-            if ((KINDS & kBlasKindQ8) && s.in_blas && (KINDS == kBlasKindQ8 || s.quant))
+            if ((KINDS & kBlasKindQ8) && s.in_blas && (KINDS == kBlasKindQ8 || s.quant)) {
+                if (STATS) cnt.qnodes++;
                 qnode_keys(s, entry, keys, refs);
-            else
+            } else {
                 fnode_keys(s, entry, keys, refs);
+            }
             if (ray_flags & RT_RAY_FLAG_TERMINATE_ON_FIRST_HIT) {
                 // Any accepted hit ends the ray and t never shrinks before
                 // that, so neither the visit order nor the stored tnear
@@ -610,6 +615,9 @@ __device__ __forceinline__ void flush_counters(RtStats* st, const Counters& c) {
         atomicAdd(reinterpret_cast<unsigned long long*>(&st->nodes_visited), (unsigned long long)c.nodes);
         atomicAdd(reinterpret_cast<unsigned long long*>(&st->triangles_tested), (unsigned long long)c.tris);
         atomicAdd(reinterpret_cast<unsigned long long*>(&st->instances_visited), (unsigned long long)c.insts);
+        if (c.qnodes)
+            atomicAdd(reinterpret_cast<unsigned long long*>(&st->quantized_nodes_visited),
+                      (unsigned long long)c.qnodes);
     }
 }
 
@@ -842,7 +850,7 @@ __device__ __forceinline__ void trace_wavefront(const WfParams& P) {
                                    : RT_RAY_FLAG_NONE;
     const uint32_t sbt_offset = MODE == kModeShadow ? 1u : 0u;
 
-    Counters cnt = {0, 0, 0};
+    Counters cnt = {0, 0, 0, 0};
     TravStack<SD, BLOCK> stack;
     if (SD > 0) {
         extern __shared__ uint2 stack_smem[];
@@ -971,10 +979,12 @@ __device__ __forceinline__ void packet_traverse(Trav& s, uint2* ws, const unsign
             } else {
                 if (STATS) cnt.nodes++;
                 uint32_t keys[8], refs[8];
-                if ((KINDS & kBlasKindQ8) && s.in_blas && (KINDS == kBlasKindQ8 || s.quant))
+                if ((KINDS & kBlasKindQ8) && s.in_blas && (KINDS == kBlasKindQ8 || s.quant)) {
+                    if (STATS) cnt.qnodes++;
                     qnode_keys(s, entry, keys, refs);
-                else
+                } else {
                     fnode_keys(s, entry, keys, refs);
+                }
                 // the nearest lane's key of each child; every lane has read its
                 // last popped entry before this point, so the pushes below
                 // cannot overwrite an entry a lane has yet to read
@@ -1089,7 +1099,7 @@ __device__ __forceinline__ void trace_packets(const WfParams& P) {
                                    ? (RT_RAY_FLAG_TERMINATE_ON_FIRST_HIT | RT_RAY_FLAG_SKIP_CLOSEST_HIT_SHADER)
                                    : RT_RAY_FLAG_NONE;
     const uint32_t sbt_offset = MODE == kModeShadow ? 1u : 0u;
-    Counters cnt = {0, 0, 0};
+    Counters cnt = {0, 0, 0, 0};
     for (;;) {
         uint32_t base = 0;
         if (lane == 0) base = atomicAdd(work, 32u);
@@ -1186,8 +1196,12 @@ __device__ __forceinline__ void trace_packets(const WfParams& P) {
 // at once: the FP32 kernels run at 20 warps per SM (96 registers, 68-byte
 // spills instead of 288 at 80 registers; 1080p frame +0.8 %, 16 warps -1 %).
 // A 256-thread block cannot make 20 warps and keeps 24.
+#ifndef RT_Q8_PACKET_WARPS
+#define RT_Q8_PACKET_WARPS 32
+#endif
 constexpr int packet_warps_per_sm(uint32_t kinds, int block) {
-    return kinds == kBlasKindQ8 ? 32 : (block == 256 ? 24 : 20);
+    return kinds == kBlasKindQ8 ? (block == 256 && RT_Q8_PACKET_WARPS < 24 ? 24 : RT_Q8_PACKET_WARPS)
+                                : (block == 256 ? 24 : 20);
 }
 
 template <int MODE, bool STATS, uint32_t KINDS, int BLOCK, bool LANE_BOUNCES>
@@ -1358,7 +1372,7 @@ template <bool STATS, uint32_t KINDS>
 __device__ __forceinline__ void trace_ray_buffer(const RayBufferParams& P, const Env& e) {
     const RayBufferLaunch& L = P.L;
     const OneScene sv{e};
-    Counters cnt = {0, 0, 0};
+    Counters cnt = {0, 0, 0, 0};
     TravStack<0, kTraceThreads> stack;
     Trav s;
     uint32_t item = kNoItem;
@@ -1595,6 +1609,18 @@ struct BatchLayout {
             max_depth = std::max(max_depth, sc[i].desc.max_trace_depth);
             any_shadow = any_shadow || sc[i].desc.shadow_ray_count > 0;
         }
+        place(n);
+    }
+    // A layout for batch totals alone (no per-scene records): the workspace
+    // of any batch of at most n scenes, `slots` ray slots (pixels padded to
+    // 8x4 tiles), `pixels` pixels and `shadow` shadow rays fits in it.
+    BatchLayout(uint32_t n, uint64_t slots_, uint64_t pixels_, uint64_t shadow) {
+        slots = slots_;
+        pixels = pixels_;
+        shadow_rays = shadow;
+        place(n);
+    }
+    void place(uint32_t n) {
         uint64_t b = 0;
         auto take = [&](uint64_t bytes) {
             uint64_t r = b;
@@ -1639,6 +1665,10 @@ bool traversal_config_supported(const RtTraversalConfig& c) {
 
 uint64_t trace_workspace_bytes(const TraceScene* scenes, uint32_t count) {
     return BatchLayout(scenes, count).total;
+}
+
+uint64_t trace_workspace_bound(uint32_t count, uint64_t slots, uint64_t pixels, uint64_t shadow_rays) {
+    return BatchLayout(count, slots, pixels, shadow_rays).total;
 }
 
 cudaError_t launch_trace_batch(const TraceBatch& tb, uint8_t* ws, int num_sms, cudaStream_t stream,

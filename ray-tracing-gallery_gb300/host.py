@@ -277,6 +277,7 @@ class GpuScene:
         infos = np.array([m.model_info() for m in self.models], abi.MODEL_INFO_DTYPE)
         self.model_info_buffer = Device.upload(infos)
         self.texture_table, self.texture_count, self._texture_refs = None, 0, []
+        self.texture_descs = None
         if own_textures:
             n = max(scene.textures) + 1 if scene.textures else 1
             table = (abi.RtTextureDesc * n)()
@@ -285,6 +286,7 @@ class GpuScene:
                 self._texture_refs.append(buf)
             self.texture_table = Device.upload(np.frombuffer(bytes(table), np.uint8))
             self.texture_count = n
+            self.texture_descs = table
         else:
             ImageManager(device).push_images(scene.textures)
         self.num_instances = len(scene.instances)
@@ -292,6 +294,16 @@ class GpuScene:
         self.instances_buffer = Device.upload(self.instances_host)
         self.tlas = AccelerationStructure.build_tlas(device, self.instances_buffer, self.num_instances, self.scratch,
                                                      tlas_flags, stream)
+
+    def bind_textures(self) -> None:
+        """Binds a scene with its own texture table into the context's
+        bindless table (rt_ctx_set_texture per index), as a host that renders
+        several scenes through rt_cmd_trace_rays does before each call."""
+        if self.texture_descs is None:
+            raise ValueError("bind_textures needs a scene built with own_textures=True")
+        for idx in range(self.texture_count):
+            self.device.check(self.device.lib.rt_ctx_set_texture(self.device.ctx, idx,
+                                                                 C.byref(self.texture_descs[idx])))
 
     def patch_instances(self, instances: np.ndarray) -> np.ndarray:
         """Scene instances carry model indices; replace them by BLAS addresses."""
@@ -492,9 +504,10 @@ class Server:
     context must be thread-safe (Device(threadsafe=True))."""
 
     def __init__(self, device: Device, budget_bytes: int, max_batch_requests: int = 32, max_batch_pixels: int = 0,
-                 max_in_flight: int = 2):
+                 max_in_flight: int = 2, max_batch_shadow_rays: int = 0):
         self.device = device
-        cfg = abi.RtServerConfig(int(budget_bytes), max_batch_requests, max_batch_pixels, max_in_flight, 0)
+        cfg = abi.RtServerConfig(int(budget_bytes), max_batch_requests, max_batch_pixels, max_in_flight,
+                                 max_batch_shadow_rays)
         self.handle = C.c_void_p()
         device.check(device.lib.rt_server_create(device.ctx, C.byref(cfg), C.byref(self.handle)))
         self.scenes = []

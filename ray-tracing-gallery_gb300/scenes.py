@@ -329,6 +329,28 @@ def checker_alpha_rgba8(size: int = 64, cell: int = 8, rgb=(200, 180, 90)) -> Te
     return Texture(t, abi.RT_FORMAT_R8G8B8A8_SRGB, abi.RT_FILTER_LINEAR)
 
 
+def bump_normal_map_rgba8(seed: int, size: int = 64, strength: float = 0.6) -> Texture:
+    """A tangent-space normal map (RGBA8 UNORM, n * 0.5 + 0.5 per channel, as
+    glTF normal textures are stored) of a height field of random sinusoidal
+    bumps; bilinear filtering."""
+    rng = Pcg32(seed, 0x4E)
+    y, x = np.mgrid[0:size, 0:size].astype(np.float64) / size
+    dx = np.zeros_like(x)
+    dy = np.zeros_like(y)
+    for _ in range(4):
+        fx, fy = 1 + int(rng.next_u32() % 4), 1 + int(rng.next_u32() % 4)
+        px, py = rng.uniform() * 2 * np.pi, rng.uniform() * 2 * np.pi
+        # height sin(2 pi fx x + px) * sin(2 pi fy y + py): its slopes
+        dx += fx * np.cos(2 * np.pi * fx * x + px) * np.sin(2 * np.pi * fy * y + py)
+        dy += fy * np.sin(2 * np.pi * fx * x + px) * np.cos(2 * np.pi * fy * y + py)
+    n = np.stack([-strength * dx / 4, -strength * dy / 4, np.ones_like(x)], -1)
+    n /= np.linalg.norm(n, axis=-1, keepdims=True)
+    t = np.zeros((size, size, 4), np.uint8)
+    t[..., :3] = np.clip(np.round((n * 0.5 + 0.5) * 255), 0, 255).astype(np.uint8)
+    t[..., 3] = 255
+    return Texture(t, abi.RT_FORMAT_R8G8B8A8_UNORM, abi.RT_FILTER_LINEAR)
+
+
 def rank_noise_rgba8(seed: int, size: int = 64) -> Texture:
     """size*size noise whose values are a random permutation of ranks
     (uniform histogram), UNORM like the reference's blue noise
@@ -445,6 +467,7 @@ TEX_MR_DEFAULT = 4
 TEX_FENCE = 5
 TEX_MR_SHINY = 6
 TEX_MIRROR_TINT = 7
+TEX_NORMAL_MAP = 8
 
 
 def _base_textures(seed: int) -> dict[int, Texture]:
@@ -457,6 +480,7 @@ def _base_textures(seed: int) -> dict[int, Texture]:
         TEX_FENCE: checker_alpha_rgba8(),
         TEX_MR_SHINY: metallic_roughness(0.5, 0.3),
         TEX_MIRROR_TINT: solid_rgba32f([1.0, 1.0, 1.0, 1.0]),
+        TEX_NORMAL_MAP: bump_normal_map_rgba8(seed),
     }
 
 
@@ -542,13 +566,16 @@ def scene_full(frame: int = 0, width: int = 1920, height: int = 1080, seed: int 
 
 def scene_gallery(width: int = 320, height: int = 200, seed: int = 11, frame: int = 0) -> Scene:
     """A small scene that exercises every program of the reference: textured
-    tori and ground, mirror tori, a portal plane (SBT offset 2) and an
-    alpha-clipped double-sided fence, soft shadows (2 rays, sun_radius 0.05)
-    and the 3-iteration bounce loop, as DefaultScene lays them out
-    (src/scene.rs:95-156)."""
+    tori and a normal-mapped ground, mirror tori, a portal plane (SBT offset
+    2) and an alpha-clipped double-sided fence, soft shadows (2 rays,
+    sun_radius 0.05) and the 3-iteration bounce loop, as DefaultScene lays
+    them out (src/scene.rs:95-156).  The ground's geometry names a normal map
+    (closest_hit_textured.glsl:123-157: the cotangent frame from its
+    positions and UVs); the tori have none."""
     rng = Pcg32(seed)
     tor = _model(torus(1.0, 0.35, 32, 16), "torus", lambda idx: [Geometry(idx, True, TEX_DIFFUSE_A, TEX_MR_SHINY)])
-    pln = _model(ground_plane(2.0, 0.0), "plane", lambda idx: [Geometry(idx, True, TEX_DIFFUSE_B, TEX_MR_DEFAULT)])
+    pln = _model(ground_plane(2.0, 0.0), "plane",
+                 lambda idx: [Geometry(idx, True, TEX_DIFFUSE_B, TEX_MR_DEFAULT, TEX_NORMAL_MAP)])
     fen = _model(quad_grid(20, 1, 2.0, 1.0, 4.0, 1.0), "fence",
                  lambda idx: [Geometry(idx, False, TEX_FENCE, TEX_MR_DEFAULT)])
     xf, mdl, sbt, flg = [], [], [], []

@@ -19,13 +19,40 @@ def _args(argv):
         sys.argv = old
 
 
-def test_defaults_are_one_gpu_on_the_frame():
+def test_defaults_are_one_gpu_on_the_headline_batch():
     a = _args([])
-    assert a.gpus == 1 and a.workload == "frame" and a.impl == "ours"
-    assert (a.width, a.height) == (1920, 1080)
+    assert a.gpus == 1 and a.workload == "batch" and a.impl == "ours"
+    assert a.batch_scenes == 64 and a.serve_seconds == 120.0
     assert a.warmup >= 3 and a.traversal is None
+    f = _args(["--workload", "frame"])
+    assert (f.width, f.height) == (1920, 1080)
     s = _args(["--workload", "scene"])
     assert (s.width, s.height) == (1280, 720)
+
+
+def test_headline_metric_is_the_baseline_metric():
+    import json
+
+    base = json.loads((ROOT / "BASELINE.json").read_text())
+    assert bench.BATCH_METRIC == base["metric"]
+
+
+def test_camera_ray_sample_points_into_the_view():
+    import numpy as np
+
+    from rtgallery import scenes
+
+    sc = scenes.scene_batch_member(0)
+    r = bench.camera_ray_sample(sc, 8)
+    assert len(r) == ((sc.height + 7) // 8) * ((sc.width + 7) // 8)
+    d = r["direction"]
+    assert np.allclose(np.linalg.norm(d, axis=1), 1.0, atol=1e-5)
+    # the centre ray looks at the scene's target (0, 0.5, 0)
+    vi = np.array(sc.uniforms.view_inverse, np.float32).reshape(4, 4).T
+    eye = vi[:3, 3]
+    to_target = np.array([0.0, 0.5, 0.0]) - eye
+    to_target /= np.linalg.norm(to_target)
+    assert float((d @ to_target).max()) > 0.999
 
 
 def test_traversal_option_is_a_config_tuple():

@@ -159,6 +159,24 @@ def test_render_matches_oracle(device, name):
     assert np.abs(img.astype(int) - o_img.astype(int)).max() <= 1
 
 
+def test_normal_map_branch_matches_oracle(device):
+    """closest_hit_textured.glsl:123-157: the gallery's ground names a normal
+    map (RGBA8 UNORM, bilinear), so its shading takes the cotangent-frame
+    branch; those pixels must match the oracle, and the branch must matter
+    (without the map the oracle's radiance there differs)."""
+    sc = scenes.scene_gallery(320, 200)
+    assert sc.models[1].geometries[0].normal_map_image == scenes.TEX_NORMAL_MAP
+    img, rad, st = _host().render(device, sc, radiance=True)
+    o_img, o_rad, _ = O.OracleScene(sc).render()
+    plain = scenes.scene_gallery(320, 200)
+    plain.models[1].geometries[0].normal_map_image = -1
+    _, p_rad, _ = O.OracleScene(plain).render()
+    mapped = np.abs(o_rad - p_rad)[..., :3].max(-1) > 1e-3
+    assert mapped.sum() > 5000, int(mapped.sum())
+    assert np.abs(rad - o_rad)[mapped].max() <= RADIANCE_TOL
+    assert np.abs(img.astype(int) - o_img.astype(int)).max() <= 1
+
+
 def test_tlas_update_matches_rebuild(device):
     """DefaultScene::update + write_resources (src/scene.rs:163-204): move one
     instance, refit the TLAS in place, then compare with the oracle."""

@@ -114,3 +114,80 @@ def test_server_needs_threadsafe_context(device):
     host = _host()
     with pytest.raises(abi.RtError):
         host.Server(device, 1 << 30)
+
+
+def _serve_limited(dev, gscenes, reqs, budget, max_batch, in_flight, max_pixels, max_shadow, host_images=False):
+    """Like _serve, with batch limits (the server then reserves its workspace
+    at creation); host_images: the images go to page-locked host buffers,
+    which the output kernel writes directly."""
+    import torch
+
+    host = _host()
+    srv = host.Server(dev, budget, max_batch_requests=max_batch, max_in_flight=in_flight,
+                      max_batch_pixels=max_pixels, max_batch_shadow_rays=max_shadow)
+    after_create = srv.stats()
+    ids = [srv.add_scene(g) for g in gscenes]
+    if host_images:
+        imgs = [torch.zeros(r["height"] * r["width"] * 4, dtype=torch.uint8).pin_memory() for r in reqs]
+        kw = [dict(image_host=img.data_ptr()) for img in imgs]
+    else:
+        imgs = [torch.zeros(r["height"] * r["width"] * 4, dtype=torch.uint8, device="cuda") for r in reqs]
+        kw = [dict(image_device=img.data_ptr()) for img in imgs]
+    torch.cuda.synchronize()
+    tickets = [srv.submit(ids[r["scene"]], r["uniforms"], r["width"], r["height"], r["max_trace_depth"],
+                          r["shadow_ray_count"], **k) for r, k in zip(reqs, kw)]
+    results = [srv.wait(t, 120000) for t in tickets]
+    stats = srv.stats()
+    srv.close()
+    torch.cuda.synchronize()
+    return [i.cpu() for i in imgs], results, stats, after_create
+
+
+def _slots(r):
+    return ((r["width"] + 7) // 8 * 8) * ((r["height"] + 3) // 4 * 4)
+
+
+def test_full_hd_request_in_a_mix_with_batch_limits(served):
+    """A 1920x1080 request with 8 shadow rays among small ones, through a
+    server with batch limits (ray slots and shadow rays) and a reserved
+    workspace: every image equals the request rendered alone, no batch
+    exceeds the limits unless it holds one request, the reserved workspace
+    is counted from creation on, and the 1080p request matches the oracle."""
+    dev, specs, gscenes = served
+    reqs = _requests(24, 11)
+    big = dict(scene=1, uniforms=scenes.random_view_uniforms(scenes.Pcg32(77, 1), 1920, 1080, frame=3),
+               width=1920, height=1080, max_trace_depth=3, shadow_ray_count=8)
+    reqs.insert(7, big)
+    limit_px, limit_sh = 1 << 20, 4 << 20
+    alone, res_a, _ = _serve(dev, gscenes, reqs, 16 << 30, 1, 1)
+    mix, res_m, st, created = _serve_limited(dev, gscenes, reqs, 16 << 30, 16, 2, limit_px, limit_sh)
+    assert all(r.state == abi.RT_SERVE_DONE and r.status == 0 for r in res_a + res_m)
+    assert created["peak_bytes"] > (64 << 20), "the reserved workspace is not counted at creation"
+    for k in range(len(reqs)):
+        assert np.array_equal(alone[k].cpu().numpy(), mix[k].numpy()), f"request {k} differs alone vs in the mix"
+    by_batch = {}
+    for r, q in zip(res_m, reqs):
+        by_batch.setdefault(r.batch, []).append(q)
+    assert max(len(v) for v in by_batch.values()) > 1, "the mix never batched"
+    for b, qs in by_batch.items():
+        if len(qs) > 1:
+            assert sum(_slots(q) for q in qs) <= limit_px, b
+            assert sum(q["width"] * q["height"] * q["shadow_ray_count"] for q in qs) <= limit_sh, b
+    assert res_m[7].batch_requests == 1  # beyond both limits on its own: rendered alone
+    o_img, _, _ = O.OracleScene(specs[1]).render(uniforms=big["uniforms"], width=1920, height=1080,
+                                                 max_trace_depth=3, shadow_ray_count=8)
+    img = mix[7].numpy().reshape(1080, 1920, 4)
+    assert np.abs(img.astype(int) - o_img.astype(int)).max() <= 1
+
+
+def test_page_locked_host_images_are_written_directly(served):
+    """Requests whose image_host is page-locked get their image from the
+    output kernel itself (no server frame buffer): the same bytes as device
+    images."""
+    dev, specs, gscenes = served
+    reqs = _requests(16, 21)
+    dev_imgs, _, _, _ = _serve_limited(dev, gscenes, reqs, 8 << 30, 8, 2, 1 << 20, 8 << 20)
+    host_imgs, res, st, _ = _serve_limited(dev, gscenes, reqs, 8 << 30, 8, 2, 1 << 20, 8 << 20, host_images=True)
+    assert all(r.state == abi.RT_SERVE_DONE and r.status == 0 for r in res)
+    for k in range(len(reqs)):
+        assert np.array_equal(dev_imgs[k].numpy(), host_imgs[k].numpy()), k

@@ -135,3 +135,17 @@ def test_static_scratch_rejects_oversized_geometry(device):
                                                     None)
     assert r == abi.RT_ERR_TOO_LARGE
     assert b"static scratch" in device.lib.rt_last_error_string()
+
+
+def test_static_scratch_rejects_quantized_nodes(device):
+    """The static-scratch build writes FP32 nodes only: a request for 8-bit
+    quantised nodes is refused before anything is queued."""
+    geo = (abi.RtGeometryTriangles * 1)()
+    geo[0].vertex_address = 4096
+    geo[0].vertex_stride = 12
+    geo[0].primitive_count = 100
+    geo[0].max_vertex = 300
+    flags = abi.RT_BUILD_PREFER_FAST_TRACE | abi.RT_BUILD_QUANTIZED_NODES
+    r = device.lib.rt_cmd_build_blas_static_scratch(device.ctx, geo, 1, flags, 1 << 20, 1 << 20, None)
+    assert r == abi.RT_ERR_UNSUPPORTED
+    assert b"QUANTIZED" in device.lib.rt_last_error_string()
