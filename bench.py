@@ -85,8 +85,8 @@ def parse_args():
                         "precision: 10,485,760-triangle icosphere, 4M random rays, quantised vs FP32 nodes; "
                         "serve: the Poisson request stream over 32 resident scenes alone")
     p.add_argument("--traversal", default=None, metavar="B,D,W,P",
-                   help="frame / scene: set this RtTraversalConfig (block_size, shared_stack_depth, leaf_wait, "
-                        "packet_lists) instead of running rt_ctx_autotune on the workload's frame")
+                   help="batch / frame / scene: set this RtTraversalConfig (block_size, shared_stack_depth, "
+                        "leaf_wait, packet_lists) instead of running rt_ctx_autotune on the workload")
     p.add_argument("--batch-scenes", type=int, default=64, help=argparse.SUPPRESS)
     p.add_argument("--serve-seconds", type=float, default=120.0,
                    help="batch / serve: length of the request stream (0: batch skips the stream)")
@@ -1034,20 +1034,26 @@ def bench_batch(args):
     # ---- the autotuner: launch shape for the FP32 batch (decomposition only), and launch shape x node
     # width {8, 4} for the quantised batch; the graph is captured with the quantised winner ----
     t_tune = time.perf_counter()
-    best32 = autotune(arr32)
-    best_q8 = autotune(arrq8)
-    frq4 = batch_setup(dev, scs, quantized=True, width4=True)
-    arrq4 = items_of(frq4)
-    with torch.cuda.stream(stream):
-        batched(arrq4)  # sizes the workspace outside the tuner
-    torch.cuda.synchronize()
-    best_q4 = autotune(arrq4)
+    if args.traversal:  # a given launch shape for both paths, 8-wide nodes, no tuning
+        fixed = abi.RtTraversalConfig(*(int(v) for v in args.traversal.split(",")))
+        best32 = best_q8 = best_q4 = (None, fixed, abi.RtAutotuneReport())
+        frq4 = arrq4 = None
+        width, tuned = 8, fixed
+    else:
+        best32 = autotune(arr32)
+        best_q8 = autotune(arrq8)
+        frq4 = batch_setup(dev, scs, quantized=True, width4=True)
+        arrq4 = items_of(frq4)
+        with torch.cuda.stream(stream):
+            batched(arrq4)  # sizes the workspace outside the tuner
+        torch.cuda.synchronize()
+        best_q4 = autotune(arrq4)
+        width = 4 if best_q4[0] < best_q8[0] else 8
+        tuned = best_q4[1] if width == 4 else best_q8[1]
     tune_s = time.perf_counter() - t_tune
-    width = 4 if best_q4[0] < best_q8[0] else 8
-    tuned = best_q4[1] if width == 4 else best_q8[1]
     frq, arrq = (frq4, arrq4) if width == 4 else (frq8, arrq8)
-    note(f"autotune {tune_s:.1f} s: quantised width {width} {tuned.as_tuple()}, "
-         f"best ms q8 {best_q8[0]:.2f} q4 {best_q4[0]:.2f} fp32 {best32[0]:.2f}")
+    note(f"traversal config: quantised width {width} {tuned.as_tuple()} ({tune_s:.1f} s), "
+         f"best ms q8 {best_q8[0]} q4 {best_q4[0]} fp32 {best32[0]}")
 
     # FP32 batched (the batching gain alone), its own tuned launch shape
     set_cfg(best32[1])
@@ -1195,7 +1201,8 @@ def bench_batch(args):
                "radiance": err,
                "autotuned_config": {"node_width": width, "block_size": tuned.block_size,
                                     "shared_stack_depth": tuned.shared_stack_depth,
-                                    "leaf_wait": tuned.leaf_wait, "packet_lists": tuned.packet_lists},
+                                    "leaf_wait": tuned.leaf_wait, "packet_lists": tuned.packet_lists,
+                                    "chosen_by": "--traversal" if args.traversal else "rt_ctx_autotune"},
                "autotune_configs": int(best_q8[2].count + best_q4[2].count + best32[2].count),
                "autotune_s": tune_s,
                "autotune_best_ms": {"quantized_width8": best_q8[0], "quantized_width4": best_q4[0],

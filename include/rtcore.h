@@ -584,6 +584,15 @@ RTCORE_API int32_t rt_trace_ray_buffer_host(rt_ctx* ctx, uint64_t tlas, const Rt
 #define RT_FN_WATERTIGHT 6u              /* in: ray + triangle (16 floats)     -> out: hit, t, u, v */
 /* `in` and `out` are device float arrays with the per-function stride. */
 RTCORE_API int32_t rt_debug_eval(uint32_t function, uint64_t in, uint64_t out, uint32_t count, void* stream);
+/* Self-test of the BVH builder's key sort (the Morton-code sort inside
+ * rt_cmd_build_blas / rt_cmd_build_tlas): sorts `count` device (uint32 key,
+ * uint32 value) pairs in place, stably by key.  `scratch` (256-byte aligned,
+ * scratch_size bytes) holds the second buffers and the sort state; with
+ * scratch = 0 only *scratch_needed is written.  Synchronises `stream`;
+ * RT_ERR_TIMEOUT if a bounded wait of the sort gave up.  No counterpart in
+ * the reference (the driver's build is closed). */
+RTCORE_API int32_t rt_debug_sort_pairs(uint64_t keys, uint64_t values, uint32_t count, uint64_t scratch,
+                                       uint64_t scratch_size, uint64_t* scratch_needed, void* stream);
 
 #ifdef __cplusplus
 } /* extern "C" */

@@ -405,6 +405,8 @@ EXPORTED_FUNCTIONS = {
                                              C.POINTER(RtShaderBindingTable), C.c_uint32, C.c_uint32, C.c_uint32,
                                              C.c_uint64, C.c_uint32, C.c_uint64, C.c_void_p]),
     "rt_debug_eval": (C.c_int32, [C.c_uint32, C.c_uint64, C.c_uint64, C.c_uint32, C.c_void_p]),
+    "rt_debug_sort_pairs": (C.c_int32, [C.c_uint64, C.c_uint64, C.c_uint32, C.c_uint64, C.c_uint64,
+                                        C.POINTER(C.c_uint64), C.c_void_p]),
 }
 
 

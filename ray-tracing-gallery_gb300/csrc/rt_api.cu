@@ -882,4 +882,34 @@ RTCORE_API int32_t rt_debug_eval(uint32_t function, uint64_t in, uint64_t out, u
     return RT_OK;
 }
 
+RTCORE_API int32_t rt_debug_sort_pairs(uint64_t keys, uint64_t values, uint32_t count, uint64_t scratch,
+                                       uint64_t scratch_size, uint64_t* scratch_needed, void* stream) {
+    // scratch: an error word, the second key / value buffers, the sort state
+    const uint64_t off_k1 = 256, off_v1 = align_up(off_k1 + (uint64_t)count * 4, 256);
+    const uint64_t off_state = align_up(off_v1 + (uint64_t)count * 4, 256);
+    const uint64_t need = off_state + key_sort_state_bytes(count);
+    if (scratch_needed) *scratch_needed = need;
+    if (!scratch) return RT_OK;
+    if (count > kMaxPrimitives) return fail(RT_ERR_TOO_LARGE, "%u pairs > %u", count, kMaxPrimitives);
+    if (scratch_size < need)
+        return fail(RT_ERR_INVALID, "scratch_size %llu < %llu", (unsigned long long)scratch_size,
+                    (unsigned long long)need);
+    if (count > 0 && (!keys || !values || !aligned(keys, 4) || !aligned(values, 4) || !aligned(scratch, 256)))
+        return fail(RT_ERR_INVALID, "keys / values must be 4-byte aligned, scratch 256-byte aligned");
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    uint8_t* base = reinterpret_cast<uint8_t*>(scratch);
+    uint32_t* err = reinterpret_cast<uint32_t*>(base);
+    cudaError_t e = cudaMemsetAsync(err, 0, 4, st);
+    if (e == cudaSuccess)
+        e = launch_key_sort(reinterpret_cast<uint32_t*>(keys), reinterpret_cast<uint32_t*>(values),
+                            reinterpret_cast<uint32_t*>(base + off_k1), reinterpret_cast<uint32_t*>(base + off_v1), count,
+                            base + off_state, err, st);
+    uint32_t h_err = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&h_err, err, 4, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_fail(e, "rt_debug_sort_pairs");
+    if (h_err & (1u << RT_ERR_TIMEOUT)) return fail(RT_ERR_TIMEOUT, "rt_debug_sort_pairs: a bounded wait gave up");
+    return RT_OK;
+}
+
 }  // extern "C"

@@ -4,9 +4,9 @@
 // 8-wide nodes:
 //   1. primitive boxes (triangles, or instance world boxes) + centroid bounds
 //   2. 30-bit Morton codes of the centroids
-//   3. stable LSD radix sort, 8-bit digits, 4 passes (reduce-then-scan:
-//      per-tile digit histograms, one exclusive scan, stable scatter ranked
-//      with warp match_any)
+//   3. stable LSD radix sort, 8-bit digits, 4 passes: one block for up to
+//      kSortTile keys, else onesweep (one upfront histogram of all digits,
+//      then one kernel per digit with decoupled look-back across partitions)
 //   4. the binary hierarchy: PLOC clustering (RT_BUILD_PREFER_FAST_TRACE;
 //      boxes and subtree sizes come with each merge), or the Karras LBVH
 //      (index-augmented for ties) with bottom-up boxes from one arrival
@@ -396,20 +396,6 @@ __global__ void k_morton(const float4* boxes, uint32_t n, const BuildState* st, 
 }
 
 // ---- radix sort -----------------------------------------------------------
-__global__ void __launch_bounds__(kSortThreads) k_radix_hist(const uint32_t* keys, uint32_t n, int shift,
-                                                             uint32_t* hist, uint32_t nblocks) {
-    __shared__ uint32_t h[256];
-    for (int i = threadIdx.x; i < 256; i += blockDim.x) h[i] = 0;
-    __syncthreads();
-    uint32_t base = blockIdx.x * kSortTile;
-    for (int j = 0; j < kSortItems; j++) {
-        uint32_t idx = base + j * kSortThreads + threadIdx.x;
-        if (idx < n) atomicAdd(&h[(keys[idx] >> shift) & 255u], 1u);
-    }
-    __syncthreads();
-    for (int d = threadIdx.x; d < 256; d += blockDim.x) hist[(size_t)d * nblocks + blockIdx.x] = h[d];
-}
-
 // Exclusive scan of m values by one block of 1024 threads.
 __global__ void __launch_bounds__(1024) k_scan_exclusive(uint32_t* data, uint32_t m) {
     __shared__ uint32_t warp_sums[32];
@@ -495,18 +481,6 @@ __global__ void __launch_bounds__(kSortThreads) k_radix_sort_small(uint32_t* k0,
     }
 }
 
-__global__ void __launch_bounds__(kSortThreads) k_radix_scatter(const uint32_t* kin, const uint32_t* vin,
-                                                                uint32_t* kout, uint32_t* vout, uint32_t n,
-                                                                int shift, const uint32_t* hist, uint32_t nblocks) {
-    __shared__ SortTileShared sm;
-    for (int d = threadIdx.x; d < 256; d += blockDim.x) {
-        sm.digit_base[d] = hist[(size_t)d * nblocks + blockIdx.x];
-        sm.run[d] = 0;
-    }
-    __syncthreads();
-    scatter_tile(sm, kin, vin, kout, vout, n, shift, blockIdx.x);
-}
-
 __device__ void scatter_tile(SortTileShared& sm, const uint32_t* kin, const uint32_t* vin, uint32_t* kout,
                              uint32_t* vout, uint32_t n, int shift, uint32_t tile) {
     uint32_t* digit_base = sm.digit_base;
@@ -548,6 +522,222 @@ __device__ void scatter_tile(SortTileShared& sm, const uint32_t* kin, const uint
         __syncthreads();
     }
 }
+
+// ---- onesweep radix sort ------------------------------------------------------
+// Keys of more than one sort tile are sorted by the single-pass LSD scheme of
+// Adinets & Merrill ("Onesweep", 2022): one upfront histogram of all four
+// 8-bit digits, then one kernel per digit.  In a digit pass each block takes
+// the next partition of kOsTile keys from a counter (so every earlier
+// partition belongs to a block that is already running), ranks its keys
+// stably per digit (warp match_any, warps over consecutive chunks), publishes
+// its per-digit counts, and finds the keys of each digit in all earlier
+// partitions by decoupled look-back: it walks back over their descriptors,
+// adding aggregates until one carries the inclusive prefix.  The tile is then
+// staged in shared memory in digit order and written out so that consecutive
+// threads write consecutive positions.  Each look-back wait is bounded: after
+// kOsSpinLimit polls the build records RT_ERR_TIMEOUT and goes on.
+constexpr int kOsThreads = 256;
+constexpr int kOsItems = 15;
+constexpr uint32_t kOsTile = kOsThreads * kOsItems;  // 3840 keys per partition
+constexpr int kOsWarps = kOsThreads / 32;
+constexpr uint32_t kOsAggregate = 1u << 30, kOsPrefix = 2u << 30, kOsValue = (1u << 30) - 1u;
+constexpr uint32_t kOsSpinLimit = 1u << 22;
+
+// The sort's scratch header: digit counts of the four passes (scanned in
+// place to each digit's first output position) and each pass's partition
+// counter.  The partition descriptors follow: [pass][partition][digit].
+struct OnesweepState {
+    uint32_t count[4][256];
+    uint32_t next_partition[4];
+};
+
+__host__ __device__ inline uint32_t onesweep_partitions(uint32_t n) { return (n + kOsTile - 1) / kOsTile; }
+
+__device__ __forceinline__ uint32_t ld_relaxed(const uint32_t* p) {
+    uint32_t v;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_relaxed(uint32_t* p, uint32_t v) {
+    asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+__global__ void __launch_bounds__(kOsThreads) k_onesweep_hist(const uint32_t* keys, uint32_t n, OnesweepState* os) {
+    __shared__ uint32_t h[4][256];
+    for (int i = threadIdx.x; i < 1024; i += blockDim.x) (&h[0][0])[i] = 0;
+    __syncthreads();
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t k = keys[i];
+        atomicAdd(&h[0][k & 255u], 1u);
+        atomicAdd(&h[1][(k >> 8) & 255u], 1u);
+        atomicAdd(&h[2][(k >> 16) & 255u], 1u);
+        atomicAdd(&h[3][k >> 24], 1u);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < 1024; i += blockDim.x) {
+        const uint32_t c = (&h[0][0])[i];
+        if (c) atomicAdd(&(&os->count[0][0])[i], c);
+    }
+}
+
+// Exclusive scan of 256 values by 256 threads (one value each).
+__device__ __forceinline__ uint32_t block_scan256(uint32_t c, uint32_t* warp_sums) {
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    uint32_t incl = c;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const uint32_t o = __shfl_up_sync(0xFFFFFFFFu, incl, off);
+        if (lane >= (uint32_t)off) incl += o;
+    }
+    if (lane == 31u) warp_sums[warp] = incl;
+    __syncthreads();
+    uint32_t before = 0;
+    for (uint32_t w = 0; w < warp; w++) before += warp_sums[w];
+    return before + incl - c;
+}
+
+// Block b: the digit counts of pass b -> each digit's first output position.
+__global__ void __launch_bounds__(256) k_onesweep_scan(OnesweepState* os) {
+    __shared__ uint32_t warp_sums[8];
+    const uint32_t d = threadIdx.x;
+    os->count[blockIdx.x][d] = block_scan256(os->count[blockIdx.x][d], warp_sums);
+}
+
+struct OnesweepShared {
+    uint32_t keys[kOsTile];
+    uint32_t vals[kOsTile];
+    uint32_t warp_cnt[kOsWarps][256];  // keys of each digit per warp, then each warp's offset among them
+    uint32_t tile_start[256];          // first position of each digit in the staged tile
+    uint32_t out_start[256];           // first output position of the tile's keys of each digit
+    uint32_t warp_sums[8];
+    uint32_t partition;
+};
+
+// One digit pass (bits pass*8 .. pass*8+7) over n keys: kin / vin -> kout / vout.
+// desc: this pass's descriptors, 256 per partition, zeroed.
+__global__ void __launch_bounds__(kOsThreads) k_onesweep_pass(const uint32_t* kin, const uint32_t* vin,
+                                                               uint32_t* kout, uint32_t* vout, uint32_t n, int pass,
+                                                               OnesweepState* os, uint32_t* desc,
+                                                               uint32_t* error) {
+    __shared__ OnesweepShared sm;
+    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    const int shift = pass * 8;
+    if (tid == 0) sm.partition = atomicAdd(&os->next_partition[pass], 1u);
+    for (uint32_t i = tid; i < kOsWarps * 256; i += kOsThreads) (&sm.warp_cnt[0][0])[i] = 0;
+    __syncthreads();
+    const uint32_t p = sm.partition;
+    const uint32_t base = p * kOsTile;
+    const uint32_t lt = (1u << lane) - 1u;
+    uint32_t key[kOsItems], val[kOsItems], rank[kOsItems];
+    // warp w ranks keys base + w*32*kOsItems .. in rounds of 32, in order: stable within the tile
+#pragma unroll
+    for (int r = 0; r < kOsItems; r++) {
+        const uint32_t idx = base + ((uint32_t)warp * kOsItems + r) * 32u + lane;
+        const bool valid = idx < n;
+        key[r] = valid ? kin[idx] : 0u;
+        val[r] = valid ? vin[idx] : 0u;
+        const uint32_t d = valid ? ((key[r] >> shift) & 255u) : 256u;
+        const uint32_t peers = __match_any_sync(0xFFFFFFFFu, d);
+        const uint32_t before = valid ? sm.warp_cnt[warp][d] : 0u;
+        __syncwarp();
+        if (valid && (peers & lt) == 0u) sm.warp_cnt[warp][d] = before + (uint32_t)__popc(peers);
+        __syncwarp();
+        rank[r] = valid ? before + (uint32_t)__popc(peers & lt) : 0xFFFFFFFFu;
+    }
+    __syncthreads();
+    // thread d: the tile's keys of digit d, and each warp's offset among them
+    const uint32_t d = tid;
+    uint32_t total = 0;
+    for (int w = 0; w < kOsWarps; w++) {
+        const uint32_t c = sm.warp_cnt[w][d];
+        sm.warp_cnt[w][d] = total;
+        total += c;
+    }
+    // publish, then look back for the keys of digit d in the earlier partitions
+    uint32_t* mine = desc + (size_t)p * 256u + d;
+    uint32_t excl = 0;
+    if (p == 0) {
+        st_relaxed(mine, kOsPrefix | total);
+    } else {
+        st_relaxed(mine, kOsAggregate | total);
+        uint32_t q = p - 1, spins = 0;
+        for (;;) {
+            const uint32_t v = ld_relaxed(desc + (size_t)q * 256u + d);
+            const uint32_t flag = v & ~kOsValue;
+            if (flag == 0u) {
+                if (++spins > kOsSpinLimit) {  // bounded: report and go on with what was found
+                    atomicOr(error, 1u << RT_ERR_TIMEOUT);
+                    break;
+                }
+                __nanosleep(32);
+                continue;
+            }
+            excl += v & kOsValue;
+            if (flag == kOsPrefix || q == 0u) break;
+            q--;
+        }
+        st_relaxed(mine, kOsPrefix | (excl + total));
+    }
+    sm.tile_start[d] = block_scan256(total, sm.warp_sums);
+    sm.out_start[d] = os->count[pass][d] + excl;
+    __syncthreads();
+    // stage the tile in digit order, then write it out in that order
+#pragma unroll
+    for (int r = 0; r < kOsItems; r++) {
+        if (rank[r] == 0xFFFFFFFFu) continue;
+        const uint32_t dg = (key[r] >> shift) & 255u;
+        const uint32_t local = sm.tile_start[dg] + sm.warp_cnt[warp][dg] + rank[r];
+        sm.keys[local] = key[r];
+        sm.vals[local] = val[r];
+    }
+    __syncthreads();
+    const uint32_t cnt = min(kOsTile, n - base);
+    for (uint32_t i = tid; i < cnt; i += kOsThreads) {
+        const uint32_t k = sm.keys[i];
+        const uint32_t dg = (k >> shift) & 255u;
+        const uint32_t pos = sm.out_start[dg] + (i - sm.tile_start[dg]);
+        if (pos < n) {
+            kout[pos] = k;
+            vout[pos] = sm.vals[i];
+        }
+    }
+}
+
+}  // namespace
+
+uint64_t key_sort_state_bytes(uint32_t n) {
+    return sizeof(OnesweepState) + (uint64_t)4 * onesweep_partitions(n ? n : 1) * 256u * 4u;
+}
+
+cudaError_t launch_key_sort(uint32_t* k0, uint32_t* v0, uint32_t* k1, uint32_t* v1, uint32_t n, uint8_t* state,
+                            uint32_t* error, cudaStream_t stream) {
+    if (n <= 1) return cudaSuccess;
+    if (n <= kSortTile) {
+        // one block sorts all four digits
+        note_launch(), k_radix_sort_small<<<1, kSortThreads, 0, stream>>>(k0, v0, k1, v1, n);
+        return cudaGetLastError();
+    }
+    OnesweepState* os = reinterpret_cast<OnesweepState*>(state);
+    uint32_t* desc = reinterpret_cast<uint32_t*>(state + sizeof(OnesweepState));
+    const uint32_t parts = onesweep_partitions(n);
+    cudaError_t e = cudaMemsetAsync(state, 0, key_sort_state_bytes(n), stream);
+    if (e != cudaSuccess) return e;
+    note_launch(), k_onesweep_hist<<<std::min<uint32_t>(parts, 1024u), kOsThreads, 0, stream>>>(k0, n, os);
+    note_launch(), k_onesweep_scan<<<4, 256, 0, stream>>>(os);
+    uint32_t* kin = k0;
+    uint32_t* vin = v0;
+    uint32_t* kout = k1;
+    uint32_t* vout = v1;
+    for (int pass = 0; pass < 4; pass++) {
+        note_launch(), k_onesweep_pass<<<parts, kOsThreads, 0, stream>>>(kin, vin, kout, vout, n, pass, os,
+                                                                          desc + (size_t)pass * parts * 256u, error);
+        std::swap(kin, kout);
+        std::swap(vin, vout);
+    }
+    return cudaGetLastError();
+}
+
+namespace {
 
 __global__ void k_gather_boxes(const float4* boxes, const uint32_t* vals, uint32_t n, float4* sboxes) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1735,7 +1925,7 @@ ScratchLayout ScratchLayout::make(uint32_t n, bool top, uint32_t build_flags) {
         o = align_up(o + bytes, 256);
         return r;
     };
-    s.sort_blocks = (uint32_t)((nn + kSortTile - 1) / kSortTile);
+    s.sort_blocks = onesweep_partitions((uint32_t)nn);
     s.state = take(sizeof(BuildState));
     s.boxes = take(nn * 32);
     s.sboxes = take(nn * 32);
@@ -1743,7 +1933,7 @@ ScratchLayout ScratchLayout::make(uint32_t n, bool top, uint32_t build_flags) {
     s.keys1 = take(nn * 4);
     s.vals0 = take(nn * 4);
     s.vals1 = take(nn * 4);
-    s.hist = take((uint64_t)256 * s.sort_blocks * 4);
+    s.hist = take(key_sort_state_bytes((uint32_t)nn));  // onesweep state + partition descriptors
     s.inodes = take(ni * 16);
     s.iboxes = take(ni * 32);
     s.iparent = take(ni * 4);
@@ -1813,21 +2003,12 @@ cudaError_t build_common(uint32_t n, bool top, uint32_t build_flags, uint32_t ge
         if (top) note_launch(), k_tlas_prims<<<blocks_for(n, T), T, 0, stream>>>(inst, n, boxes, temp, st);
         else note_launch(), k_blas_prims<<<blocks_for(n, T), T, 0, stream>>>(*blas, boxes, st);
         note_launch(), k_morton<<<blocks_for(n, T), T, 0, stream>>>(boxes, n, st, keys[0], vals[0]);
-        int cur = 0;
-        if (n > 1 && n <= kSortTile) {
-            // one block sorts all four digits; the result lands back in keys[0] / vals[0]
-            note_launch(), k_radix_sort_small<<<1, kSortThreads, 0, stream>>>(keys[0], vals[0], keys[1], vals[1], n);
-        } else if (n > 1) {
-            for (int pass = 0; pass < 4; pass++) {
-                int shift = pass * 8;
-                note_launch(), k_radix_hist<<<sl.sort_blocks, kSortThreads, 0, stream>>>(keys[cur], n, shift, hist, sl.sort_blocks);
-                note_launch(), k_scan_exclusive<<<1, 1024, 0, stream>>>(hist, 256u * sl.sort_blocks);
-                note_launch(), k_radix_scatter<<<sl.sort_blocks, kSortThreads, 0, stream>>>(keys[cur], vals[cur], keys[cur ^ 1],
-                                                                             vals[cur ^ 1], n, shift, hist,
-                                                                             sl.sort_blocks);
-                cur ^= 1;
-            }
-        }
+        // four stable digit passes: the sorted pairs land back in keys[0] / vals[0]
+        const int cur = 0;
+        if (cudaError_t e = launch_key_sort(keys[0], vals[0], keys[1], vals[1], n,
+                                            reinterpret_cast<uint8_t*>(hist), &st->error, stream);
+            e != cudaSuccess)
+            return e;
         note_launch(), k_gather_boxes<<<blocks_for(n, T), T, 0, stream>>>(boxes, vals[cur], n, sboxes);
         uint32_t* counts = nullptr;
         if (sl.ploc) {

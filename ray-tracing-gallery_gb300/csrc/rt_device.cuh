@@ -96,14 +96,18 @@ __host__ __device__ inline uint32_t node_meta(uint32_t m0, uint32_t m1, int c) {
 // k's planes are origin_a + q * s_a with q = qlo / qhi bytes.  The builder
 // puts origin on the quantum grid one quantum below the node's union box and
 // rounds every child plane outward to the grid with at least kQuantSlack of
-// a quantum to spare, so the decoded box contains the FP32 child box with
-// that margin (the traversal's fast decode and the FP32 node test together
-// err by under 0.2 of a quantum while the ray origin is within 2^19 quanta
-// of the node); an empty child is qlo = 255, qhi = 0 (never hit).
+// a quantum to spare, so the decoded box contains the padded FP32 child box
+// (the traversal's test of it is widened by a bound of its own rounding
+// error, so it is never narrower than the exact test of the decoded box); an
+// empty child is qlo = 255, qhi = 0 (never hit).
 // child_ref is as in WideNode.
 constexpr uint32_t kQNodeBytes = 96;
 constexpr float kQuantSlack = 0.25f;
-constexpr float kQuantFastLimit = 524288.0f;  // 2^19 quanta
+// Widening of the quantised slab test (rt_trace.cu, qnode_keys): each plane
+// distance moves out by kQuantMargin quanta, the entry / exit distances by
+// kQuantRelative of themselves (16 u, u = 2^-24).
+constexpr float kQuantMargin = 0.008f;
+constexpr float kQuantRelative = 9.5367431640625e-07f;
 struct alignas(16) QNode {
     float origin[3];
     uint8_t exp[3];

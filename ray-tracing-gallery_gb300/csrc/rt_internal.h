@@ -65,6 +65,15 @@ struct AsLayout {
 
 constexpr uint32_t kMaxPrimitives = (1u << 28) - 1;  // leaf refs carry 28 bits
 
+// The builder's key sort: n (key, value) pairs, stably by key (four 8-bit
+// digit passes; one block for small n, else the onesweep scheme).  The
+// result lands back in k0 / v0; k1 / v1 are the second buffers; `state` is
+// key_sort_state_bytes(n) of scratch; a bounded wait that gave up sets bit
+// RT_ERR_TIMEOUT in *error.
+uint64_t key_sort_state_bytes(uint32_t n);
+cudaError_t launch_key_sort(uint32_t* k0, uint32_t* v0, uint32_t* k1, uint32_t* v1, uint32_t n, uint8_t* state,
+                            uint32_t* error, cudaStream_t stream);
+
 cudaError_t launch_blas_build(const BlasInput& in, uint32_t build_flags, uint8_t* dst, uint8_t* scratch,
                               cudaStream_t stream);
 cudaError_t launch_tlas_build(const RtAccelerationStructureInstance* instances, uint32_t n, uint32_t build_flags,

@@ -294,9 +294,10 @@ __device__ __forceinline__ float qbyte(uint32_t w, int j) {
 }
 
 // Exact decode (plane = origin + q s is an exact float by construction; then
-// the FP32 node's arithmetic, so the test is at least as wide as the FP32
-// node's).  Used when the ray origin is more than 2^19 quanta from the node,
-// where the fast form could lose the slack the builder adds.
+// the FP32 node's arithmetic, which is conservative for those planes).  Only
+// used when a node's scale times the ray's inverse direction is outside
+// [2^-100, 2^100], where the fast form's products could underflow or
+// overflow.
 struct Keys8 {
     uint32_t k[8];
 };
@@ -322,16 +323,22 @@ __device__ __noinline__ Keys8 qnode_keys_exact(const uint8_t* node, float ox, fl
     return out;
 }
 
-// Slab tests of a quantised node.  With A = s inv and B = (origin - o) inv
-// per axis, plane t = q A + B = (1 + q 2^-15) (2^15 A) + (B - 2^15 A): one
-// PRMT and one FMA per plane.  The near / far byte words are fetched by the
-// ray's octant (s.oct) like the FP32 node's planes.  Error of the fast form
-// against exact arithmetic, in quanta, while |B| <= 2^19 |A|: 2^19 2^-23
-// from the two roundings of B, (2^19 + 2^15) 2^-24 from B - 2^15 A, about
-// 2^19 2^-24 from the final FMA and 255 2^-24 from A: under 0.128.  The
-// FP32 node test of the same plane errs by at most (2^19 + 256) 2^-23, under
-// 0.063.  The builder's slack (kQuantSlack = 0.25) covers both, so the fast
-// test is never narrower than the FP32 node's and the hits are identical.
+// Slab tests of a quantised node, conservative by an error bound.  Per axis,
+// with quantum s, A = s inv and B = (origin - o) inv, the plane of byte q is
+// at t = q A + B = (1 + q 2^-15) (2^15 A) + (B - 2^15 A): one PRMT (the byte
+// as the float 1 + q 2^-15) and one FMA per plane; the near / far byte words
+// are fetched by the ray's octant (s.oct) like the FP32 node's planes.
+// Against the exact slab distance (plane - o) / d, the computed t errs by at
+// most about 6u|t| + 0.004|A| (u = 2^-24: the reciprocal, the two roundings
+// of B, the rounding of B - 2^15 A and the final FMA, with |B - 2^15 A| <=
+// |t| + 33023|A|).  Each near plane is therefore lowered and each far plane
+// raised by 0.008|A| (folded into the constant term), and the combined entry
+// / exit distances are moved out by 16u of themselves before tmin / the
+// current hit distance bound them.  The test is thus never narrower than the
+// exact test of the quantised box, which contains the padded FP32 child box
+// (the builder rounds every plane outward): every child an FP32 traversal
+// would need is visited, so the hits are identical, whatever the distance
+// between the ray origin and the node.
 __device__ __forceinline__ void qnode_keys(const Trav& s, uint32_t entry, uint32_t keys[8], uint32_t refs[8]) {
     const uint8_t* node = reinterpret_cast<const uint8_t*>(s.nodes) + (size_t)entry * kQNodeBytes;
     const uint4* qp = reinterpret_cast<const uint4*>(node);
@@ -348,30 +355,31 @@ __device__ __forceinline__ void qnode_keys(const Trav& s, uint32_t entry, uint32
     const float Ax = __uint_as_float((h.w & 0xFFu) << 23) * s.inv.x;
     const float Ay = __uint_as_float(((h.w >> 8) & 0xFFu) << 23) * s.inv.y;
     const float Az = __uint_as_float(((h.w >> 16) & 0xFFu) << 23) * s.inv.z;
-    const float Bx = (__uint_as_float(h.x) - s.o.x) * s.inv.x;
-    const float By = (__uint_as_float(h.y) - s.o.y) * s.inv.y;
-    const float Bz = (__uint_as_float(h.z) - s.o.z) * s.inv.z;
-    const float lim = kQuantFastLimit, amin = 7.88860905e-31f;  // 2^-100
     const float ax = fabsf(Ax), ay = fabsf(Ay), az = fabsf(Az);
-    if (!(fabsf(Bx) <= lim * ax && fabsf(By) <= lim * ay && fabsf(Bz) <= lim * az && fmin3(ax, ay, az) >= amin)) {
+    if (!(fmin3(ax, ay, az) >= 7.88860905e-31f && fmax3(ax, ay, az) <= 1.26765060e30f)) {  // 2^-100, 2^100
         Keys8 kk = qnode_keys_exact(node, s.o.x, s.o.y, s.o.z, s.inv.x, s.inv.y, s.inv.z, s.tmin, s.t);
 #pragma unroll
         for (int k = 0; k < 8; k++) keys[k] = kk.k[k];
         return;
     }
+    const float Bx = (__uint_as_float(h.x) - s.o.x) * s.inv.x;
+    const float By = (__uint_as_float(h.y) - s.o.y) * s.inv.y;
+    const float Bz = (__uint_as_float(h.z) - s.o.z) * s.inv.z;
     const float Sx = Ax * 32768.0f, Sy = Ay * 32768.0f, Sz = Az * 32768.0f;
     const float Cx = fmaf(-32768.0f, Ax, Bx), Cy = fmaf(-32768.0f, Ay, By), Cz = fmaf(-32768.0f, Az, Bz);
-    const float tcap = s.t;
+    const float Nx = fmaf(-kQuantMargin, ax, Cx), Ny = fmaf(-kQuantMargin, ay, Cy), Nz = fmaf(-kQuantMargin, az, Cz);
+    const float Fx = fmaf(kQuantMargin, ax, Cx), Fy = fmaf(kQuantMargin, ay, Cy), Fz = fmaf(kQuantMargin, az, Cz);
+    const float tcap = s.t, tlo = s.tmin;
 #pragma unroll
     for (int k = 0; k < 8; k++) {
         const int j = k & 3;
         const uint32_t wnx = k < 4 ? nx.x : nx.y, wfx = k < 4 ? fx.x : fx.y;
         const uint32_t wny = k < 4 ? ny.x : ny.y, wfy = k < 4 ? fy.x : fy.y;
         const uint32_t wnz = k < 4 ? nz.x : nz.y, wfz = k < 4 ? fz.x : fz.y;
-        float tnx = fmaf(qbyte(wnx, j), Sx, Cx), tfx = fmaf(qbyte(wfx, j), Sx, Cx);
-        float tny = fmaf(qbyte(wny, j), Sy, Cy), tfy = fmaf(qbyte(wfy, j), Sy, Cy);
-        float tnz = fmaf(qbyte(wnz, j), Sz, Cz), tfz = fmaf(qbyte(wfz, j), Sz, Cz);
-        keys[k] = child_key(fmax3(fmaxf(tnx, s.tmin), tny, tnz), fmin3(fminf(tfx, tcap), tfy, tfz), refs[k], k);
+        const float tn = fmax3(fmaf(qbyte(wnx, j), Sx, Nx), fmaf(qbyte(wny, j), Sy, Ny), fmaf(qbyte(wnz, j), Sz, Nz));
+        const float tf = fmin3(fmaf(qbyte(wfx, j), Sx, Fx), fmaf(qbyte(wfy, j), Sy, Fy), fmaf(qbyte(wfz, j), Sz, Fz));
+        keys[k] = child_key(fmaxf(fmaf(-kQuantRelative, fabsf(tn), tn), tlo),
+                            fminf(fmaf(kQuantRelative, fabsf(tf), tf), tcap), refs[k], k);
     }
 }
 
