@@ -1581,10 +1581,16 @@ __global__ void k_write_insts(const InstRecord* temp, const uint32_t* vals, cons
 // Smallest biased exponent e (quantum s = 2^(e-127)) with ext <= 252 s and
 // |floor(L / s)| + 512 < 2^24, so that the grid origin (floor(L/s) - 1) s and
 // every decoded plane origin + q s (q <= 255) are exact floats.
-__device__ uint32_t quantum_exponent(float L, float ext) {
+// e_floor keeps a thin axis's quantum at least 2^-24 of the node's largest
+// extent: a flat node (a ground plane's, zero extent on one axis) would
+// otherwise get the smallest quantum there, whose scale times any ray's
+// inverse direction falls below the fast test's range, and every ray would
+// take the exact decode.  The box grows by a quarter of that quantum at most.
+__device__ uint32_t quantum_exponent(float L, float ext, uint32_t e_floor) {
     uint32_t e = (__float_as_uint(ext / 252.0f) >> 23) & 0xFFu;
     uint32_t el = (__float_as_uint(fabsf(L)) >> 23) & 0xFFu;
     e = max(e, el > 23u ? el - 23u : 1u);
+    e = max(e, e_floor);
     if (e < 1u) e = 1u;
     for (; e < 254u; e++) {
         float s = __uint_as_float(e << 23);
@@ -1620,6 +1626,11 @@ __global__ void k_quantize_nodes(const WideNode* in, const uint32_t* node_count,
     }
     uint8_t* qlo[3] = {q.qlo_x, q.qlo_y, q.qlo_z};
     uint8_t* qhi[3] = {q.qhi_x, q.qhi_y, q.qhi_z};
+    float mext = 0.0f;  // the node's largest extent
+    for (int a = 0; a < 3; a++)
+        if (L[a] <= H[a]) mext = fmaxf(mext, __fsub_ru(H[a], L[a]));
+    const uint32_t em = (__float_as_uint(mext) >> 23) & 0xFFu;
+    const uint32_t e_floor = em > 24u ? em - 24u : 1u;
     for (int a = 0; a < 3; a++) {
         if (!(L[a] <= H[a])) {  // no valid child: any grid, every child empty
             q.origin[a] = 0.0f;
@@ -1628,7 +1639,7 @@ __global__ void k_quantize_nodes(const WideNode* in, const uint32_t* node_count,
             continue;
         }
         float ext = __fsub_ru(H[a], L[a]);
-        uint32_t e = quantum_exponent(L[a], ext);
+        uint32_t e = quantum_exponent(L[a], ext, e_floor);
         float s = __uint_as_float(e << 23);
         float origin = (floorf(L[a] / s) - 1.0f) * s;
         q.origin[a] = origin;

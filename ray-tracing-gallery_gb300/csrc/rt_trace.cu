@@ -699,6 +699,44 @@ __device__ __forceinline__ uint32_t scene_of(const WfParams& P, uint32_t v) {
     return lo;
 }
 
+// Rays of a persistent shadow-ray launch: a warp takes RT_FETCH_CHUNK
+// consecutive list entries at a time from the launch's counter and its lanes
+// take their next rays from that chunk, so the rays one warp works on stay
+// neighbours in the list (the shadow rays of neighbouring pixels, which meet
+// the same instances).  Measured on the 64-scene batch: shadow launch 11.65
+// -> 10.38 ms with chunks of 128 (512: 10.85); the closest-hit lists keep the
+// whole-list counter (chunks made them 6 % slower).
+#ifndef RT_FETCH_CHUNK
+#define RT_FETCH_CHUNK 128
+#endif
+struct WarpChunk {
+    uint32_t next = 0, end = 0;  // the same in every lane of the warp
+    bool exhausted = false;
+};
+// All 32 lanes call it, converged.  Returns the list entry of a lane that
+// wants one, kNoItem if it gets none this time.
+__device__ __forceinline__ uint32_t chunk_fetch(WarpChunk& c, uint32_t* work, uint32_t total, bool want) {
+    const unsigned need = __ballot_sync(0xFFFFFFFFu, want);
+    if (need && c.next >= c.end && !c.exhausted) {
+        uint32_t base = 0;
+        if ((threadIdx.x & 31u) == 0u) base = atomicAdd(work, (uint32_t)RT_FETCH_CHUNK);
+        base = __shfl_sync(0xFFFFFFFFu, base, 0);
+        if (base >= total) {
+            c.exhausted = true;
+        } else {
+            c.next = base;
+            c.end = min(base + (uint32_t)RT_FETCH_CHUNK, total);
+        }
+    }
+    uint32_t it = kNoItem;
+    if (need && c.next < c.end) {
+        const uint32_t r = (uint32_t)__popc(need & lanemask_lt());
+        if (want && c.next + r < c.end) it = c.next + r;
+        c.next = min(c.next + (uint32_t)__popc(need), c.end);
+    }
+    return it;
+}
+
 // Warp-aggregated append of n items per lane; all 32 lanes must call it.
 __device__ __forceinline__ uint32_t warp_append_n(uint32_t* counter, uint32_t n) {
     const uint32_t lane = threadIdx.x & 31u;
@@ -869,8 +907,17 @@ __device__ __forceinline__ void trace_wavefront(const WfParams& P) {
     bool heat = false;
     uint32_t t0 = 0;  // clock() at the ray's start (heatmap only)
     uint32_t depth = 0;  // bits 0-7: depth of the ray being traced; 8-15: depth the slot started at
+    WarpChunk chunk;
     for (;;) {
-        uint32_t my = warp_append(work, item == kNoItem);
+        uint32_t my;
+        if (MODE == kModeShadow && RT_FETCH_CHUNK) {
+            const bool want = item == kNoItem;
+            if (__all_sync(0xFFFFFFFFu, want) && chunk.exhausted) break;
+            my = chunk_fetch(chunk, work, total, want);
+            if (want && my == kNoItem) continue;  // idle until the warp has a ray for it (or is done)
+        } else {
+            my = warp_append(work, item == kNoItem);
+        }
         if (item == kNoItem) {
             if (my >= total) break;
             item = my;
