@@ -699,19 +699,26 @@ __device__ __forceinline__ uint32_t scene_of(const WfParams& P, uint32_t v) {
     return lo;
 }
 
-// Rays of a persistent shadow-ray launch: a warp takes RT_FETCH_CHUNK
+// Rays of a persistent shadow-ray launch: a warp takes a chunk of
 // consecutive list entries at a time from the launch's counter and its lanes
 // take their next rays from that chunk, so the rays one warp works on stay
 // neighbours in the list (the shadow rays of neighbouring pixels, which meet
-// the same instances).  Measured on the 64-scene batch: shadow launch 11.65
-// -> 10.38 ms with chunks of 128 (512: 10.85); the closest-hit lists keep the
-// whole-list counter (chunks made them 6 % slower).
+// the same instances).  The chunk is RT_FETCH_CHUNK entries, less for short
+// lists (at least 32, and about 8 chunks per resident warp), so a small frame
+// still spreads over every warp.  Measured on the 64-scene batch: shadow
+// launch 11.65 -> 10.38 ms with chunks of 128 (512: 10.85); the closest-hit
+// lists keep the whole-list counter (chunks made them 6 % slower).
 #ifndef RT_FETCH_CHUNK
 #define RT_FETCH_CHUNK 128
 #endif
 struct WarpChunk {
     uint32_t next = 0, end = 0;  // the same in every lane of the warp
+    uint32_t size = 32;
     bool exhausted = false;
+    __device__ explicit WarpChunk(uint32_t total) {
+        const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+        size = min((uint32_t)RT_FETCH_CHUNK, max(32u, total / (8u * warps)));
+    }
 };
 // All 32 lanes call it, converged.  Returns the list entry of a lane that
 // wants one, kNoItem if it gets none this time.
@@ -719,13 +726,13 @@ __device__ __forceinline__ uint32_t chunk_fetch(WarpChunk& c, uint32_t* work, ui
     const unsigned need = __ballot_sync(0xFFFFFFFFu, want);
     if (need && c.next >= c.end && !c.exhausted) {
         uint32_t base = 0;
-        if ((threadIdx.x & 31u) == 0u) base = atomicAdd(work, (uint32_t)RT_FETCH_CHUNK);
+        if ((threadIdx.x & 31u) == 0u) base = atomicAdd(work, c.size);
         base = __shfl_sync(0xFFFFFFFFu, base, 0);
         if (base >= total) {
             c.exhausted = true;
         } else {
             c.next = base;
-            c.end = min(base + (uint32_t)RT_FETCH_CHUNK, total);
+            c.end = min(base + c.size, total);
         }
     }
     uint32_t it = kNoItem;
@@ -907,7 +914,7 @@ __device__ __forceinline__ void trace_wavefront(const WfParams& P) {
     bool heat = false;
     uint32_t t0 = 0;  // clock() at the ray's start (heatmap only)
     uint32_t depth = 0;  // bits 0-7: depth of the ray being traced; 8-15: depth the slot started at
-    WarpChunk chunk;
+    WarpChunk chunk(total);
     for (;;) {
         uint32_t my;
         if (MODE == kModeShadow && RT_FETCH_CHUNK) {
