@@ -118,13 +118,22 @@ __device__ void reduce_bounds(BuildState* st, const float cmin[3], const float c
             v[k] = is_min ? min(v[k], o) : max(v[k], o);
         }
     }
-    if ((threadIdx.x & 31) == 0) {
-        for (int k = 0; k < 3; k++) {
-            atomicMin(&st->cb[k], v[k]);
-            atomicMax(&st->cb[3 + k], v[3 + k]);
-            atomicMin(&st->bb[k], v[6 + k]);
-            atomicMax(&st->bb[3 + k], v[9 + k]);
-        }
+    // then over the block's warps, so that each block makes one atomic per
+    // bound (one per warp serialised ~82k same-address atomics per bound on a
+    // 2.6M-triangle build); every thread of the block must call this
+    __shared__ uint32_t s[32][12];
+    const uint32_t w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    if ((threadIdx.x & 31) == 0)
+        for (int k = 0; k < 12; k++) s[w][k] = v[k];
+    __syncthreads();
+    if (threadIdx.x < 12) {
+        const int k = threadIdx.x;
+        const bool is_min = (k < 3) || (k >= 6 && k < 9);
+        uint32_t r = s[0][k];
+        for (uint32_t j = 1; j < nw; j++) r = is_min ? min(r, s[j][k]) : max(r, s[j][k]);
+        uint32_t* dst = k < 6 ? &st->cb[k] : &st->bb[k - 6];
+        if (is_min) atomicMin(dst, r);
+        else atomicMax(dst, r);
     }
 }
 
@@ -1431,12 +1440,12 @@ __global__ void k_collapse_tail(CollapseCtx c, const uint4* fin) {
 __global__ void k_write_tris(const __grid_constant__ BlasInput in, const uint32_t* vals, const uint32_t* perm,
                              TriRecord* tris, BuildState* st) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= in.n) return;
-    uint32_t p = vals[min(perm[i], in.n - 1u)];
-    int g;
-    uint32_t prim;
+    const bool here = i < in.n;  // every thread takes part in the block's reductions below
+    uint32_t p = here ? vals[min(perm[i], in.n - 1u)] : 0u;
+    int g = 0;
+    uint32_t prim = 0;
     float v[3][3];
-    bool ok = fetch_triangle(in, p, &g, &prim, v);
+    bool ok = here && fetch_triangle(in, p, &g, &prim, v);
     if (!ok) {
         float qn = __int_as_float(0x7FC00000);
         for (int c = 0; c < 3; c++) v[c][0] = v[c][1] = v[c][2] = qn;
@@ -1449,12 +1458,14 @@ __global__ void k_write_tris(const __grid_constant__ BlasInput in, const uint32_
         float r = fmaxf(fmaxf(distance_ru(v[0], c), distance_ru(v[1], c)), distance_ru(v[2], c));
         rb = __float_as_uint(r);  // an overflow (+inf) turns the sphere off
     }
-    const unsigned active = __activemask();
-    rb = __reduce_max_sync(active, rb);
-    const bool leader = (threadIdx.x & 31u) == (uint32_t)(__ffs(active) - 1);
-    if (leader && rb) atomicMax(&st->radius_bits, rb);
-    // 14-DOP: extreme projections on the seven axes (sums of +-coordinates,
-    // rounded up for the maxima and down for the minima)
+    // the radius and the 14-DOP's extreme projections (sums of +-coordinates,
+    // rounded up for the maxima and down for the minima) are reduced over the
+    // warp, then over the block, and each block makes one atomic per value
+    __shared__ uint32_t red[32][15];  // [warp][radius, 7 maxima, 7 minima]
+    const uint32_t w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    const bool leader = (threadIdx.x & 31u) == 0u;
+    rb = __reduce_max_sync(0xFFFFFFFFu, rb);
+    if (leader) red[w][0] = rb;
     const bool valid = ok && finite3(v[0]) && finite3(v[1]) && finite3(v[2]);
 #pragma unroll
     for (int k = 0; k < 7; k++) {
@@ -1474,13 +1485,27 @@ __global__ void k_write_tris(const __grid_constant__ BlasInput in, const uint32_
             hi = f2o(ph);
             lo = f2o(pl);
         }
-        hi = __reduce_max_sync(active, hi);
-        lo = __reduce_min_sync(active, lo);
-        if (leader && hi != 0u) {  // some lane of the warp had a valid triangle
-            atomicMax(&st->dop_hi[k], hi);
-            atomicMin(&st->dop_lo[k], lo);
+        hi = __reduce_max_sync(0xFFFFFFFFu, hi);
+        lo = __reduce_min_sync(0xFFFFFFFFu, lo);
+        if (leader) {
+            red[w][1 + k] = hi;
+            red[w][8 + k] = lo;
         }
     }
+    __syncthreads();
+    if (threadIdx.x < 15) {
+        const int k = threadIdx.x;
+        uint32_t r = red[0][k];
+        for (uint32_t j = 1; j < nw; j++) r = k < 8 ? max(r, red[j][k]) : min(r, red[j][k]);
+        if (k == 0) {
+            if (r) atomicMax(&st->radius_bits, r);
+        } else if (k < 8) {
+            if (r != 0u) atomicMax(&st->dop_hi[k - 1], r);  // 0: no valid triangle in the block
+        } else if (r != 0xFFFFFFFFu) {
+            atomicMin(&st->dop_lo[k - 8], r);
+        }
+    }
+    if (!here) return;
     uint32_t flags = (in.g[g].flags & RT_GEOMETRY_OPAQUE) ? 1u : 0u;
     TriRecord r;
     r.v0 = make_float4(v[0][0], v[0][1], v[0][2], __uint_as_float(prim));

@@ -171,7 +171,6 @@ struct Trav {
     uint32_t c_inst, c_sbt_flags;  // the instance being traversed
     uint32_t steps;
     uint32_t scene;            // the ray's scene in a batched launch
-    uint32_t post;             // shadow rays: a BLAS leaf set aside for a later leaf phase (kNoEntry: none)
 };
 
 __device__ __forceinline__ void trav_begin(Trav& s, const Env& e, V3 o, V3 d, float tmin, float tmax) {
@@ -199,7 +198,6 @@ __device__ __forceinline__ void trav_begin(Trav& s, const Env& e, V3 o, V3 d, fl
     s.c_inst = 0;
     s.c_sbt_flags = 0;
     s.steps = 0;
-    s.post = kNoEntry;
     s.entry = (e.tnode_count == 0 || !(tmin <= tmax)) ? kNoEntry : 0u;  // 0 = TLAS root
 }
 
@@ -713,9 +711,7 @@ __device__ __forceinline__ uint32_t scene_of(const WfParams& P, uint32_t v) {
 #ifndef RT_FETCH_CHUNK
 #define RT_FETCH_CHUNK 128
 #endif
-#ifndef RT_SHADOW_POSTPONE
-#define RT_SHADOW_POSTPONE 0
-#endif
+
 struct WarpChunk {
     uint32_t next = 0, end = 0;  // the same in every lane of the warp
     uint32_t size = 32;
@@ -951,33 +947,7 @@ __device__ __forceinline__ void trace_wavefront(const WfParams& P) {
             heat = pix != kNoPixel && P.B.scenes[sc].uniforms->show_heatmap != 0;
             if (heat) t0 = (uint32_t)clock();
         }
-        int phase;
-        if (MODE == kModeShadow && RT_SHADOW_POSTPONE) {
-            // Any hit ends a shadow ray and the order of its steps does not
-            // matter, so a lane whose next step is a BLAS leaf sets it aside
-            // and steps the node below it on its stack, keeping node phases
-            // full; leaf phases then run the set-aside leaves first.
-            if (s.post == kNoEntry && s.in_blas && s.entry != kNoEntry && (s.entry & kLeafEntry) && s.sp > 0) {
-                const uint2 top = stack.get(s.sp - 1);
-                if (is_node_entry(top.x)) {
-                    s.post = s.entry;
-                    s.entry = top.x;
-                    s.sp--;
-                }
-            }
-            const unsigned act = __activemask();
-            const bool node = is_node_entry(s.entry);
-            const unsigned nm = __ballot_sync(act, node);
-            const unsigned lm = __ballot_sync(act, !node || s.post != kNoEntry);
-            phase = (nm == 0u || (uint32_t)__popc(lm) * 32u >= P.leaf_wait * (uint32_t)__popc(act)) ? 0 : 1;
-            if (phase == 0 && s.post != kNoEntry && s.sp < (int)kStackSize) {
-                stack.put(s.sp++, make_uint2(s.entry, 0u));  // back under the set-aside leaf
-                s.entry = s.post;
-                s.post = kNoEntry;
-            }
-        } else {
-            phase = node_phase(s.entry, P.leaf_wait) ? 1 : 0;
-        }
+        const int phase = node_phase(s.entry, P.leaf_wait) ? 1 : 0;
         if (!trav_step<STATS, KINDS>(s, stack, sv, &P.sbt, P.status, ray_flags, 0xFFu, sbt_offset, cnt, phase))
             continue;
         // the ray is finished
