@@ -145,6 +145,12 @@ uint32_t reverse_bits(uint32_t v, int n) {
     return r;
 }
 
+// Canonical Huffman decoding as RFC 1951 section 3.2.2 defines the codes
+// (codes of each length are consecutive integers, assigned in symbol order):
+// the slow path walks the lengths 1..15 keeping the first code and the first
+// symbol index of each length (the counting decode that zlib's
+// contrib/puff/puff.c also uses), and a kFast-bit table indexed by the
+// bit-reversed next bits resolves the short codes in one lookup.
 class Huffman {
 public:
     static constexpr int kFast = 10;

@@ -273,17 +273,29 @@ __device__ __forceinline__ void fnode_keys4(const Trav& s, float4 nx, float4 fx,
 // slots are tested (empty ones never hit): skipping children 4-7 of nodes
 // with at most four children measured slower than the branch saves, 4-wide
 // builds included.
-__device__ __forceinline__ void fnode_keys(const Trav& s, uint32_t entry, uint32_t keys[8], uint32_t refs[8]) {
-    const float4* np = reinterpret_cast<const float4*>(s.nodes + entry);
+// Node loads: read-only global loads, or plain loads of a copy the warp
+// staged in shared memory (packet traversal, RT_PACKET_STAGE).
+template <bool GLOBAL, class T>
+__device__ __forceinline__ T ldn(const T* p) {
+    if constexpr (GLOBAL) return __ldg(p);
+    else return *p;
+}
+
+template <bool GLOBAL = true>
+__device__ __forceinline__ void fnode_keys_at(const Trav& s, const float4* np, uint32_t keys[8], uint32_t refs[8]) {
     const uint32_t ox = s.oct & 0xFFu, oy = (s.oct >> 8) & 0xFFu, oz = s.oct >> 16;
-    const uint4 r0 = __ldg(reinterpret_cast<const uint4*>(np + 12));
-    const uint4 r1 = __ldg(reinterpret_cast<const uint4*>(np + 13));
-    const float4 nx0 = __ldg(np + ox), fx0 = __ldg(np + (ox ^ 2u)), ny0 = __ldg(np + oy), fy0 = __ldg(np + (oy ^ 2u));
-    const float4 nz0 = __ldg(np + oz), fz0 = __ldg(np + (oz ^ 2u));
-    const float4 nx1 = __ldg(np + ox + 1), fx1 = __ldg(np + (ox ^ 2u) + 1), ny1 = __ldg(np + oy + 1);
-    const float4 fy1 = __ldg(np + (oy ^ 2u) + 1), nz1 = __ldg(np + oz + 1), fz1 = __ldg(np + (oz ^ 2u) + 1);
+    const uint4 r0 = ldn<GLOBAL>(reinterpret_cast<const uint4*>(np + 12));
+    const uint4 r1 = ldn<GLOBAL>(reinterpret_cast<const uint4*>(np + 13));
+    const float4 nx0 = ldn<GLOBAL>(np + ox), fx0 = ldn<GLOBAL>(np + (ox ^ 2u)), ny0 = ldn<GLOBAL>(np + oy);
+    const float4 fy0 = ldn<GLOBAL>(np + (oy ^ 2u)), nz0 = ldn<GLOBAL>(np + oz), fz0 = ldn<GLOBAL>(np + (oz ^ 2u));
+    const float4 nx1 = ldn<GLOBAL>(np + ox + 1), fx1 = ldn<GLOBAL>(np + (ox ^ 2u) + 1), ny1 = ldn<GLOBAL>(np + oy + 1);
+    const float4 fy1 = ldn<GLOBAL>(np + (oy ^ 2u) + 1), nz1 = ldn<GLOBAL>(np + oz + 1);
+    const float4 fz1 = ldn<GLOBAL>(np + (oz ^ 2u) + 1);
     fnode_keys4(s, nx0, fx0, ny0, fy0, nz0, fz0, r0, 0, keys, refs);
     fnode_keys4(s, nx1, fx1, ny1, fy1, nz1, fz1, r1, 4, keys, refs);
+}
+__device__ __forceinline__ void fnode_keys(const Trav& s, uint32_t entry, uint32_t keys[8], uint32_t refs[8]) {
+    fnode_keys_at<true>(s, reinterpret_cast<const float4*>(s.nodes + entry), keys, refs);
 }
 
 // Byte j of w as the float 1 + q 2^-15: q lands in mantissa bits 8..15 of
@@ -339,17 +351,18 @@ __device__ __noinline__ Keys8 qnode_keys_exact(const uint8_t* node, float ox, fl
 // (the builder rounds every plane outward): every child an FP32 traversal
 // would need is visited, so the hits are identical, whatever the distance
 // between the ray origin and the node.
-__device__ __forceinline__ void qnode_keys(const Trav& s, uint32_t entry, uint32_t keys[8], uint32_t refs[8]) {
-    const uint8_t* node = reinterpret_cast<const uint8_t*>(s.nodes) + (size_t)entry * kQNodeBytes;
+template <bool GLOBAL = true>
+__device__ __forceinline__ void qnode_keys_at(const Trav& s, const uint8_t* node, uint32_t keys[8],
+                                              uint32_t refs[8]) {
     const uint4* qp = reinterpret_cast<const uint4*>(node);
     const uint2* q2 = reinterpret_cast<const uint2*>(node);
-    uint4 h = __ldg(qp), r0 = __ldg(qp + 1), r1 = __ldg(qp + 2);
+    uint4 h = ldn<GLOBAL>(qp), r0 = ldn<GLOBAL>(qp + 1), r1 = ldn<GLOBAL>(qp + 2);
     // uint2 index of the near-plane words: qlo at 6 + 2a, qhi at 7 + 2a
     const uint32_t ix = 6u + ((s.oct & 0xFFu) >> 1), iy = 6u + (((s.oct >> 8) & 0xFFu) >> 1),
                    iz = 6u + ((s.oct >> 16) >> 1);
-    uint2 nx = __ldg(q2 + ix), fx = __ldg(q2 + (ix ^ 1u));
-    uint2 ny = __ldg(q2 + iy), fy = __ldg(q2 + (iy ^ 1u));
-    uint2 nz = __ldg(q2 + iz), fz = __ldg(q2 + (iz ^ 1u));
+    uint2 nx = ldn<GLOBAL>(q2 + ix), fx = ldn<GLOBAL>(q2 + (ix ^ 1u));
+    uint2 ny = ldn<GLOBAL>(q2 + iy), fy = ldn<GLOBAL>(q2 + (iy ^ 1u));
+    uint2 nz = ldn<GLOBAL>(q2 + iz), fz = ldn<GLOBAL>(q2 + (iz ^ 1u));
     refs[0] = r0.x; refs[1] = r0.y; refs[2] = r0.z; refs[3] = r0.w;
     refs[4] = r1.x; refs[5] = r1.y; refs[6] = r1.z; refs[7] = r1.w;
     const float Ax = __uint_as_float((h.w & 0xFFu) << 23) * s.inv.x;
@@ -381,6 +394,9 @@ __device__ __forceinline__ void qnode_keys(const Trav& s, uint32_t entry, uint32
         keys[k] = child_key(fmaxf(fmaf(-kQuantRelative, fabsf(tn), tn), tlo),
                             fminf(fmaf(kQuantRelative, fabsf(tf), tf), tcap), refs[k], k);
     }
+}
+__device__ __forceinline__ void qnode_keys(const Trav& s, uint32_t entry, uint32_t keys[8], uint32_t refs[8]) {
+    qnode_keys_at<true>(s, reinterpret_cast<const uint8_t*>(s.nodes) + (size_t)entry * kQNodeBytes, keys, refs);
 }
 
 // (inst, geom, prim) below the best hit's, comparing caller instance indices
@@ -711,6 +727,11 @@ __device__ __forceinline__ uint32_t scene_of(const WfParams& P, uint32_t v) {
 #ifndef RT_FETCH_CHUNK
 #define RT_FETCH_CHUNK 128
 #endif
+// Packet traversal: each node is staged through shared memory by the
+// sub-packet (1) or read by every lane from global memory (0).
+#ifndef RT_PACKET_STAGE
+#define RT_PACKET_STAGE 0
+#endif
 
 struct WarpChunk {
     uint32_t next = 0, end = 0;  // the same in every lane of the warp
@@ -1019,9 +1040,10 @@ __global__ void __launch_bounds__(BLOCK, trace_warps_per_sm(KINDS) * 32 / BLOCK)
 // Traverses the sub-packet `act` (the calling lanes, converged, one scene,
 // each at the TLAS root).  ws: the warp's stack (kStackSize entries).
 template <bool STATS, uint32_t KINDS>
-__device__ __forceinline__ void packet_traverse(Trav& s, uint2* ws, const unsigned act, const SceneTable& sv,
-                                                const RtShaderBindingTable* sbt, uint32_t* status,
-                                                uint32_t ray_flags, uint32_t ray_sbt_offset, Counters& cnt) {
+__device__ __forceinline__ void packet_traverse(Trav& s, uint2* ws, float4* nb, const unsigned act,
+                                                const SceneTable& sv, const RtShaderBindingTable* sbt,
+                                                uint32_t* status, uint32_t ray_flags, uint32_t ray_sbt_offset,
+                                                Counters& cnt) {
     const bool any_hit = (ray_flags & RT_RAY_FLAG_TERMINATE_ON_FIRST_HIT) != 0u;
     const bool leader = (threadIdx.x & 31u) == (uint32_t)(__ffs(act) - 1);
     bool done = false;  // any-hit rays: an accepted hit ends the lane's part
@@ -1042,7 +1064,25 @@ __device__ __forceinline__ void packet_traverse(Trav& s, uint2* ws, const unsign
             } else {
                 if (STATS) cnt.nodes++;
                 uint32_t keys[8], refs[8];
-                if ((KINDS & kBlasKindQ8) && s.in_blas && (KINDS == kBlasKindQ8 || s.quant)) {
+                const bool qn = (KINDS & kBlasKindQ8) && s.in_blas && (KINDS == kBlasKindQ8 || s.quant);
+                if (RT_PACKET_STAGE) {
+                    // the sub-packet's lanes copy the node into the warp's buffer with one
+                    // 16-byte load each, then every lane reads its planes from there
+                    const float4* src = qn ? reinterpret_cast<const float4*>(reinterpret_cast<const uint8_t*>(s.nodes) +
+                                                                             (size_t)entry * kQNodeBytes)
+                                           : reinterpret_cast<const float4*>(s.nodes + entry);
+                    const uint32_t n16 = qn ? kQNodeBytes / 16u : kNodeBytes / 16u;
+                    const uint32_t r = (uint32_t)__popc(act & lanemask_lt()), na = (uint32_t)__popc(act);
+                    __syncwarp(act);  // every lane has read the previous node
+                    for (uint32_t q = r; q < n16; q += na) nb[q] = __ldg(src + q);
+                    __syncwarp(act);
+                    if (qn) {
+                        if (STATS) cnt.qnodes++;
+                        qnode_keys_at<false>(s, reinterpret_cast<const uint8_t*>(nb), keys, refs);
+                    } else {
+                        fnode_keys_at<false>(s, nb, keys, refs);
+                    }
+                } else if (qn) {
                     if (STATS) cnt.qnodes++;
                     qnode_keys(s, entry, keys, refs);
                 } else {
@@ -1145,6 +1185,7 @@ __device__ __forceinline__ void packet_traverse(Trav& s, uint2* ws, const unsign
 template <int MODE, bool STATS, uint32_t KINDS, int BLOCK, bool LANE_BOUNCES>
 __device__ __forceinline__ void trace_packets(const WfParams& P) {
     __shared__ uint2 stacks[BLOCK / 32][kStackSize];
+    __shared__ float4 nbuf[BLOCK / 32][RT_PACKET_STAGE ? kNodeBytes / 16 : 1];  // staged node per warp
     uint2* ws = stacks[threadIdx.x >> 5];
     const SceneTable sv{P.B.scenes};
     const uint32_t lane = threadIdx.x & 31u;
@@ -1201,7 +1242,8 @@ __device__ __forceinline__ void trace_packets(const WfParams& P) {
             pending &= ~act;
             bool cont = false;
             if ((act >> lane) & 1u) {
-                packet_traverse<STATS, KINDS>(s, ws, act, sv, &P.sbt, P.status, ray_flags, sbt_offset, cnt);
+                packet_traverse<STATS, KINDS>(s, ws, nbuf[threadIdx.x >> 5], act, sv, &P.sbt, P.status, ray_flags,
+                                              sbt_offset, cnt);
                 if (MODE == kModeBounce && LANE_BOUNCES) {
                     // every further bounce of the lane's ray, traced by the lane
                     // alone (the closest-hit program's arithmetic, bit for bit)
