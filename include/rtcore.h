@@ -360,9 +360,9 @@ RTCORE_API int32_t rt_cmd_build_blas(rt_ctx* ctx, const RtGeometryTriangles* geo
  * FP32 nodes only: RT_BUILD_QUANTIZED_NODES returns RT_ERR_UNSUPPORTED.
  * Limit: geometries whose rt_get_blas_build_sizes().build_scratch_size (with
  * the same flags) is above RT_STATIC_SCRATCH_BYTES are rejected with
- * RT_ERR_TOO_LARGE before anything is queued.  That is about 264k triangles
+ * RT_ERR_TOO_LARGE before anything is queued.  That is about 288k triangles
  * with RT_BUILD_PREFER_FAST_TRACE (its PLOC hierarchy needs more scratch)
- * and about 406k otherwise; the size query is the exact check.  Every call uses the same
+ * and about 462k otherwise; the size query is the exact check.  Every call uses the same
  * array, so calls whose GPU work can overlap (different streams with no
  * ordering between them) race and corrupt each other's builds; order them.
  * The first call on each device looks the array's device address up

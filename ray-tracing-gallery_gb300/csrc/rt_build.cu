@@ -16,9 +16,11 @@
 //      children or none can open; a subtree of <= leaf_max primitives is a
 //      leaf.  Each task carries the first position of its primitives in the
 //      final order; its children's primitives follow each other in slot
-//      order, and a leaf child writes its primitives' positions (perm).  The
-//      first kLevels wide levels run as one launch each, the rest as one
-//      depth-first task per thread.
+//      order, and a leaf child writes its primitives' positions (perm).
+//      Levels run breadth-first, one launch each: a task is stashed in its
+//      own (not yet written) wide-node slot, and the nodes one launch
+//      allocates are the next launch's tasks.  The levels past the launched
+//      ones run as one depth-first task per thread.
 //   6. primitive records written in that final order.
 // Everything runs on the caller's stream; no host synchronisation.
 //
@@ -40,8 +42,9 @@ namespace {
 
 constexpr uint32_t kNone = 0xFFFFFFFFu;
 constexpr uint32_t kLeafBit = 0x80000000u;
-constexpr int kLevels = 6;                     // wide levels built breadth-first
-constexpr uint32_t kFrontierCap = 1u << 18;    // 8^kLevels
+constexpr int kMinLevels = 6;   // wide levels built breadth-first (more for large n: collapse_levels)
+constexpr int kMaxLevels = 24;
+constexpr uint32_t kCollapseBlocks = 2432;  // 152 SMs x 16 blocks of 128 threads
 constexpr int kTailStack = 192;
 constexpr int kSortThreads = 256;
 constexpr int kSortItems = 8;
@@ -51,7 +54,8 @@ struct BuildState {
     uint32_t cb[6];   // centroid bounds, ordered-uint encoding: min xyz, max xyz
     uint32_t bb[6];   // primitive box bounds
     uint32_t node_counter;
-    uint32_t frontier_count[kLevels + 2];
+    uint32_t level_lo, level_hi;  // wide-node slots holding the current collapse level's tasks
+    uint32_t level_blocks_done;   // blocks of the current collapse launch that have finished
     uint32_t error;
     uint32_t depth;
     uint32_t blas_kinds;  // TLAS: kBlasKind* bits of the BLASes its instances enter
@@ -146,7 +150,8 @@ __global__ void k_init_state(BuildState* st) {
             st->bb[3 + k] = 0u;
         }
         st->node_counter = 1;
-        for (int k = 0; k < kLevels + 2; k++) st->frontier_count[k] = 0;
+        st->level_lo = st->level_hi = 0;
+        st->level_blocks_done = 0;
         st->error = 0;
         st->depth = 1;
         st->blas_kinds = 0;
@@ -1374,8 +1379,19 @@ __device__ void collapse_task(const CollapseCtx& c, uint32_t bref, uint32_t slot
     atomicMax(&c.st->depth, depth + 1);
 }
 
+// A collapse task waiting for its level: the binary node, the wide node's
+// depth and its first primitive position, stashed in the first 16 bytes of
+// the wide-node slot it will write (nothing else writes that slot before).
+__device__ __forceinline__ void stash_task(const CollapseCtx& c, uint32_t slot, uint32_t bref, uint32_t depth,
+                                           uint32_t first) {
+    *reinterpret_cast<uint4*>(&c.nodes[slot]) = make_uint4(bref, depth, first, 0u);
+}
+__device__ __forceinline__ uint4 stashed_task(const CollapseCtx& c, uint32_t slot) {
+    return *reinterpret_cast<const uint4*>(&c.nodes[slot]);
+}
+
 // Root wide node: a single leaf for n <= leaf_max, else the level-0 task.
-__global__ void k_collapse_root(CollapseCtx c, uint32_t n, uint4* frontier0) {
+__global__ void k_collapse_root(CollapseCtx c, uint32_t n) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     if (c.parents) c.parents[0] = kNone;
     if (n == 0 || n <= c.leaf_max) {
@@ -1395,31 +1411,48 @@ __global__ void k_collapse_root(CollapseCtx c, uint32_t n, uint4* frontier0) {
         write_node(&c.nodes[0], lo, hi, ref, meta, cnt);
         return;
     }
-    frontier0[0] = make_uint4(0u, 0u, 0u, 0u);
-    c.st->frontier_count[0] = 1;
+    stash_task(c, 0, 0u, 0u, 0u);
+    c.st->level_lo = 0;
+    c.st->level_hi = 1;
 }
 
-__global__ void k_collapse_level(CollapseCtx c, int level, const uint4* fin, uint4* fout) {
-    uint32_t count = c.st->frontier_count[level];
-    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < count; t += gridDim.x * blockDim.x) {
-        uint4 task = fin[t];
-        collapse_task(c, task.x, task.y, task.z, task.w, [&](uint32_t r, uint32_t s, uint32_t d, uint32_t f) {
-            uint32_t k = atomicAdd(&c.st->frontier_count[level + 1], 1u);
-            if (k < kFrontierCap) fout[k] = make_uint4(r, s, d, f);
-            else atomicOr(&c.st->error, 1u << RT_ERR_TOO_LARGE);
+// One breadth-first level: the tasks stashed in slots [level_lo, level_hi).
+// Every internal child gets the next slot from node_counter and its task is
+// stashed there, so the slots this launch allocates are the next level.  The
+// block that finishes last publishes that range (a count of finished blocks;
+// no block waits for another).
+__global__ void k_collapse_level(CollapseCtx c) {
+    const uint32_t lo = c.st->level_lo, hi = c.st->level_hi;
+    for (uint32_t t = lo + blockIdx.x * blockDim.x + threadIdx.x; t < hi; t += gridDim.x * blockDim.x) {
+        const uint4 task = stashed_task(c, t);
+        collapse_task(c, task.x, t, task.y, task.z, [&](uint32_t r, uint32_t s, uint32_t d, uint32_t f) {
+            stash_task(c, s, r, d, f);
         });
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(&c.st->level_blocks_done, 1u) == gridDim.x - 1) {
+            __threadfence();
+            const uint32_t allocated = atomicAdd(&c.st->node_counter, 0u);
+            c.st->level_lo = hi;
+            c.st->level_hi = min(allocated, c.max_nodes);
+            c.st->level_blocks_done = 0;
+        }
     }
 }
 
-__global__ void k_collapse_tail(CollapseCtx c, const uint4* fin) {
-    uint32_t count = c.st->frontier_count[kLevels];
-    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < count; t += gridDim.x * blockDim.x) {
+// The levels below the last breadth-first launch: each stashed task of the
+// last range is collapsed depth-first by one thread.
+__global__ void k_collapse_tail(CollapseCtx c) {
+    const uint32_t lo = c.st->level_lo, hi = c.st->level_hi;
+    for (uint32_t t = lo + blockIdx.x * blockDim.x + threadIdx.x; t < hi; t += gridDim.x * blockDim.x) {
         uint2 stack[kTailStack];
         uint2 dstack[kTailStack];   // depth, first primitive position
         int sp = 0;
-        uint4 task = fin[t];
-        stack[sp] = make_uint2(task.x, task.y);
-        dstack[sp++] = make_uint2(task.z, task.w);
+        const uint4 task = stashed_task(c, t);
+        stack[sp] = make_uint2(task.x, t);
+        dstack[sp++] = make_uint2(task.y, task.z);
         while (sp > 0) {
             --sp;
             uint2 e = stack[sp];
@@ -1908,6 +1941,13 @@ __global__ void k_as_copy(const uint8_t* src, uint8_t* dst, uint64_t dst_size, u
 }
 
 inline uint32_t blocks_for(uint64_t n, uint32_t t) { return (uint32_t)((n + t - 1) / t); }
+// Breadth-first collapse launches for n primitives: ceil(log8 n) wide levels
+// plus three for unbalanced trees; deeper subtrees finish depth-first.
+inline int collapse_levels(uint32_t n) {
+    int l = 0;
+    for (uint64_t c = 1; c < n; c *= 8) l++;
+    return std::min(std::max(l + 3, kMinLevels), kMaxLevels);
+}
 
 // PLOC hierarchy for builds that prefer trace speed (the reference's BLAS and
 // TLAS flags); the Karras LBVH for PREFER_FAST_BUILD or no preference, and
@@ -1975,9 +2015,6 @@ ScratchLayout ScratchLayout::make(uint32_t n, bool top, uint32_t build_flags) {
     s.iparent = take(ni * 4);
     s.lparent = take(nn * 4);
     s.flags = take(ni * 4);
-    uint64_t f = std::min<uint64_t>(kFrontierCap, cap);
-    s.frontier0 = take(f * 16);
-    s.frontier1 = take(f * 16);
     s.temp_inst = top ? take(nn * kInstBytes) : 0;
     s.fp32_nodes = quantized ? take(cap * kNodeBytes) : 0;
     s.perm = take(nn * 4);
@@ -2030,7 +2067,6 @@ cudaError_t build_common(uint32_t n, bool top, uint32_t build_flags, uint32_t ge
     uint32_t* iparent = reinterpret_cast<uint32_t*>(scratch + sl.iparent);
     uint32_t* lparent = reinterpret_cast<uint32_t*>(scratch + sl.lparent);
     uint32_t* flags = reinterpret_cast<uint32_t*>(scratch + sl.flags);
-    uint4* fr[2] = {reinterpret_cast<uint4*>(scratch + sl.frontier0), reinterpret_cast<uint4*>(scratch + sl.frontier1)};
     InstRecord* temp = top ? reinterpret_cast<InstRecord*>(scratch + sl.temp_inst) : nullptr;
     const uint32_t T = 256;
 
@@ -2102,16 +2138,19 @@ cudaError_t build_common(uint32_t n, bool top, uint32_t build_flags, uint32_t ge
         cc.width = node_width(build_flags);
         cc.max_nodes = al.max_nodes;
         cc.n = n;
-        note_launch(), k_collapse_root<<<1, 32, 0, stream>>>(cc, n, fr[0]);
+        note_launch(), k_collapse_root<<<1, 32, 0, stream>>>(cc, n);
         if (n > cc.leaf_max) {
+            // level lv holds at most 8^lv nodes: its grid covers that many tasks
+            // (grid-stride beyond kCollapseBlocks blocks)
+            const int levels = collapse_levels(n);
             uint64_t cap = 1;
-            for (int lv = 0; lv < kLevels; lv++) {
-                uint32_t g = blocks_for(std::min<uint64_t>(cap, al.max_nodes), 128);
-                note_launch(), k_collapse_level<<<g, 128, 0, stream>>>(cc, lv, fr[lv & 1], fr[(lv + 1) & 1]);
-                cap *= 8;
+            for (int lv = 0; lv < levels; lv++) {
+                const uint32_t g = blocks_for(std::min<uint64_t>(cap, (uint64_t)kCollapseBlocks * 128), 128);
+                note_launch(), k_collapse_level<<<g, 128, 0, stream>>>(cc);
+                cap = std::min<uint64_t>(cap * 8, al.max_nodes);
             }
-            uint32_t g = blocks_for(std::min<uint64_t>(kFrontierCap, al.max_nodes), 128);
-            note_launch(), k_collapse_tail<<<g, 128, 0, stream>>>(cc, fr[kLevels & 1]);
+            const uint32_t g = blocks_for(std::min<uint64_t>(al.max_nodes, (uint64_t)kCollapseBlocks * 128), 128);
+            note_launch(), k_collapse_tail<<<g, 128, 0, stream>>>(cc);
         }
         if (top) {
             note_launch(), k_write_insts<<<blocks_for(n, T), T, 0, stream>>>(temp, vals[cur], perm, n,
@@ -2131,7 +2170,7 @@ cudaError_t build_common(uint32_t n, bool top, uint32_t build_flags, uint32_t ge
         cc.width = node_width(build_flags);
         cc.max_nodes = al.max_nodes;
         cc.n = n;
-        note_launch(), k_collapse_root<<<1, 32, 0, stream>>>(cc, 0, fr[0]);
+        note_launch(), k_collapse_root<<<1, 32, 0, stream>>>(cc, 0);
     }
     if (quantized) {
         uint32_t g = blocks_for(al.max_nodes, 128);

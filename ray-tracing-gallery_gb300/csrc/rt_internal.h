@@ -41,7 +41,7 @@ struct BlasInput {
 // Byte offsets of the build scratch regions for n primitives.
 struct ScratchLayout {
     uint64_t boxes, sboxes, keys0, keys1, vals0, vals1, hist, inodes, iboxes, iparent, lparent, flags;
-    uint64_t frontier0, frontier1, state, temp_inst, refit_counters;
+    uint64_t state, temp_inst, refit_counters;
     uint64_t fp32_nodes;       // quantised builds: FP32 nodes before quantisation
     uint64_t perm;             // final primitive order
     // PLOC builds (RT_BUILD_PREFER_FAST_TRACE): cluster refs / boxes (two

@@ -152,9 +152,8 @@ class AccelerationStructure:
     def device_address(self, device: Device | None = None) -> int:
         return self.buffer.data_ptr()
 
-    @classmethod
-    def build_blas(cls, device: Device, name: str, scratch: ScratchBuffer, geometries: list[GeometryDesc],
-                   flags: int = abi.RT_BUILD_PREFER_FAST_TRACE, stream=None) -> "AccelerationStructure":
+    @staticmethod
+    def _geometry_array(geometries: list[GeometryDesc]):
         arr = (abi.RtGeometryTriangles * max(len(geometries), 1))()
         for i, g in enumerate(geometries):
             arr[i].vertex_address = g.position_buffer_address
@@ -163,6 +162,12 @@ class AccelerationStructure:
             arr[i].max_vertex = max(g.num_vertices - 1, 0)
             arr[i].primitive_count = g.num_indices // 3
             arr[i].flags = abi.RT_GEOMETRY_OPAQUE if g.opaque else 0
+        return arr
+
+    @classmethod
+    def build_blas(cls, device: Device, name: str, scratch: ScratchBuffer, geometries: list[GeometryDesc],
+                   flags: int = abi.RT_BUILD_PREFER_FAST_TRACE, stream=None) -> "AccelerationStructure":
+        arr = cls._geometry_array(geometries)
         sizes = abi.RtBuildSizes()
         device.check(device.lib.rt_get_blas_build_sizes(arr, len(geometries), flags, C.byref(sizes)))
         scr = scratch.ensure_size_of(sizes.build_scratch_size)
@@ -171,6 +176,17 @@ class AccelerationStructure:
                                                   sizes.acceleration_structure_size, scr, scratch.size,
                                                   Device.stream_handle(stream)))
         return cls(buf, sizes.acceleration_structure_size, flags, cls.BOTTOM_LEVEL, name)
+
+    def rebuild_blas(self, device: Device, scratch: ScratchBuffer, geometries: list[GeometryDesc],
+                     stream=None) -> None:
+        """The same BLAS built again into its own memory (same geometries and
+        flags): the build's device work alone, with no upload or allocation."""
+        arr = self._geometry_array(geometries)
+        sizes = abi.RtBuildSizes()
+        device.check(device.lib.rt_get_blas_build_sizes(arr, len(geometries), self.flags, C.byref(sizes)))
+        scr = scratch.ensure_size_of(sizes.build_scratch_size)
+        device.check(device.lib.rt_cmd_build_blas(device.ctx, arr, len(geometries), self.flags, self.buffer.data_ptr(),
+                                                  self.size, scr, scratch.size, Device.stream_handle(stream)))
 
     @classmethod
     def build_tlas(cls, device: Device, instances, num_instances: int, scratch: ScratchBuffer,
@@ -238,6 +254,7 @@ class GpuModel:
                                       len(model.positions), g.opaque))
             infos[i] = (ib.data_ptr(), g.diffuse_image, g.metallic_roughness_image, g.normal_map_image, 0)
         self.geometry_info_buffer = Device.upload(infos)
+        self.geometries = geoms
         self.blas = AccelerationStructure.build_blas(device, f"{model.name} blas", scratch, geoms, build_flags,
                                                      stream)
 

@@ -347,6 +347,37 @@ def test_mid_size_mesh_bit_exact(device):
     assert (g["instance_id"] != 0xFFFFFFFF).mean() > 0.2
 
 
+@pytest.mark.parametrize("blas_flags", [abi.RT_BUILD_PREFER_FAST_BUILD, 0,
+                                        abi.RT_BUILD_PREFER_FAST_BUILD | abi.RT_BUILD_QUANTIZED_NODES],
+                         ids=["fast_build", "no_preference", "fast_build_quantized"])
+def test_karras_hierarchy_builds_bit_exact(device, blas_flags):
+    """BLASes and TLASes built without PREFER_FAST_TRACE take the Karras LBVH
+    hierarchy instead of PLOC: every hit of the three parity scenes and of the
+    655,360-triangle mesh is still bit-exact against the oracle, and a render
+    matches it within the radiance tolerance."""
+    host = _host()
+    tlas_flags = (blas_flags & ~abi.RT_BUILD_QUANTIZED_NODES) | abi.RT_BUILD_ALLOW_UPDATE
+    for name, make in SCENES.items():
+        sc = make()
+        gs = host.GpuScene(device, sc, blas_flags=blas_flags, tlas_flags=tlas_flags)
+        assert all(m.blas.info(device).build_flags & abi.RT_BUILD_PREFER_FAST_TRACE == 0 for m in gs.models)
+        o = O.OracleScene(sc)
+        rays = scenes.random_rays(20000, 37, 60.0 if name == "full" else 16.0)
+        rays["tmax"] = 1e4
+        _assert_hits_equal(host.trace_ray_buffer(device, gs, rays), o.trace(rays)[0], f"{name} karras")
+        img, rad, st = host.render(device, sc, radiance=True, gpu_scene=gs)
+        o_img, o_rad, o_st = o.render()
+        assert st["status"] == 0 and st["traversals"] == o_st["traversals"]
+        assert np.abs(rad - o_rad).max() <= RADIANCE_TOL
+    m = scenes.precision_mesh(level=7)
+    sc = scenes.single_mesh_scene(m)
+    gs = host.GpuScene(device, sc, blas_flags=blas_flags, tlas_flags=tlas_flags)
+    rays = scenes.random_rays(100000, 13, 30.0)
+    g = host.trace_ray_buffer(device, gs, rays, with_models=False)
+    _assert_hits_equal(g, O.OracleScene(sc).trace(rays, with_models=False)[0], "icosphere l7 karras")
+    assert (g["instance_id"] != 0xFFFFFFFF).mean() > 0.2
+
+
 def test_host_buffer_query_matches_device_query(device):
     """rt_trace_ray_buffer_host returns the same hits as
     rt_cmd_trace_ray_buffer: pinned buffers traced in place (chunk_rays 0),
