@@ -61,6 +61,7 @@ struct BuildState {
     uint32_t blas_kinds;  // TLAS: kBlasKind* bits of the BLASes its instances enter
     uint32_t ploc_count[2];  // PLOC clusters entering the round (double-buffered by round parity)
     uint32_t merge_counter;  // PLOC merges so far (internal node ids count down from n - 2)
+    uint32_t ploc_blocks_done;  // blocks of the current merge launch that have finished
     uint32_t radius_bits;    // BLAS: largest vertex distance from the bounds centre (float bits, rounded up)
     uint32_t dop_hi[7], dop_lo[7];  // BLAS: largest / smallest vertex projection on each 14-DOP axis (ordered uint)
 };
@@ -157,6 +158,7 @@ __global__ void k_init_state(BuildState* st) {
         st->blas_kinds = 0;
         st->ploc_count[0] = st->ploc_count[1] = 0;
         st->merge_counter = 0;
+        st->ploc_blocks_done = 0;
         st->radius_bits = 0;
         for (int k = 0; k < 7; k++) {
             st->dop_hi[k] = 0u;
@@ -409,19 +411,19 @@ __global__ void k_morton(const float4* boxes, uint32_t n, const BuildState* st, 
     vals[i] = i;
 }
 
-// ---- radix sort -----------------------------------------------------------
-// Exclusive scan of m values by one block of 1024 threads.
-__global__ void __launch_bounds__(1024) k_scan_exclusive(uint32_t* data, uint32_t m) {
-    __shared__ uint32_t warp_sums[32];
-    uint32_t per = (m + 1023) / 1024;
-    uint32_t b = threadIdx.x * per, e = min(m, b + per);
+// Exclusive scan of m values in place by one block of 1024 threads (all of
+// them call it); returns the total to every thread.  Values are read through
+// L2: other blocks of the same launch may have written them.
+__device__ uint32_t block_exclusive_scan(uint32_t* data, uint32_t m, uint32_t* warp_sums) {
+    const uint32_t per = (m + 1023) / 1024;
+    const uint32_t b = threadIdx.x * per, e = min(m, b + per);
     uint32_t sum = 0;
-    for (uint32_t i = b; i < e; i++) sum += data[i];
-    uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (uint32_t i = b; i < e; i++) sum += __ldcg(&data[i]);
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     uint32_t incl = sum;
     for (int off = 1; off < 32; off <<= 1) {
         uint32_t o = __shfl_up_sync(0xFFFFFFFFu, incl, off);
-        if (lane >= off) incl += o;
+        if (lane >= (uint32_t)off) incl += o;
     }
     if (lane == 31) warp_sums[warp] = incl;
     __syncthreads();
@@ -430,17 +432,21 @@ __global__ void __launch_bounds__(1024) k_scan_exclusive(uint32_t* data, uint32_
         uint32_t wi = w;
         for (int off = 1; off < 32; off <<= 1) {
             uint32_t o = __shfl_up_sync(0xFFFFFFFFu, wi, off);
-            if (lane >= off) wi += o;
+            if (lane >= (uint32_t)off) wi += o;
         }
         warp_sums[lane] = wi - w;
+        if (lane == 31) warp_sums[32] = wi;
     }
     __syncthreads();
     uint32_t run = warp_sums[warp] + incl - sum;
     for (uint32_t i = b; i < e; i++) {
-        uint32_t v = data[i];
+        const uint32_t v = __ldcg(&data[i]);
         data[i] = run;
         run += v;
     }
+    const uint32_t total = warp_sums[32];
+    __syncthreads();
+    return total;
 }
 
 struct SortTileShared {
@@ -865,16 +871,6 @@ __device__ __forceinline__ float merged_half_area(float ax, float ay, float az, 
     return ex * ey + ey * ez + ez * ex;
 }
 
-// Internal node id of the next merge, or kNone past the n - 1 that exist.
-__device__ __forceinline__ uint32_t ploc_claim(BuildState* st, uint32_t n) {
-    uint32_t k = atomicAdd(&st->merge_counter, 1u);
-    if (k + 2u > n) {
-        atomicOr(&st->error, 1u << RT_ERR_BAD_AS);
-        return kNone;
-    }
-    return n - 2u - k;
-}
-
 __device__ __forceinline__ uint32_t ploc_size(const uint32_t* counts, uint32_t r) {
     return (r & kLeafBit) ? 1u : __ldcg(&counts[r]);
 }
@@ -888,38 +884,64 @@ __global__ void k_ploc_init(const float4* sboxes, uint32_t n, uint32_t* cref, fl
     cbox[2 * (size_t)i + 1] = sboxes[2 * (size_t)i + 1];
 }
 
+// Nearest neighbour of every cluster within kPlocRadius positions (smallest
+// merged-box surface area, the lower position on ties).  The area of a pair
+// does not depend on the order of its boxes (min / max per axis), so each pair
+// is evaluated once: a block stages kPlocChunk clusters' boxes plus the halo in
+// shared memory, every position p of [c0 - R, c0 + kPlocChunk) writes the
+// areas of (p, p + o) for o = 1..R, and then each cluster scans its candidates
+// in ascending position, the pairs below it first.
 __global__ void __launch_bounds__(kPlocChunk) k_ploc_nn(const float4* cbox, uint32_t* nn, const BuildState* st,
                                                           int round, int forced) {
     const uint32_t count = st->ploc_count[round & 1];
     if (count <= kPlocSmall) return;
-    __shared__ float4 slo[kPlocChunk + 2 * kPlocRadius], shi[kPlocChunk + 2 * kPlocRadius];
+    constexpr int R = kPlocRadius;
+    constexpr int kSpan = (int)kPlocChunk + R;  // positions whose forward pairs a tile needs
+    __shared__ float4 slo[kPlocChunk + 2 * R], shi[kPlocChunk + 2 * R];
+    __shared__ float area[R][kSpan];            // area[o - 1][p - (c0 - R)] = area of (p, p + o)
     for (uint32_t c0 = blockIdx.x * kPlocChunk; c0 < count; c0 += gridDim.x * kPlocChunk) {
-        for (uint32_t t = threadIdx.x; t < kPlocChunk + 2 * kPlocRadius; t += blockDim.x) {
-            int64_t g = (int64_t)c0 - kPlocRadius + t;
+        const uint32_t i = c0 + threadIdx.x;
+        if (forced) {  // pair rounds: neighbours are fixed pairs
+            if (i < count) nn[i] = (i ^ 1u) < count ? (i ^ 1u) : i;
+            continue;
+        }
+        for (uint32_t t = threadIdx.x; t < kPlocChunk + 2 * R; t += blockDim.x) {
+            const int64_t g = (int64_t)c0 - R + t;
             if (g >= 0 && g < (int64_t)count) {
                 slo[t] = __ldcg(&cbox[2 * g]);
                 shi[t] = __ldcg(&cbox[2 * g + 1]);
             }
         }
         __syncthreads();
-        const uint32_t i = c0 + threadIdx.x;
+        for (int lp = threadIdx.x; lp < kSpan; lp += blockDim.x) {
+            const int64_t gp = (int64_t)c0 - R + lp;
+            if (gp < 0 || gp >= (int64_t)count) continue;
+            const float4 a = slo[lp], b = shi[lp];
+#pragma unroll
+            for (int o = 1; o <= R; o++) {
+                const float4 c = slo[lp + o], d = shi[lp + o];
+                area[o - 1][lp] = merged_half_area(a.x, a.y, a.z, b.x, b.y, b.z, c.x, c.y, c.z, d.x, d.y, d.z);
+            }
+        }
+        __syncthreads();
         if (i < count) {
+            const int li = (int)threadIdx.x + R;
             uint32_t best = i;
-            if (forced) {
-                best = (i ^ 1u) < count ? (i ^ 1u) : i;
-            } else {
-                const int li = (int)threadIdx.x + kPlocRadius;
-                const float4 a = slo[li], b = shi[li];
-                float bd = INFINITY;
-                for (int o = -kPlocRadius; o <= kPlocRadius; o++) {
-                    int64_t j = (int64_t)i + o;
-                    if (o == 0 || j < 0 || j >= (int64_t)count) continue;
-                    const float4 c = slo[li + o], d = shi[li + o];
-                    float h = merged_half_area(a.x, a.y, a.z, b.x, b.y, b.z, c.x, c.y, c.z, d.x, d.y, d.z);
-                    if (h < bd) {  // ties keep the lower position
-                        bd = h;
-                        best = (uint32_t)j;
-                    }
+            float bd = INFINITY;
+            for (int o = R; o >= 1; o--) {  // candidates i - R .. i - 1
+                if ((int64_t)i - o < 0) continue;
+                const float h = area[o - 1][li - o];
+                if (h < bd) {  // ties keep the lower position
+                    bd = h;
+                    best = i - o;
+                }
+            }
+            for (int o = 1; o <= R; o++) {  // candidates i + 1 .. i + R
+                if (i + o >= count) break;
+                const float h = area[o - 1][li];
+                if (h < bd) {
+                    bd = h;
+                    best = i + o;
                 }
             }
             nn[i] = best;
@@ -928,75 +950,106 @@ __global__ void __launch_bounds__(kPlocChunk) k_ploc_nn(const float4* cbox, uint
     }
 }
 
-__global__ void k_ploc_merge(const uint32_t* cref, const float4* cbox, const uint32_t* nn, uint32_t* tref,
-                             float4* tbox, uint32_t* keep, uint4* inodes, float4* iboxes, uint32_t* counts,
-                             BuildState* st, int round, uint32_t n) {
+// One round's merges and the compaction offsets.  Block b takes tiles of
+// kPlocScanBlock clusters.  Cluster i merges with its nearest neighbour j
+// when j's nearest is i: the lower position keeps the new node, the higher
+// one drops out.  One scan per tile counts survivors (low 16 bits) and merges
+// (high 16 bits): the survivors' offsets go to scan and their total to blk,
+// and the tile claims its merges' node ids (counting down from n - 2) with
+// one atomic.  The block that finishes last turns the tile totals into tile
+// offsets and sets the next round's cluster count (a count of finished
+// blocks: no block waits for another).
+__global__ void __launch_bounds__(kPlocScanBlock) k_ploc_merge(
+    const uint32_t* cref, const float4* cbox, const uint32_t* nn, uint32_t* tref, float4* tbox, uint32_t* keep,
+    uint32_t* scan, uint32_t* blk, uint4* inodes, float4* iboxes, uint32_t* counts, BuildState* st, int round,
+    uint32_t n) {
     const uint32_t count = st->ploc_count[round & 1];
     if (count <= kPlocSmall) return;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
-        const uint32_t j = __ldcg(&nn[i]);
-        uint32_t r = __ldcg(&cref[i]);
-        float4 lo = __ldcg(&cbox[2 * (size_t)i]), hi = __ldcg(&cbox[2 * (size_t)i + 1]);
-        uint32_t k = 1u;
-        if (j != i && j < count && __ldcg(&nn[j]) == i) {
-            if (i < j) {
+    __shared__ uint32_t warp_sums[33];
+    __shared__ uint32_t tile_base, last;
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    const uint32_t tiles = (count + kPlocScanBlock - 1) / kPlocScanBlock;
+    for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+        const uint32_t i = tile * kPlocScanBlock + threadIdx.x;
+        const bool valid = i < count;
+        uint32_t r = 0u, k = 0u, j = i;
+        bool merging = false;
+        float4 lo = make_float4(0.f, 0.f, 0.f, 0.f), hi = lo;
+        if (valid) {
+            j = __ldcg(&nn[i]);
+            r = __ldcg(&cref[i]);
+            lo = __ldcg(&cbox[2 * (size_t)i]);
+            hi = __ldcg(&cbox[2 * (size_t)i + 1]);
+            k = 1u;
+            if (j != i && j < count && __ldcg(&nn[j]) == i) {
+                if (i < j) merging = true;
+                else k = 0u;
+            }
+        }
+        const uint32_t v = k | (merging ? 1u << 16 : 0u);
+        uint32_t incl = v;
+        for (int off = 1; off < 32; off <<= 1) {
+            const uint32_t o = __shfl_up_sync(0xFFFFFFFFu, incl, off);
+            if (lane >= (uint32_t)off) incl += o;
+        }
+        if (lane == 31u) warp_sums[warp] = incl;
+        __syncthreads();
+        if (warp == 0) {
+            const uint32_t w = warp_sums[lane];
+            uint32_t wi = w;
+            for (int off = 1; off < 32; off <<= 1) {
+                const uint32_t o = __shfl_up_sync(0xFFFFFFFFu, wi, off);
+                if (lane >= (uint32_t)off) wi += o;
+            }
+            warp_sums[lane] = wi - w;
+            if (lane == 31u) {
+                blk[tile] = wi & 0xFFFFu;
+                tile_base = (wi >> 16) ? atomicAdd(&st->merge_counter, wi >> 16) : 0u;
+            }
+        }
+        __syncthreads();
+        const uint32_t excl = warp_sums[warp] + incl - v;
+        if (merging) {
+            const uint32_t claim = tile_base + (excl >> 16);
+            if (claim + 2u > n) {  // more merges than a binary tree over n primitives has
+                atomicOr(&st->error, 1u << RT_ERR_BAD_AS);
+            } else {
+                const uint32_t id = n - 2u - claim;
                 const uint32_t rj = __ldcg(&cref[j]);
                 const float4 lj = __ldcg(&cbox[2 * (size_t)j]), hj = __ldcg(&cbox[2 * (size_t)j + 1]);
                 lo = make_float4(fminf(lo.x, lj.x), fminf(lo.y, lj.y), fminf(lo.z, lj.z), 0.0f);
                 hi = make_float4(fmaxf(hi.x, hj.x), fmaxf(hi.y, hj.y), fmaxf(hi.z, hj.z), 0.0f);
-                const uint32_t id = ploc_claim(st, n);
-                if (id != kNone) {
-                    inodes[id] = make_uint4(r, rj, 0u, 0u);
-                    iboxes[2 * (size_t)id] = lo;
-                    iboxes[2 * (size_t)id + 1] = hi;
-                    counts[id] = ploc_size(counts, r) + ploc_size(counts, rj);
-                    r = id;
-                }
-            } else {
-                k = 0u;
+                inodes[id] = make_uint4(r, rj, 0u, 0u);
+                iboxes[2 * (size_t)id] = lo;
+                iboxes[2 * (size_t)id + 1] = hi;
+                counts[id] = ploc_size(counts, r) + ploc_size(counts, rj);
+                r = id;
             }
         }
-        tref[i] = r;
-        tbox[2 * (size_t)i] = lo;
-        tbox[2 * (size_t)i + 1] = hi;
-        keep[i] = k;
-    }
-}
-
-// Exclusive scan of keep within each block of kPlocScanBlock clusters; the
-// block totals go to blk (scanned by k_scan_exclusive).
-__global__ void __launch_bounds__(kPlocScanBlock) k_ploc_block_scan(const uint32_t* keep, uint32_t* scan,
-                                                                     uint32_t* blk, const BuildState* st,
-                                                                     int round) {
-    const uint32_t count = st->ploc_count[round & 1];
-    __shared__ uint32_t warp_sums[32];
-    const uint32_t i = blockIdx.x * kPlocScanBlock + threadIdx.x;
-    if (count <= kPlocSmall || blockIdx.x * kPlocScanBlock >= count) {
-        if (threadIdx.x == 0) blk[blockIdx.x] = 0u;
-        return;
-    }
-    const uint32_t v = i < count ? __ldcg(&keep[i]) : 0u;
-    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-    uint32_t incl = v;
-    for (int off = 1; off < 32; off <<= 1) {
-        uint32_t o = __shfl_up_sync(0xFFFFFFFFu, incl, off);
-        if (lane >= (uint32_t)off) incl += o;
-    }
-    if (lane == 31u) warp_sums[warp] = incl;
-    __syncthreads();
-    if (warp == 0) {
-        uint32_t w = warp_sums[lane], wi = w;
-        for (int off = 1; off < 32; off <<= 1) {
-            uint32_t o = __shfl_up_sync(0xFFFFFFFFu, wi, off);
-            if (lane >= (uint32_t)off) wi += o;
+        if (valid) {
+            tref[i] = r;
+            tbox[2 * (size_t)i] = lo;
+            tbox[2 * (size_t)i + 1] = hi;
+            keep[i] = k;
+            scan[i] = excl & 0xFFFFu;
         }
-        warp_sums[lane] = wi - w;
-        if (lane == 31u) blk[blockIdx.x] = wi;
+        __syncthreads();
     }
+    __threadfence();
     __syncthreads();
-    if (i < count) scan[i] = warp_sums[warp] + incl - v;
+    if (threadIdx.x == 0) last = atomicAdd(&st->ploc_blocks_done, 1u) == gridDim.x - 1 ? 1u : 0u;
+    __syncthreads();
+    if (last) {
+        __threadfence();
+        const uint32_t total = block_exclusive_scan(blk, tiles, warp_sums);
+        if (threadIdx.x == 0) {
+            st->ploc_count[(round + 1) & 1] = total;
+            st->ploc_blocks_done = 0;
+        }
+    }
 }
 
+// Survivors to their compacted positions (tile offset + offset in the tile).
 __global__ void k_ploc_scatter(const uint32_t* tref, const float4* tbox, const uint32_t* keep, const uint32_t* scan,
                                const uint32_t* blk, uint32_t* cref, float4* cbox, BuildState* st, int round) {
     const uint32_t count = st->ploc_count[round & 1];
@@ -1012,7 +1065,6 @@ __global__ void k_ploc_scatter(const uint32_t* tref, const float4* tbox, const u
             cbox[2 * (size_t)pos] = __ldcg(&tbox[2 * (size_t)i]);
             cbox[2 * (size_t)pos + 1] = __ldcg(&tbox[2 * (size_t)i + 1]);
         }
-        if (i == count - 1u) st->ploc_count[(round + 1) & 1] = pos + k;
     }
 }
 
@@ -2096,18 +2148,18 @@ cudaError_t build_common(uint32_t n, bool top, uint32_t build_flags, uint32_t ge
             note_launch(), k_ploc_init<<<blocks_for(n, T), T, 0, stream>>>(sboxes, n, cref[0], cbox[0], st);
             int round = 0;
             if (n > kPlocSmall) {
-                // grid-wide rounds until kPlocSmall clusters remain (later rounds do nothing)
-                const uint32_t g = std::min<uint32_t>(blocks_for(n, kPlocChunk), 4096u);
-                const uint32_t nblk = blocks_for(n, kPlocScanBlock);
+                // grid-wide rounds until kPlocSmall clusters remain (later rounds
+                // do nothing); grids of at most one full SM load (152 SMs x 2048
+                // threads), grid-stride beyond
+                const uint32_t g = std::min<uint32_t>(blocks_for(n, kPlocChunk), 1216u);
+                const uint32_t gm = std::min<uint32_t>(blocks_for(n, kPlocScanBlock), 304u);
                 int nn_rounds = 0, pair_rounds = 0;
                 ploc_grid_rounds(n, &nn_rounds, &pair_rounds);
                 for (; round < nn_rounds + pair_rounds; round++) {
                     const int forced = round >= nn_rounds;
                     note_launch(), k_ploc_nn<<<g, kPlocChunk, 0, stream>>>(cbox[0], nnb, st, round, forced);
-                    note_launch(), k_ploc_merge<<<g, 256, 0, stream>>>(cref[0], cbox[0], nnb, cref[1], cbox[1], keep,
-                                                                      inodes, iboxes, counts, st, round, n);
-                    note_launch(), k_ploc_block_scan<<<nblk, kPlocScanBlock, 0, stream>>>(keep, scan, blk, st, round);
-                    note_launch(), k_scan_exclusive<<<1, 1024, 0, stream>>>(blk, nblk);
+                    note_launch(), k_ploc_merge<<<gm, kPlocScanBlock, 0, stream>>>(
+                        cref[0], cbox[0], nnb, cref[1], cbox[1], keep, scan, blk, inodes, iboxes, counts, st, round, n);
                     note_launch(), k_ploc_scatter<<<g, 256, 0, stream>>>(cref[1], cbox[1], keep, scan, blk, cref[0],
                                                                         cbox[0], st, round);
                 }
