@@ -47,6 +47,9 @@ constexpr int kMaxLevels = 24;
 constexpr uint32_t kCollapseBlocks = 2432;  // 152 SMs x 16 blocks of 128 threads
 constexpr int kTailStack = 192;
 constexpr int kSortThreads = 256;
+constexpr int kDopThreads = 32;
+constexpr int kDopTriples = 14 * 13 * 12 / 6;  // 364 plane triples of the 14-DOP
+constexpr int kDopBlocks = (kDopTriples + kDopThreads - 1) / kDopThreads;
 constexpr int kSortItems = 8;
 constexpr uint32_t kSortTile = kSortThreads * kSortItems;
 
@@ -64,6 +67,9 @@ struct BuildState {
     uint32_t ploc_blocks_done;  // blocks of the current merge launch that have finished
     uint32_t radius_bits;    // BLAS: largest vertex distance from the bounds centre (float bits, rounded up)
     uint32_t dop_hi[7], dop_lo[7];  // BLAS: largest / smallest vertex projection on each 14-DOP axis (ordered uint)
+    uint32_t dop_blocks_done;       // blocks of k_dop_vertices that have finished
+    uint32_t dop_state[kDopTriples];  // 1: the triple's planes meet in a point of the 14-DOP
+    double dop_cand[kDopTriples][3];  // that point
 };
 
 // The seven 14-DOP axes (unnormalised): x, y, z and the four diagonals.
@@ -159,6 +165,7 @@ __global__ void k_init_state(BuildState* st) {
         st->ploc_count[0] = st->ploc_count[1] = 0;
         st->merge_counter = 0;
         st->ploc_blocks_done = 0;
+        st->dop_blocks_done = 0;
         st->radius_bits = 0;
         for (int k = 0; k < 7; k++) {
             st->dop_hi[k] = 0u;
@@ -1599,25 +1606,26 @@ __global__ void k_write_tris(const __grid_constant__ BlasInput in, const uint32_
     tris[i] = r;
 }
 
-// The 14-DOP's vertices (one block of kDopThreads): every triple of its 14
-// planes solved in double, kept when it satisfies all 14 (with a relative
-// tolerance), duplicates merged.  More than kDopMaxVertices distinct points
-// (only through rounding) or a non-finite projection leave the header's
-// dop_count at 0.  The vertices' float rounding (a few 1e-8 relative) is
-// covered by the instance box padding (1e-5 relative).
-constexpr int kDopThreads = 128;
-constexpr int kDopCandidates = 128;
-
-__global__ void __launch_bounds__(kDopThreads) k_dop_vertices(AsHeader* h, const BuildState* st) {
+// The 14-DOP's vertices: every triple of its 14 planes solved in double, one
+// thread per triple over kDopBlocks blocks (this part's FP64 rate makes one
+// SM take hundreds of microseconds for the 364 triples), kept when the point
+// satisfies all 14 planes (with a relative tolerance).  The block that
+// finishes last (a count of finished blocks: no block waits) merges
+// duplicates: a point within the tolerance of a point of an earlier triple is
+// dropped, and the rest are written in triple order.  More than
+// kDopMaxVertices distinct points (only through rounding) or a non-finite
+// projection leave the header's dop_count at 0.  The vertices' float rounding
+// (a few 1e-8 relative) is covered by the instance box padding (1e-5
+// relative).
+__global__ void __launch_bounds__(kDopThreads) k_dop_vertices(AsHeader* h, BuildState* st) {
     __shared__ double pn[14][3], ph[14];
-    __shared__ double cand[kDopCandidates][3];
-    __shared__ uint32_t ncand;
+    __shared__ double cand[kDopTriples][3];
+    __shared__ uint8_t state[kDopTriples];  // 0: no point, 1: point, 2: duplicate of an earlier point
     __shared__ bool ok;
-    const int t = threadIdx.x;
-    if (t == 0) {
-        ncand = 0;
+    __shared__ uint32_t last;
+    const int t = blockIdx.x * kDopThreads + threadIdx.x;
+    if (threadIdx.x == 0) {
         ok = true;
-        h->dop_count = 0;
         for (int k = 0; k < 7; k++) {
             const float hi = o2f(st->dop_hi[k]), lo = o2f(st->dop_lo[k]);
             if (!(lo <= hi) || !(fabsf(hi) <= FLT_MAX) || !(fabsf(lo) <= FLT_MAX)) ok = false;
@@ -1628,56 +1636,80 @@ __global__ void __launch_bounds__(kDopThreads) k_dop_vertices(AsHeader* h, const
             ph[2 * k] = (double)hi;
             ph[2 * k + 1] = -(double)lo;
         }
+        if (blockIdx.x == 0) h->dop_count = 0;
     }
     __syncthreads();
-    if (!ok) return;
+    if (!ok) return;  // the same in every block
     double scale = 1e-30;
     for (int j = 0; j < 14; j++) scale = fmax(scale, fabs(ph[j]));
-    int idx = 0;
-    for (int a = 0; a < 14; a++)
-        for (int b = a + 1; b < 14; b++)
-            for (int c = b + 1; c < 14; c++, idx++) {
-                if (idx % kDopThreads != t) continue;
-                // Cramer's rule on the rows pn[a], pn[b], pn[c]
-                const double* A = pn[a];
-                const double* B = pn[b];
-                const double* C = pn[c];
-                const double det = A[0] * (B[1] * C[2] - B[2] * C[1]) - A[1] * (B[0] * C[2] - B[2] * C[0]) +
-                                   A[2] * (B[0] * C[1] - B[1] * C[0]);
-                if (fabs(det) < 1e-9) continue;
-                const double x = (ph[a] * (B[1] * C[2] - B[2] * C[1]) - A[1] * (ph[b] * C[2] - B[2] * ph[c]) +
-                                  A[2] * (ph[b] * C[1] - B[1] * ph[c])) / det;
-                const double y = (A[0] * (ph[b] * C[2] - B[2] * ph[c]) - ph[a] * (B[0] * C[2] - B[2] * C[0]) +
-                                  A[2] * (B[0] * ph[c] - ph[b] * C[0])) / det;
-                const double z = (A[0] * (B[1] * ph[c] - ph[b] * C[1]) - A[1] * (B[0] * ph[c] - ph[b] * C[0]) +
-                                  ph[a] * (B[0] * C[1] - B[1] * C[0])) / det;
-                bool inside = true;
-                for (int j = 0; j < 14 && inside; j++)
-                    inside = pn[j][0] * x + pn[j][1] * y + pn[j][2] * z <= ph[j] + 1e-9 * scale;
-                if (!inside) continue;
-                const uint32_t s = atomicAdd(&ncand, 1u);
-                if (s < (uint32_t)kDopCandidates) {
-                    cand[s][0] = x;
-                    cand[s][1] = y;
-                    cand[s][2] = z;
+    if (t < kDopTriples) {
+        int a = 0, b = 1, c = 2;
+        for (int idx = 0; idx < t; idx++) {  // the t-th triple a < b < c in lexicographic order
+            if (++c == 14) {
+                if (++b == 13) {
+                    ++a;
+                    b = a + 1;
                 }
+                c = b + 1;
             }
+        }
+        uint32_t found = 0;
+        // Cramer's rule on the rows pn[a], pn[b], pn[c]
+        const double* A = pn[a];
+        const double* B = pn[b];
+        const double* C = pn[c];
+        const double det = A[0] * (B[1] * C[2] - B[2] * C[1]) - A[1] * (B[0] * C[2] - B[2] * C[0]) +
+                           A[2] * (B[0] * C[1] - B[1] * C[0]);
+        if (fabs(det) >= 1e-9) {
+            const double x = (ph[a] * (B[1] * C[2] - B[2] * C[1]) - A[1] * (ph[b] * C[2] - B[2] * ph[c]) +
+                              A[2] * (ph[b] * C[1] - B[1] * ph[c])) / det;
+            const double y = (A[0] * (ph[b] * C[2] - B[2] * ph[c]) - ph[a] * (B[0] * C[2] - B[2] * C[0]) +
+                              A[2] * (B[0] * ph[c] - ph[b] * C[0])) / det;
+            const double z = (A[0] * (B[1] * ph[c] - ph[b] * C[1]) - A[1] * (B[0] * ph[c] - ph[b] * C[0]) +
+                              ph[a] * (B[0] * C[1] - B[1] * C[0])) / det;
+            bool inside = true;
+            for (int j = 0; j < 14 && inside; j++)
+                inside = pn[j][0] * x + pn[j][1] * y + pn[j][2] * z <= ph[j] + 1e-9 * scale;
+            if (inside) {
+                st->dop_cand[t][0] = x;
+                st->dop_cand[t][1] = y;
+                st->dop_cand[t][2] = z;
+                found = 1;
+            }
+        }
+        st->dop_state[t] = found;
+    }
+    __threadfence();
     __syncthreads();
-    if (t != 0) return;
-    const uint32_t nc = min(ncand, (uint32_t)kDopCandidates);
-    if (ncand > (uint32_t)kDopCandidates || nc < 4u) return;
-    uint32_t nv = 0;
-    for (uint32_t i = 0; i < nc; i++) {
+    if (threadIdx.x == 0) last = atomicAdd(&st->dop_blocks_done, 1u) == gridDim.x - 1 ? 1u : 0u;
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    for (int i = threadIdx.x; i < kDopTriples; i += kDopThreads) {
+        state[i] = (uint8_t)__ldcg(&st->dop_state[i]);
+        if (state[i])
+            for (int a = 0; a < 3; a++) cand[i][a] = __ldcg(&st->dop_cand[i][a]);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < kDopTriples; i += kDopThreads) {
+        if (state[i] == 0) continue;
         bool dup = false;
-        for (uint32_t j = 0; j < i && !dup; j++)
-            dup = fabs(cand[i][0] - cand[j][0]) <= 1e-7 * scale && fabs(cand[i][1] - cand[j][1]) <= 1e-7 * scale &&
-                  fabs(cand[i][2] - cand[j][2]) <= 1e-7 * scale;
-        if (dup) continue;
+        for (int j = 0; j < i && !dup; j++)
+            dup = state[j] != 0 && fabs(cand[i][0] - cand[j][0]) <= 1e-7 * scale &&
+                  fabs(cand[i][1] - cand[j][1]) <= 1e-7 * scale && fabs(cand[i][2] - cand[j][2]) <= 1e-7 * scale;
+        if (dup) state[i] = 2;  // other threads only test state != 0, which this keeps
+    }
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    st->dop_blocks_done = 0;
+    uint32_t nv = 0;
+    for (int i = 0; i < kDopTriples; i++) {
+        if (state[i] != 1) continue;
         if (nv == kDopMaxVertices) return;  // more points than a 14-DOP has: leave it off
         for (int a = 0; a < 3; a++) h->dop_vertex[nv][a] = (float)cand[i][a];
         nv++;
     }
-    h->dop_count = nv;
+    if (nv >= 4u) h->dop_count = nv;
 }
 
 __global__ void k_write_insts(const InstRecord* temp, const uint32_t* vals, const uint32_t* perm, uint32_t n,
@@ -2211,7 +2243,7 @@ cudaError_t build_common(uint32_t n, bool top, uint32_t build_flags, uint32_t ge
             note_launch(), k_write_tris<<<blocks_for(n, T), T, 0, stream>>>(*blas, vals[cur], perm,
                                                                              reinterpret_cast<TriRecord*>(dst + al.prims),
                                                                              st);
-            note_launch(), k_dop_vertices<<<1, kDopThreads, 0, stream>>>(reinterpret_cast<AsHeader*>(dst), st);
+            note_launch(), k_dop_vertices<<<kDopBlocks, kDopThreads, 0, stream>>>(reinterpret_cast<AsHeader*>(dst), st);
         }
     } else {
         CollapseCtx cc{};
