@@ -47,9 +47,10 @@ constexpr int kMaxLevels = 24;
 constexpr uint32_t kCollapseBlocks = 2432;  // 152 SMs x 16 blocks of 128 threads
 constexpr int kTailStack = 192;
 constexpr int kSortThreads = 256;
-constexpr int kDopThreads = 32;
+constexpr int kDopThreads = 128;
 constexpr int kDopTriples = 14 * 13 * 12 / 6;  // 364 plane triples of the 14-DOP
 constexpr int kDopBlocks = (kDopTriples + kDopThreads - 1) / kDopThreads;
+constexpr int kDopPer = (kDopTriples + kDopThreads - 1) / kDopThreads;  // triples per thread when merging
 constexpr int kSortItems = 8;
 constexpr uint32_t kSortTile = kSortThreads * kSortItems;
 
@@ -1607,20 +1608,23 @@ __global__ void k_write_tris(const __grid_constant__ BlasInput in, const uint32_
 }
 
 // The 14-DOP's vertices: every triple of its 14 planes solved in double, one
-// thread per triple over kDopBlocks blocks (this part's FP64 rate makes one
-// SM take hundreds of microseconds for the 364 triples), kept when the point
-// satisfies all 14 planes (with a relative tolerance).  The block that
-// finishes last (a count of finished blocks: no block waits) merges
-// duplicates: a point within the tolerance of a point of an earlier triple is
-// dropped, and the rest are written in triple order.  More than
+// thread per triple over kDopBlocks blocks, kept when the point satisfies all
+// 14 planes (with a relative tolerance).  The block that finishes last (a
+// count of finished blocks: no block waits) gathers the points in triple
+// order and merges duplicates: a point within the tolerance of an earlier one
+// is dropped, one thread per point (a serial pass over all pairs in double
+// took hundreds of microseconds at this part's FP64 rate).  More than
 // kDopMaxVertices distinct points (only through rounding) or a non-finite
 // projection leave the header's dop_count at 0.  The vertices' float rounding
 // (a few 1e-8 relative) is covered by the instance box padding (1e-5
 // relative).
 __global__ void __launch_bounds__(kDopThreads) k_dop_vertices(AsHeader* h, BuildState* st) {
     __shared__ double pn[14][3], ph[14];
-    __shared__ double cand[kDopTriples][3];
-    __shared__ uint8_t state[kDopTriples];  // 0: no point, 1: point, 2: duplicate of an earlier point
+    __shared__ double cand[kDopTriples][3];  // the points found, in triple order (last block)
+    __shared__ float candf[kDopTriples][3];
+    __shared__ uint8_t dup[kDopTriples];      // 1: within the tolerance of an earlier point
+    __shared__ uint32_t warp_sums[kDopThreads / 32];
+    __shared__ uint32_t npts;
     __shared__ bool ok;
     __shared__ uint32_t last;
     const int t = blockIdx.x * kDopThreads + threadIdx.x;
@@ -1685,26 +1689,67 @@ __global__ void __launch_bounds__(kDopThreads) k_dop_vertices(AsHeader* h, Build
     __syncthreads();
     if (!last) return;
     __threadfence();
-    for (int i = threadIdx.x; i < kDopTriples; i += kDopThreads) {
-        state[i] = (uint8_t)__ldcg(&st->dop_state[i]);
-        if (state[i])
-            for (int a = 0; a < 3; a++) cand[i][a] = __ldcg(&st->dop_cand[i][a]);
+    // the points, in triple order (each thread takes kDopPer consecutive triples)
+    const int t0 = threadIdx.x * kDopPer;
+    uint32_t mine = 0;
+    for (int k = 0; k < kDopPer; k++)
+        if (t0 + k < kDopTriples && __ldcg(&st->dop_state[t0 + k])) mine++;
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    uint32_t incl = mine;
+    for (int off = 1; off < 32; off <<= 1) {
+        const uint32_t o = __shfl_up_sync(0xFFFFFFFFu, incl, off);
+        if (lane >= (uint32_t)off) incl += o;
+    }
+    if (lane == 31u) warp_sums[warp] = incl;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t run = 0;
+        for (uint32_t w = 0; w < kDopThreads / 32; w++) {
+            const uint32_t v = warp_sums[w];
+            warp_sums[w] = run;
+            run += v;
+        }
+        npts = run;
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < kDopTriples; i += kDopThreads) {
-        if (state[i] == 0) continue;
-        bool dup = false;
-        for (int j = 0; j < i && !dup; j++)
-            dup = state[j] != 0 && fabs(cand[i][0] - cand[j][0]) <= 1e-7 * scale &&
-                  fabs(cand[i][1] - cand[j][1]) <= 1e-7 * scale && fabs(cand[i][2] - cand[j][2]) <= 1e-7 * scale;
-        if (dup) state[i] = 2;  // other threads only test state != 0, which this keeps
+    uint32_t at = warp_sums[warp] + incl - mine;
+    for (int k = 0; k < kDopPer; k++) {
+        const int i = t0 + k;
+        if (i < kDopTriples && __ldcg(&st->dop_state[i])) {
+            for (int a = 0; a < 3; a++) {
+                cand[at][a] = __ldcg(&st->dop_cand[i][a]);
+                candf[at][a] = (float)cand[at][a];
+            }
+            dup[at] = 0;
+            at++;
+        }
+    }
+    __syncthreads();
+    // A pair is a duplicate when every coordinate differs by at most 1e-7
+    // scale (in double).  The float copies screen the pairs first: every
+    // coordinate is within scale (1 + 1e-9) (the axis planes bound it), so
+    // rounding to float moves a difference by at most 2^-23 scale, and a
+    // pair whose float difference exceeds 4e-7 scale cannot pass the double
+    // test.  Only the few pairs that pass the screen use the slow FP64 pipe.
+    const double tol = 1e-7 * scale;
+    const float tolf = 4e-7f * (float)scale;
+    for (uint32_t i = threadIdx.x; i < npts; i += kDopThreads) {
+        bool d = false;
+        for (uint32_t j = 0; j < i && !d; j++) {
+            if (fabsf(candf[i][0] - candf[j][0]) > tolf || fabsf(candf[i][1] - candf[j][1]) > tolf ||
+                fabsf(candf[i][2] - candf[j][2]) > tolf)
+                continue;
+            d = fabs(cand[i][0] - cand[j][0]) <= tol && fabs(cand[i][1] - cand[j][1]) <= tol &&
+                fabs(cand[i][2] - cand[j][2]) <= tol;
+        }
+        dup[i] = d ? 1 : 0;
     }
     __syncthreads();
     if (threadIdx.x != 0) return;
     st->dop_blocks_done = 0;
     uint32_t nv = 0;
-    for (int i = 0; i < kDopTriples; i++) {
-        if (state[i] != 1) continue;
+    for (uint32_t i = 0; i < npts; i++) {
+        if (dup[i]) continue;
         if (nv == kDopMaxVertices) return;  // more points than a 14-DOP has: leave it off
         for (int a = 0; a < 3; a++) h->dop_vertex[nv][a] = (float)cand[i][a];
         nv++;
