@@ -2070,11 +2070,12 @@ __global__ void k_as_copy(const uint8_t* src, uint8_t* dst, uint64_t dst_size, u
 }
 
 inline uint32_t blocks_for(uint64_t n, uint32_t t) { return (uint32_t)((n + t - 1) / t); }
-// Breadth-first collapse launches for n primitives: ceil(log8 n) wide levels
-// plus three for unbalanced trees; deeper subtrees finish depth-first.
-inline int collapse_levels(uint32_t n) {
+// Breadth-first collapse launches for n primitives and `width` children per
+// node: ceil(log_width n) wide levels plus three for unbalanced trees; deeper
+// subtrees finish depth-first.
+inline int collapse_levels(uint32_t n, uint32_t width) {
     int l = 0;
-    for (uint64_t c = 1; c < n; c *= 8) l++;
+    for (uint64_t c = 1; c < n; c *= width) l++;
     return std::min(std::max(l + 3, kMinLevels), kMaxLevels);
 }
 
@@ -2269,9 +2270,9 @@ cudaError_t build_common(uint32_t n, bool top, uint32_t build_flags, uint32_t ge
         cc.n = n;
         note_launch(), k_collapse_root<<<1, 32, 0, stream>>>(cc, n);
         if (n > cc.leaf_max) {
-            // level lv holds at most 8^lv nodes: its grid covers that many tasks
+            // level lv holds at most width^lv nodes: its grid covers 8^lv tasks
             // (grid-stride beyond kCollapseBlocks blocks)
-            const int levels = collapse_levels(n);
+            const int levels = collapse_levels(n, cc.width);
             uint64_t cap = 1;
             for (int lv = 0; lv < levels; lv++) {
                 const uint32_t g = blocks_for(std::min<uint64_t>(cap, (uint64_t)kCollapseBlocks * 128), 128);
