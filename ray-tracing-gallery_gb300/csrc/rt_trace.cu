@@ -69,12 +69,22 @@ constexpr int kMaxDepth = 64;
 // Resident warps per SM every trace kernel variant is compiled for (at most
 // 80 registers a thread); block size x blocks per SM = 24 warps.
 constexpr int kTraceWarpsPerSM = 24;
-// Kernels that decode only quantised BLAS nodes hold far fewer node registers
-// and run at 32 warps per SM (at most 64 registers a thread).
+// Kernels that decode only quantised BLAS nodes hold fewer node registers.
+// The ray-buffer query runs them at 32 warps per SM (at most 64 registers a
+// thread: random rays over a hierarchy larger than L2 want the most rays in
+// flight); the wavefront launches at 24 (80 registers, fewer spills: the
+// 64-scene batch's shadow launch 12.5 -> 12.1 ms; 20 and 28 warps were
+// slower).
 #ifndef RT_Q8_TRACE_WARPS
-#define RT_Q8_TRACE_WARPS 32
+#define RT_Q8_TRACE_WARPS 24
+#endif
+#ifndef RT_Q8_RAYBUF_WARPS
+#define RT_Q8_RAYBUF_WARPS 32
 #endif
 constexpr int trace_warps_per_sm(uint32_t kinds) { return kinds == kBlasKindQ8 ? RT_Q8_TRACE_WARPS : kTraceWarpsPerSM; }
+constexpr int raybuf_warps_per_sm(uint32_t kinds) {
+    return kinds == kBlasKindQ8 ? RT_Q8_RAYBUF_WARPS : kTraceWarpsPerSM;
+}
 
 constexpr int kModeBounce = 0;   // closest hit of a bounce list -> hit records
 constexpr int kModeShadow = 1;   // any hit of generated shadow rays -> lit counters
@@ -1526,7 +1536,7 @@ __device__ __forceinline__ void trace_ray_buffer(const RayBufferParams& P, const
 }
 
 template <bool STATS, uint32_t KINDS>
-__global__ void __launch_bounds__(kTraceThreads, trace_warps_per_sm(KINDS) * 32 / kTraceThreads)
+__global__ void __launch_bounds__(kTraceThreads, raybuf_warps_per_sm(KINDS) * 32 / kTraceThreads)
     k_trace_ray_buffer(const __grid_constant__ RayBufferParams P) {
     const Env e = make_env(P.L.tlas, P.L.push.model_info, P.L.textures, RT_MAX_BOUND_IMAGES, P.L.status);
     if (kinds_selected(P.L.kinds_built, e.blas_kinds, KINDS)) trace_ray_buffer<STATS, KINDS>(P, e);
