@@ -1310,7 +1310,9 @@ __device__ __forceinline__ void trace_packets(const WfParams& P) {
 // Packets hold the per-lane keys, the reduced keys and the child references
 // at once: the FP32 kernels run at 20 warps per SM (96 registers, 68-byte
 // spills instead of 288 at 80 registers; 1080p frame +0.8 %, 16 warps -1 %).
-// A 256-thread block cannot make 20 warps and keeps 24.
+// A 256-thread block cannot make 20 warps and keeps 24.  The quantised-only
+// packet kernels run at 32 warps (64 registers): 28, 24 and 20 warps made the
+// 64-scene batch's camera-ray launch slower (11.9 -> 12.3 / 12.6 / 12.7 ms).
 #ifndef RT_Q8_PACKET_WARPS
 #define RT_Q8_PACKET_WARPS 32
 #endif
