@@ -114,3 +114,36 @@ def test_null_and_alignment_rejected_before_launch(rtlib):
     assert rtlib.rt_get_acceleration_structure_device_address(4096) == 4096
     assert rtlib.rt_debug_eval(99, 0, 0, 0, None) == abi.RT_ERR_INVALID
     del s
+
+
+def _static_scratch_limit(rtlib, flags: int) -> int:
+    """Largest triangle count whose BLAS build scratch fits the library's
+    static scratch array (rt_cmd_build_blas_static_scratch), by the size query."""
+    def fits(n):
+        g = (abi.RtGeometryTriangles * 1)()
+        g[0].vertex_address = 4096
+        g[0].index_address = 8192
+        g[0].vertex_stride = 12
+        g[0].max_vertex = 3 * n
+        g[0].primitive_count = n
+        s = abi.RtBuildSizes()
+        assert rtlib.rt_get_blas_build_sizes(g, 1, flags, C.byref(s)) == abi.RT_OK
+        return s.build_scratch_size <= abi.RT_STATIC_SCRATCH_BYTES
+
+    lo, hi = 1, 4 << 20
+    while lo < hi:
+        mid = (lo + hi + 1) // 2
+        lo, hi = (mid, hi) if fits(mid) else (lo, mid - 1)
+    return lo
+
+
+def test_static_scratch_limits_match_the_documentation(rtlib):
+    """The triangle limits the header states for the allocation-free build
+    (about 288k with PREFER_FAST_TRACE, about 462k without) follow from the
+    size query, within 1 %."""
+    text = (ROOT / "include" / "rtcore.h").read_text()
+    assert "about 288k triangles" in text and "about 462k otherwise" in text
+    fast_trace = _static_scratch_limit(rtlib, abi.RT_BUILD_PREFER_FAST_TRACE)
+    plain = _static_scratch_limit(rtlib, 0)
+    assert abs(fast_trace - 288_000) <= 2_880, fast_trace
+    assert abs(plain - 462_000) <= 4_620, plain
